@@ -1,0 +1,287 @@
+/*
+ * ltpg.h — C ABI of the GB300 deterministic batch concurrency-control engine.
+ *
+ * The engine runs LTPG's three-phase protocol on one GPU:
+ *   1. execute + register: every operation of every transaction in a batch
+ *      records its TID (= position in the batch) as the minimum reader / writer
+ *      of the row it touches, and reads what it needs from the batch-start
+ *      snapshot;
+ *   2. check: a read conflicts (RAW) when a smaller TID registered a write of
+ *      its row, a write conflicts (WAR / WAW) when a smaller TID registered a
+ *      read / write of its row;
+ *   3. write-back: a transaction commits iff !WAW && (!RAW || !WAR), and the
+ *      writes of committed transactions are applied to the table image.
+ *
+ * The reference program exposes this path as three __global__ kernels plus two
+ * host classes that own the buffers; it has no library interface.  Each entry
+ * point below names the reference interface it replaces (paths are relative to
+ * the LTPG project root; TF = LTPG/TPCC-allopt-final, Y1 = LTPG/YCSB/1).
+ *
+ * Conventions: every call returns an int status (LTPG_OK = 0); on failure the
+ * message is available from ltpg_last_error(ctx).  No exception crosses the ABI.
+ * A context is driven by one host thread at a time, like the reference's epoch
+ * loop (TF/tp.cu:136-261).  Pointers named host_* are host memory; pinned memory
+ * from ltpg_host_alloc() makes the copies asynchronous.
+ */
+#ifndef LTPG_H
+#define LTPG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LTPG_OK 0
+#define LTPG_ERR_INVALID 1 /* bad argument or size                        */
+#define LTPG_ERR_CUDA 2    /* CUDA runtime error                           */
+#define LTPG_ERR_STATE 3   /* call out of order (no table, empty slot ...) */
+#define LTPG_ERR_NOMEM 4   /* device or host allocation failed             */
+#define LTPG_ERR_TIMEOUT 5 /* a bounded device wait gave up                */
+#define LTPG_ERR_BOUNDS 6  /* a key or index in a batch is out of range    */
+
+/* ---- workloads and run modes ------------------------------------------ */
+#define LTPG_WORKLOAD_YCSB 1
+#define LTPG_WORKLOAD_TPCC 2
+
+#define LTPG_MODE_PLAIN 0      /* three kernels, one per phase                  */
+#define LTPG_MODE_FUSED 1      /* tuned kernels: execute | check+write-back      */
+#define LTPG_MODE_PERSISTENT 2 /* one cooperative kernel, grid barriers         */
+#define LTPG_MODE_GRAPH 3      /* tuned kernels captured into a CUDA graph       */
+
+/* ---- per-transaction conflict flags (ltpg_txn_flags) ------------------- */
+#define LTPG_FLAG_RAW 0x1u
+#define LTPG_FLAG_WAR 0x2u
+#define LTPG_FLAG_WAW 0x4u
+#define LTPG_FLAG_COMMIT 0x8u
+
+/* ---- YCSB ----------------------------------------------------------------
+ * Table: n_records rows of 10 uint64 fields, row-major (80 B per row).
+ * Initial value of field f of key k = ltpg_hash3(seed, k, f).
+ * A batch holds n_txn transactions of ops_per_txn operations each; the op words
+ * of transaction t sit at ops[t * op_stride + j] (op_stride = ops_per_txn
+ * rounded up to 4, so every transaction starts on a 16-byte boundary); unused
+ * words hold LTPG_YCSB_OP_PAD.  Op word layout:
+ *   bit 31      1 = update, 0 = read
+ *   bits 27..30 field written by an update (0..9)
+ *   bits 0..26  key
+ * Updates carry their new values in vals[], in transaction/op order;
+ * val_off[t] is the index of transaction t's first value (val_off[n_txn] =
+ * number of updates).  Per-transaction result: sum over the reads j of
+ * (xor of the 10 fields of the row) * (2j + 1), mod 2^64, read from the
+ * batch-start image.
+ */
+#define LTPG_YCSB_FIELDS 10
+#define LTPG_YCSB_OP_PAD 0xFFFFFFFFu
+#define LTPG_YCSB_KEY_BITS 27
+#define LTPG_YCSB_MAX_OPS 32
+
+typedef struct {
+    uint32_t n_txn;
+    uint32_t ops_per_txn;
+    uint32_t op_stride;
+    uint32_t n_updates;
+    const uint32_t *ops;     /* n_txn * op_stride */
+    const uint32_t *val_off; /* n_txn + 1         */
+    const uint64_t *vals;    /* n_updates         */
+} ltpg_ycsb_batch;
+
+typedef struct {
+    uint64_t seed;
+    uint64_t n_records;    /* keys 0 .. n_records-1                      */
+    uint32_t n_txn;        /* transactions per batch                     */
+    uint32_t ops_per_txn;  /* distinct keys per transaction (<= 32)      */
+    uint32_t update_pct;   /* share of update operations, 0..100         */
+    uint32_t rotate_every; /* new hot-set permutation every R batches; 0 = key rank order */
+    double theta;          /* Zipf exponent, 0 = uniform                 */
+} ltpg_ycsb_params;
+
+/* ---- TPC-C ---------------------------------------------------------------
+ * Nine tables of uint64 columns, row-major.  Table ids and column counts:
+ */
+#define LTPG_T_WAREHOUSE 0 /*  9 cols, W rows            */
+#define LTPG_T_DISTRICT 1  /* 11 cols, 10 W rows         */
+#define LTPG_T_CUSTOMER 2  /* 21 cols, 30,000 W rows     */
+#define LTPG_T_HISTORY 3   /*  8 cols, 30,000 W rows     */
+#define LTPG_T_NEWORDER 4  /*  3 cols, 30,000 W rows     */
+#define LTPG_T_ORDER 5     /*  8 cols, 30,000 W rows     */
+#define LTPG_T_ORDERLINE 6 /* 10 cols, 450,000 W rows    */
+#define LTPG_T_STOCK 7     /* 17 cols, 100,000 W rows    */
+#define LTPG_T_ITEM 8      /*  5 cols, 100,000 rows      */
+#define LTPG_TPCC_TABLES 9
+
+#define LTPG_TPCC_NEWORDER 0
+#define LTPG_TPCC_PAYMENT 1
+#define LTPG_TPCC_MAX_LINES 15
+
+/* 32-byte transaction record.  kind_info: bits 0..7 kind, 8..15 order-line
+ * count, 16..23 district, 24..31 customer district (Payment).
+ * NewOrder: a = O_ID, b = NO_ID, c = first OL_ID.   Payment: a = H_ID,
+ * b/c = low/high 32 bits of the amount in cents (int64).
+ * line_off = number of order lines of all earlier transactions of the batch. */
+typedef struct {
+    uint32_t kind_info;
+    uint32_t w;
+    uint32_t c_w;
+    uint32_t c_id;
+    uint32_t a;
+    uint32_t b;
+    uint32_t c;
+    uint32_t line_off;
+} ltpg_tpcc_txn;
+
+typedef struct {
+    uint32_t i_id;
+    uint16_t supply_w;
+    uint16_t qty;
+} ltpg_tpcc_line;
+
+typedef struct {
+    uint32_t n_txn;
+    uint32_t n_lines;
+    uint64_t txn_base; /* global number of transaction 0 (O_ENTRY_D / H_DATE) */
+    const ltpg_tpcc_txn *txns;
+    const ltpg_tpcc_line *lines;
+} ltpg_tpcc_batch;
+
+typedef struct {
+    uint64_t seed;
+    uint32_t warehouses;
+    uint32_t n_txn;
+    uint32_t neworder_pct; /* share of NewOrder, rest Payment         */
+    uint32_t remote_line_pct; /* NewOrder remote supply, per line (1)  */
+    uint32_t remote_pay_pct;  /* Payment remote customer (15)          */
+} ltpg_tpcc_params;
+
+/* ---- engine context ---------------------------------------------------- */
+typedef struct ltpg_ctx ltpg_ctx;
+
+typedef struct {
+    int32_t device;
+    uint32_t n_slots;        /* device batch slots (>= 1)                    */
+    uint32_t max_txn;        /* capacity per slot, transactions              */
+    uint32_t max_ops_per_txn;/* YCSB capacity per transaction                */
+    uint32_t max_lines;      /* TPC-C capacity per slot, order lines         */
+    uint32_t flags;          /* LTPG_CFG_*                                   */
+} ltpg_config;
+
+/* The reference registers the NEW-ORDER insert as a read and never runs its
+ * WAR check (TF/Execute_neworder.h:115,639-646); that is the default here.
+ * With this flag the insert registers and checks as a write. */
+#define LTPG_CFG_STRICT_INSERT 0x1u
+
+typedef struct {
+    uint64_t n_txn;
+    uint64_t commits;
+    uint64_t raw;      /* transactions with a RAW conflict */
+    uint64_t war;
+    uint64_t waw;
+    uint64_t staged_ops;   /* registrations served from shared memory */
+    uint64_t total_ops;    /* registrations issued                    */
+} ltpg_batch_stats;
+
+/* Replaces: Database / YCSBDatabase constructors + Query constructors, which
+ * cudaMalloc every buffer (TF/Database.h:37-57, TF/Query.h:330-355,
+ * Y1/Database.h:27-39, Y1/Query.h:142-149). */
+int ltpg_create(const ltpg_config *cfg, ltpg_ctx **out);
+/* Replaces: the never-run destructors (TF/Database.h:59-77, TF/Query.h:356-376). */
+int ltpg_destroy(ltpg_ctx *ctx);
+const char *ltpg_last_error(const ltpg_ctx *ctx);
+/* Runs all device work of ctx on this stream (cudaStream_t; NULL = ctx's own). */
+int ltpg_set_stream(ltpg_ctx *ctx, void *stream);
+void *ltpg_get_stream(ltpg_ctx *ctx);
+int ltpg_sync(ltpg_ctx *ctx);
+
+/* Pinned host memory for fast copies (the reference's cudaMallocHost buffers,
+ * TF/Query.h:338-343). */
+void *ltpg_host_alloc(size_t bytes);
+void ltpg_host_free(void *p);
+
+/* ---- tables (Database.h surface) ---------------------------------------- */
+/* Replaces: YCSBDatabase + initial_ycsb_data (Y1/Database.h:27-131): build the
+ * table and load it into HBM. The image is generated on the device. */
+int ltpg_db_load_ycsb(ltpg_ctx *ctx, uint64_t seed, uint64_t n_records);
+/* Replaces: Database + initial_data (TF/Database.h:13-451). */
+int ltpg_db_load_tpcc(ltpg_ctx *ctx, uint64_t seed, uint32_t warehouses);
+/* Table ids for the calls below: LTPG_T_* for TPC-C, LTPG_TABLE_YCSB for YCSB. */
+#define LTPG_TABLE_YCSB 100
+/* Rows and columns (uint64 each) of a loaded table. */
+int ltpg_db_table_shape(ltpg_ctx *ctx, uint32_t table, uint64_t *rows, uint32_t *cols);
+/* H2D load of a host image / D2H download (the reference's cudaMemcpy of the
+ * SNAPSHOT, TF/Database.h:445-446).  bytes must equal rows * cols * 8. */
+int ltpg_db_upload(ltpg_ctx *ctx, uint32_t table, const void *host, size_t bytes);
+int ltpg_db_download(ltpg_ctx *ctx, uint32_t table, void *host, size_t bytes);
+
+/* ---- batches (Query.h surface) ------------------------------------------- */
+/* Deterministic generators.  Replace MakeYCSB / MakeNeworder / MakePayment and
+ * Query::initial_* (Y1/Query.h:18-117,161-188; TF/Query.h:16-212,478-525),
+ * whose output depends on rand() and thread timing. */
+typedef struct ltpg_gen ltpg_gen;
+int ltpg_gen_create_ycsb(const ltpg_ycsb_params *p, ltpg_gen **out);
+int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out);
+int ltpg_gen_destroy(ltpg_gen *g);
+/* Capacity needed for one batch: ops words / values (YCSB) or txns / lines (TPC-C). */
+int ltpg_gen_capacity(const ltpg_gen *g, uint64_t *cap_a, uint64_t *cap_b);
+/* Fill caller buffers with batch number batch_id.  YCSB: ops (n_txn*op_stride),
+ * val_off (n_txn+1), vals (capacity).  The TPC-C generator is stateful (per-
+ * warehouse order / history counters advance like TF/Query.h:54-88,157-166), so
+ * batches must be drawn in order. */
+int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t *val_off,
+                        uint64_t *vals, ltpg_ycsb_batch *out);
+int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
+                        ltpg_tpcc_line *lines, ltpg_tpcc_batch *out);
+
+/* Replaces: Query::copy_to_device (TF/Query.h:532-605, Y1/Query.h:194-213).
+ * Copies a host batch into device slot `slot` on the context stream. */
+int ltpg_batch_upload_ycsb(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b);
+int ltpg_batch_upload_tpcc(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b);
+
+/* ---- phases (Genericfunction.h / Execute*.h surface) --------------------- */
+/* Replaces: KERNEL_EXECUTE (TF/tp.cu:24-54, Y1/ycsb.cu:9-24) → __REGISTER /
+ * __READ / __WRITE (TF/Genericfunction.h:78-251). */
+int ltpg_execute_register(ltpg_ctx *ctx, uint32_t slot);
+/* Replaces: KERNEL_CHECK (TF/tp.cu:55-85, Y1/ycsb.cu:25-40) → __CHECK
+ * (TF/Genericfunction.h:252-414). */
+int ltpg_check_conflict(ltpg_ctx *ctx, uint32_t slot);
+/* Replaces: KERNEL_WRITEBACK (TF/tp.cu:86-117, Y1/ycsb.cu:41-58) → write_back /
+ * __WRITEBACK / __REDUCE_UPGRADE (TF/Genericfunction.h:416-518). */
+int ltpg_write_back(ltpg_ctx *ctx, uint32_t slot);
+/* One whole batch in the given mode (LTPG_MODE_*). */
+int ltpg_run_batch(ltpg_ctx *ctx, uint32_t slot, int mode);
+/* count batches in slots first..first+count-1, in order. */
+int ltpg_run_batches(ltpg_ctx *ctx, uint32_t first, uint32_t count, int mode);
+/* Upload + run + copy the commit bitmap back, all on the context stream and
+ * synchronised before return: the host-buffer call a caller of the reference's
+ * epoch loop makes per batch. */
+int ltpg_run_ycsb_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b, int mode,
+                       uint32_t *host_bitmap);
+int ltpg_run_tpcc_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, int mode,
+                       uint32_t *host_bitmap);
+
+/* ---- results (statistic_query / copy_to_host surface) ------------------- */
+/* Replaces: Query::copy_to_host (TF/Query.h:606-631), which reads back only
+ * the commit counters. */
+int ltpg_commit_bitmap(ltpg_ctx *ctx, uint32_t slot, uint32_t *host_bits, size_t words);
+int ltpg_txn_flags(ltpg_ctx *ctx, uint32_t slot, uint8_t *host_flags, size_t n);
+int ltpg_txn_results(ltpg_ctx *ctx, uint32_t slot, int64_t *host_results, size_t n);
+int ltpg_batch_stats_get(ltpg_ctx *ctx, uint32_t slot, ltpg_batch_stats *out);
+/* Device pointer of the commit bitmap of a slot (for callers that keep results
+ * on the GPU). */
+int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev_bits);
+
+/* ---- tuning --------------------------------------------------------------- */
+/* Block size and transactions per block-tile used by the tuned kernels of the
+ * current workload; 0 keeps the current value. */
+int ltpg_set_launch(ltpg_ctx *ctx, uint32_t block_threads, uint32_t tile_txn, uint32_t stage_ways);
+int ltpg_get_launch(ltpg_ctx *ctx, uint32_t *block_threads, uint32_t *tile_txn, uint32_t *stage_ways);
+
+/* ---- hashing used by generators and the table image --------------------- */
+uint64_t ltpg_splitmix64(uint64_t x);
+uint64_t ltpg_hash3(uint64_t seed, uint64_t a, uint64_t b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LTPG_H */

@@ -1,0 +1,295 @@
+"""ltpg_gb300 — GB300 engine for LTPG's deterministic batch concurrency control.
+
+Python host mirror of the engine's C ABI (include/ltpg.h), in the roles of the
+reference's host classes:
+  Engine            Database + Query device buffers and the three kernels
+                    (TF/Database.h:13-348, TF/Query.h:297-639, TF/tp.cu:11-117)
+  YcsbGenerator     MakeYCSB / YCSBQuery::initial_ycsb_a_query (Y1/Query.h:18-188)
+  TpccGenerator     MakeNeworder / MakePayment / Query::initial_* (TF/Query.h:16-212,478-525)
+All device work runs in libltpg.so; there is no CPU fallback: importing this
+package on a machine without the built library raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import (FLAG_COMMIT, FLAG_RAW, FLAG_WAR, FLAG_WAW, MODES, MODE_FUSED, MODE_GRAPH,  # noqa: F401
+                  MODE_PERSISTENT, MODE_PLAIN, TABLE_YCSB, TPCC_COLS)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libltpg.so")
+_lib = None
+
+
+class LtpgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ltpg error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """The loaded engine library (build it with ltpg_gb300.build.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m ltpg_gb300.build` first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in abi.SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+class YcsbBatch:
+    """A YCSB batch in the engine's format (see include/ltpg.h)."""
+
+    def __init__(self, ops, val_off, vals, n_txn, ops_per_txn):
+        self.ops = np.ascontiguousarray(ops, dtype=np.uint32)
+        self.val_off = np.ascontiguousarray(val_off, dtype=np.uint32)
+        self.vals = np.ascontiguousarray(vals, dtype=np.uint64)
+        self.n_txn = int(n_txn)
+        self.ops_per_txn = int(ops_per_txn)
+        self.op_stride = (self.ops_per_txn + 3) & ~3
+        self.n_updates = int(self.val_off[self.n_txn])
+
+    def as_c(self):
+        return abi.YcsbBatchC(self.n_txn, self.ops_per_txn, self.op_stride, self.n_updates,
+                              self.ops.ctypes.data, self.val_off.ctypes.data,
+                              self.vals.ctypes.data if len(self.vals) else None)
+
+    def nbytes(self):
+        return self.n_txn * self.op_stride * 4 + (self.n_txn + 1) * 4 + self.n_updates * 8
+
+    @staticmethod
+    def from_ops(op_lists, values):
+        """Builds a batch from per-transaction lists of (key, is_update, field) and
+        per-transaction lists of update values (hand-written test batches)."""
+        B = len(op_lists)
+        k = max(len(o) for o in op_lists)
+        stride = (k + 3) & ~3
+        ops = np.full(B * stride, abi.YCSB_OP_PAD, dtype=np.uint32)
+        val_off = np.zeros(B + 1, dtype=np.uint32)
+        vals = []
+        for t, lst in enumerate(op_lists):
+            nu = 0
+            for j, (key, upd, field) in enumerate(lst):
+                ops[t * stride + j] = (0x80000000 if upd else 0) | ((field & 0xF) << 27) | key
+                nu += bool(upd)
+            assert nu == len(values[t])
+            vals.extend(values[t])
+            val_off[t + 1] = val_off[t] + nu
+        return YcsbBatch(ops, val_off, np.array(vals, dtype=np.uint64), B, k)
+
+
+class TpccBatch:
+    TXN_DTYPE = np.dtype([("kind_info", "<u4"), ("w", "<u4"), ("c_w", "<u4"), ("c_id", "<u4"), ("a", "<u4"),
+                          ("b", "<u4"), ("c", "<u4"), ("line_off", "<u4")])
+    LINE_DTYPE = np.dtype([("i_id", "<u4"), ("supply_w", "<u2"), ("qty", "<u2")])
+
+    def __init__(self, txns, lines, txn_base=0):
+        self.txns = np.ascontiguousarray(txns, dtype=self.TXN_DTYPE)
+        self.lines = np.ascontiguousarray(lines, dtype=self.LINE_DTYPE)
+        self.n_txn = len(self.txns)
+        self.n_lines = len(self.lines)
+        self.txn_base = int(txn_base)
+
+    def as_c(self):
+        return abi.TpccBatchC(self.n_txn, self.n_lines, self.txn_base, self.txns.ctypes.data,
+                              self.lines.ctypes.data if self.n_lines else None)
+
+    def nbytes(self):
+        return self.n_txn * 32 + self.n_lines * 8
+
+
+def _check(code, ctx=None):
+    if code != abi.OK:
+        msg = lib().ltpg_last_error(ctx).decode() if ctx else "invalid argument"
+        raise LtpgError(code, msg)
+
+
+class YcsbGenerator:
+    """Deterministic YCSB batches (Zipf by Gray et al., splitmix64 streams)."""
+
+    def __init__(self, seed, n_records, n_txn, ops_per_txn=10, update_pct=50, theta=0.6, rotate_every=0):
+        self.params = abi.YcsbParamsC(seed, n_records, n_txn, ops_per_txn, update_pct, rotate_every, theta)
+        h = C.c_void_p()
+        _check(lib().ltpg_gen_create_ycsb(C.byref(self.params), C.byref(h)))
+        self._h = h
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib().ltpg_gen_capacity(h, C.byref(a), C.byref(b)))
+        self.cap_ops, self.cap_vals = a.value, b.value
+
+    def batch(self, batch_id):
+        p = self.params
+        ops = np.empty(self.cap_ops, dtype=np.uint32)
+        val_off = np.empty(p.n_txn + 1, dtype=np.uint32)
+        vals = np.empty(self.cap_vals, dtype=np.uint64)
+        out = abi.YcsbBatchC()
+        _check(lib().ltpg_gen_ycsb_batch(self._h, batch_id, _p(ops), _p(val_off), _p(vals), C.byref(out)))
+        return YcsbBatch(ops, val_off, vals[:out.n_updates].copy(), p.n_txn, p.ops_per_txn)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ltpg_gen_destroy(self._h)
+            self._h = None
+
+
+class TpccGenerator:
+    """Deterministic, stateful TPC-C NewOrder/Payment batches (draw in order)."""
+
+    def __init__(self, seed, warehouses, n_txn, neworder_pct=50, remote_line_pct=1, remote_pay_pct=15):
+        self.params = abi.TpccParamsC(seed, warehouses, n_txn, neworder_pct, remote_line_pct, remote_pay_pct)
+        h = C.c_void_p()
+        _check(lib().ltpg_gen_create_tpcc(C.byref(self.params), C.byref(h)))
+        self._h = h
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib().ltpg_gen_capacity(h, C.byref(a), C.byref(b)))
+        self.cap_txn, self.cap_lines = a.value, b.value
+        self.next_id = 0
+
+    def next(self):
+        txns = np.empty(self.cap_txn, dtype=TpccBatch.TXN_DTYPE)
+        lines = np.empty(self.cap_lines, dtype=TpccBatch.LINE_DTYPE)
+        out = abi.TpccBatchC()
+        _check(lib().ltpg_gen_tpcc_batch(self._h, self.next_id, _p(txns), _p(lines), C.byref(out)))
+        self.next_id += 1
+        return TpccBatch(txns[:out.n_txn].copy(), lines[:out.n_lines].copy(), out.txn_base)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ltpg_gen_destroy(self._h)
+            self._h = None
+
+
+class Engine:
+    """One GPU context: tables, batch slots, phases, results."""
+
+    def __init__(self, device=0, n_slots=2, max_txn=1 << 16, max_ops_per_txn=16, max_lines=0,
+                 strict_insert=False):
+        cfg = abi.ConfigC(device, n_slots, max_txn, max_ops_per_txn, max_lines,
+                          abi.CFG_STRICT_INSERT if strict_insert else 0)
+        h = C.c_void_p()
+        code = lib().ltpg_create(C.byref(cfg), C.byref(h))
+        if code != abi.OK:
+            raise LtpgError(code, "ltpg_create failed")
+        self._h = h
+        self.n_slots = n_slots
+        self.max_txn = max_txn
+
+    def _ck(self, code):
+        _check(code, self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ltpg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # stream / sync
+    def set_stream(self, stream_ptr):
+        self._ck(lib().ltpg_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def stream(self):
+        return lib().ltpg_get_stream(self._h)
+
+    def sync(self):
+        self._ck(lib().ltpg_sync(self._h))
+
+    # tables
+    def load_ycsb(self, seed, n_records):
+        self._ck(lib().ltpg_db_load_ycsb(self._h, seed, n_records))
+
+    def load_tpcc(self, seed, warehouses):
+        self._ck(lib().ltpg_db_load_tpcc(self._h, seed, warehouses))
+
+    def table_shape(self, table):
+        r, c = C.c_uint64(), C.c_uint32()
+        self._ck(lib().ltpg_db_table_shape(self._h, table, C.byref(r), C.byref(c)))
+        return r.value, c.value
+
+    def download_table(self, table):
+        rows, cols = self.table_shape(table)
+        a = np.empty(rows * cols, dtype=np.uint64)
+        self._ck(lib().ltpg_db_download(self._h, table, _p(a), a.nbytes))
+        return a
+
+    def upload_table(self, table, a):
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        self._ck(lib().ltpg_db_upload(self._h, table, _p(a), a.nbytes))
+
+    # batches
+    def upload(self, slot, batch):
+        cb = batch.as_c()
+        if isinstance(batch, YcsbBatch):
+            self._ck(lib().ltpg_batch_upload_ycsb(self._h, slot, C.byref(cb)))
+        else:
+            self._ck(lib().ltpg_batch_upload_tpcc(self._h, slot, C.byref(cb)))
+
+    def execute_register(self, slot):
+        self._ck(lib().ltpg_execute_register(self._h, slot))
+
+    def check_conflict(self, slot):
+        self._ck(lib().ltpg_check_conflict(self._h, slot))
+
+    def write_back(self, slot):
+        self._ck(lib().ltpg_write_back(self._h, slot))
+
+    def run_batch(self, slot, mode="plain"):
+        self._ck(lib().ltpg_run_batch(self._h, slot, MODES[mode] if isinstance(mode, str) else mode))
+
+    def run_batches(self, first, count, mode="graph"):
+        self._ck(lib().ltpg_run_batches(self._h, first, count, MODES[mode] if isinstance(mode, str) else mode))
+
+    def run_host(self, slot, batch, mode="plain", bitmap=None):
+        """Upload + run + bitmap download, synchronised (host-buffer call)."""
+        words = (batch.n_txn + 31) // 32
+        out = bitmap if bitmap is not None else np.empty(words, dtype=np.uint32)
+        cb = batch.as_c()
+        m = MODES[mode] if isinstance(mode, str) else mode
+        if isinstance(batch, YcsbBatch):
+            self._ck(lib().ltpg_run_ycsb_host(self._h, slot, C.byref(cb), m, _p(out)))
+        else:
+            self._ck(lib().ltpg_run_tpcc_host(self._h, slot, C.byref(cb), m, _p(out)))
+        return out
+
+    # results
+    def commit_bitmap(self, slot, n_txn):
+        out = np.empty((n_txn + 31) // 32, dtype=np.uint32)
+        self._ck(lib().ltpg_commit_bitmap(self._h, slot, _p(out), len(out)))
+        return out
+
+    def txn_flags(self, slot, n_txn):
+        out = np.empty(n_txn, dtype=np.uint8)
+        self._ck(lib().ltpg_txn_flags(self._h, slot, _p(out), n_txn))
+        return out
+
+    def txn_results(self, slot, n_txn):
+        out = np.empty(n_txn, dtype=np.int64)
+        self._ck(lib().ltpg_txn_results(self._h, slot, _p(out), n_txn))
+        return out
+
+    def stats(self, slot):
+        s = abi.StatsC()
+        self._ck(lib().ltpg_batch_stats_get(self._h, slot, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.StatsC._fields_}
+
+    def set_launch(self, block=0, tile=0, ways=0):
+        self._ck(lib().ltpg_set_launch(self._h, block, tile, ways))
+
+    def get_launch(self):
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._ck(lib().ltpg_get_launch(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value

@@ -1,0 +1,106 @@
+"""ctypes mirror of include/ltpg.h (structs, constants, function signatures)."""
+import ctypes as C
+
+OK = 0
+ERR_INVALID, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_TIMEOUT, ERR_BOUNDS = 1, 2, 3, 4, 5, 6
+WORKLOAD_YCSB, WORKLOAD_TPCC = 1, 2
+MODE_PLAIN, MODE_FUSED, MODE_PERSISTENT, MODE_GRAPH = 0, 1, 2, 3
+MODES = {"plain": MODE_PLAIN, "fused": MODE_FUSED, "persistent": MODE_PERSISTENT, "graph": MODE_GRAPH}
+FLAG_RAW, FLAG_WAR, FLAG_WAW, FLAG_COMMIT = 1, 2, 4, 8
+YCSB_FIELDS = 10
+YCSB_OP_PAD = 0xFFFFFFFF
+YCSB_KEY_BITS = 27
+YCSB_MAX_OPS = 32
+TABLE_YCSB = 100
+T_WAREHOUSE, T_DISTRICT, T_CUSTOMER, T_HISTORY, T_NEWORDER, T_ORDER, T_ORDERLINE, T_STOCK, T_ITEM = range(9)
+TPCC_TABLES = 9
+TPCC_COLS = (9, 11, 21, 8, 3, 8, 10, 17, 5)
+TPCC_NEWORDER, TPCC_PAYMENT = 0, 1
+TPCC_MAX_LINES = 15
+CFG_STRICT_INSERT = 1
+
+
+class YcsbBatchC(C.Structure):
+    _fields_ = [("n_txn", C.c_uint32), ("ops_per_txn", C.c_uint32), ("op_stride", C.c_uint32),
+                ("n_updates", C.c_uint32), ("ops", C.c_void_p), ("val_off", C.c_void_p), ("vals", C.c_void_p)]
+
+
+class YcsbParamsC(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_records", C.c_uint64), ("n_txn", C.c_uint32),
+                ("ops_per_txn", C.c_uint32), ("update_pct", C.c_uint32), ("rotate_every", C.c_uint32),
+                ("theta", C.c_double)]
+
+
+class TpccBatchC(C.Structure):
+    _fields_ = [("n_txn", C.c_uint32), ("n_lines", C.c_uint32), ("txn_base", C.c_uint64),
+                ("txns", C.c_void_p), ("lines", C.c_void_p)]
+
+
+class TpccParamsC(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("warehouses", C.c_uint32), ("n_txn", C.c_uint32),
+                ("neworder_pct", C.c_uint32), ("remote_line_pct", C.c_uint32), ("remote_pay_pct", C.c_uint32)]
+
+
+class ConfigC(C.Structure):
+    _fields_ = [("device", C.c_int32), ("n_slots", C.c_uint32), ("max_txn", C.c_uint32),
+                ("max_ops_per_txn", C.c_uint32), ("max_lines", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class StatsC(C.Structure):
+    _fields_ = [("n_txn", C.c_uint64), ("commits", C.c_uint64), ("raw", C.c_uint64), ("war", C.c_uint64),
+                ("waw", C.c_uint64), ("staged_ops", C.c_uint64), ("total_ops", C.c_uint64)]
+
+
+P = C.c_void_p
+U32, U64, I32 = C.c_uint32, C.c_uint64, C.c_int32
+SZ = C.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "ltpg_create": (C.c_int, [C.POINTER(ConfigC), C.POINTER(P)]),
+    "ltpg_destroy": (C.c_int, [P]),
+    "ltpg_last_error": (C.c_char_p, [P]),
+    "ltpg_set_stream": (C.c_int, [P, P]),
+    "ltpg_get_stream": (P, [P]),
+    "ltpg_sync": (C.c_int, [P]),
+    "ltpg_host_alloc": (P, [SZ]),
+    "ltpg_host_free": (None, [P]),
+    "ltpg_db_load_ycsb": (C.c_int, [P, U64, U64]),
+    "ltpg_db_load_tpcc": (C.c_int, [P, U64, U32]),
+    "ltpg_db_table_shape": (C.c_int, [P, U32, C.POINTER(U64), C.POINTER(U32)]),
+    "ltpg_db_upload": (C.c_int, [P, U32, P, SZ]),
+    "ltpg_db_download": (C.c_int, [P, U32, P, SZ]),
+    "ltpg_gen_create_ycsb": (C.c_int, [C.POINTER(YcsbParamsC), C.POINTER(P)]),
+    "ltpg_gen_create_tpcc": (C.c_int, [C.POINTER(TpccParamsC), C.POINTER(P)]),
+    "ltpg_gen_destroy": (C.c_int, [P]),
+    "ltpg_gen_capacity": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
+    "ltpg_gen_ycsb_batch": (C.c_int, [P, U64, P, P, P, C.POINTER(YcsbBatchC)]),
+    "ltpg_gen_tpcc_batch": (C.c_int, [P, U64, P, P, C.POINTER(TpccBatchC)]),
+    "ltpg_batch_upload_ycsb": (C.c_int, [P, U32, C.POINTER(YcsbBatchC)]),
+    "ltpg_batch_upload_tpcc": (C.c_int, [P, U32, C.POINTER(TpccBatchC)]),
+    "ltpg_execute_register": (C.c_int, [P, U32]),
+    "ltpg_check_conflict": (C.c_int, [P, U32]),
+    "ltpg_write_back": (C.c_int, [P, U32]),
+    "ltpg_run_batch": (C.c_int, [P, U32, C.c_int]),
+    "ltpg_run_batches": (C.c_int, [P, U32, U32, C.c_int]),
+    "ltpg_run_ycsb_host": (C.c_int, [P, U32, C.POINTER(YcsbBatchC), C.c_int, P]),
+    "ltpg_run_tpcc_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), C.c_int, P]),
+    "ltpg_commit_bitmap": (C.c_int, [P, U32, P, SZ]),
+    "ltpg_txn_flags": (C.c_int, [P, U32, P, SZ]),
+    "ltpg_txn_results": (C.c_int, [P, U32, P, SZ]),
+    "ltpg_batch_stats_get": (C.c_int, [P, U32, C.POINTER(StatsC)]),
+    "ltpg_commit_bitmap_device": (C.c_int, [P, U32, C.POINTER(P)]),
+    "ltpg_set_launch": (C.c_int, [P, U32, U32, U32]),
+    "ltpg_get_launch": (C.c_int, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    "ltpg_splitmix64": (U64, [U64]),
+    "ltpg_hash3": (U64, [U64, U64, U64]),
+}
+
+
+def declared_functions(header_path):
+    """Names of the functions include/ltpg.h declares (for the export test)."""
+    import re
+    text = open(header_path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?\**\s*\**(ltpg_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))

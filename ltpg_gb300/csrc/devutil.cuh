@@ -1,0 +1,81 @@
+// devutil.cuh — small device helpers shared by the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "engine.h"
+
+namespace ltpg {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// 16-byte load of a registration slot that bypasses L1: slots are written by
+// atomics at L2 in the previous phase.
+__device__ __forceinline__ ulonglong2 ld_slot(const RegSlot *p) {
+    ulonglong2 v;
+    asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+// Read-only 16-byte load through the non-coherent path (table rows, batches).
+__device__ __forceinline__ ulonglong2 ld_nc16(const void *p) {
+    ulonglong2 v;
+    asm("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint4 ld_nc_u4(const void *p) {
+    uint4 v;
+    asm("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
+    return v;
+}
+// Fire-and-forget atomic minimum (no return value, so it issues as a
+// reduction at L2).
+__device__ __forceinline__ void red_min(unsigned long long *p, unsigned long long v) {
+    asm volatile("red.global.min.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_add_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void report_error(DevCtl *ctl, uint32_t code, uint32_t index) {
+    if (atomicOr(&ctl->error, code) == 0u) ctl->err_index = index;
+}
+
+// Called by every block at the very end of a batch's final kernel: the last
+// block to finish advances the batch epoch.
+__device__ __forceinline__ void finish_batch(DevCtl *ctl) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&ctl->done, 1u);
+        if (prev == gridDim.x - 1u) {
+            ctl->done = 0u;
+            atomicAdd(&ctl->epoch, 1u);
+            __threadfence();
+        }
+    }
+}
+
+// Warp-cooperative scatter list: lane L owns n_L items (inclusive prefix incl);
+// returns the lane that owns item e (0 <= e < total).
+__device__ __forceinline__ int owner_lane(int incl, unsigned e) {
+    int lo = 0;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const unsigned v = (unsigned)__shfl_sync(FULL, incl, lo + s - 1);
+        if (v <= e) lo += s;
+    }
+    return lo;
+}
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+}  // namespace ltpg

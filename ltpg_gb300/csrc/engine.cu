@@ -1,0 +1,530 @@
+// engine.cu — the C ABI: context, tables, batch slots, phase dispatch, results.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+using namespace ltpg;
+
+namespace {
+
+int fail(ltpg_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what) {
+    return fail(c, LTPG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+template <class T>
+cudaError_t dev_alloc(T **p, uint64_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+template <class T>
+void dev_free(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_slot(Slot &s) {
+    dev_free(s.ops);
+    dev_free(s.val_off);
+    dev_free(s.vals);
+    dev_free(s.txns);
+    dev_free(s.lines);
+    dev_free(s.flags);
+    dev_free(s.bitmap);
+    dev_free(s.results);
+    dev_free(s.stats);
+    s = Slot{};
+}
+
+void drop_graphs(ltpg_ctx *c) {
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+// Output buffers of a slot, sized for n transactions.
+int ensure_outputs(ltpg_ctx *c, Slot &s, uint64_t n) {
+    if (s.cap_out >= n && s.stats) return LTPG_OK;
+    dev_free(s.flags);
+    dev_free(s.bitmap);
+    dev_free(s.results);
+    dev_free(s.stats);
+    const uint64_t cap = std::max<uint64_t>(n, c->cfg.max_txn);
+    CK(dev_alloc(&s.flags, cap), "alloc flags");
+    CK(dev_alloc(&s.bitmap, (cap + 31) / 32 + 1), "alloc bitmap");
+    CK(dev_alloc(&s.results, cap), "alloc results");
+    CK(dev_alloc(&s.stats, 1), "alloc stats");
+    CK(cudaMemset(s.stats, 0, sizeof(DevStats)), "clear stats");
+    s.cap_out = cap;
+    drop_graphs(c);
+    return LTPG_OK;
+}
+
+// Reads and clears the device error word; call after a synchronisation.
+int check_device_error(ltpg_ctx *c) {
+    DevCtl h;
+    CK(cudaMemcpy(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost), "read control block");
+    if (h.error == 0) return LTPG_OK;
+    const uint32_t zero = 0;
+    CK(cudaMemcpy(&c->ctl->error, &zero, sizeof zero, cudaMemcpyHostToDevice), "clear error");
+    char buf[160];
+    if (h.error & DERR_TIMEOUT) {
+        snprintf(buf, sizeof buf, "device wait timed out (index %u)", h.err_index);
+        return fail(c, LTPG_ERR_TIMEOUT, buf);
+    }
+    snprintf(buf, sizeof buf, "key or index out of range in batch (transaction %u)", h.err_index);
+    return fail(c, LTPG_ERR_BOUNDS, buf);
+}
+
+Slot *get_slot(ltpg_ctx *c, uint32_t slot) {
+    if (!c || slot >= c->slots.size()) return nullptr;
+    return &c->slots[slot];
+}
+
+}  // namespace
+
+extern "C" {
+
+int ltpg_create(const ltpg_config *cfg, ltpg_ctx **out) {
+    if (!cfg || !out) return LTPG_ERR_INVALID;
+    *out = nullptr;
+    if (cfg->n_slots == 0 || cfg->n_slots > 4096 || cfg->max_txn == 0 || cfg->max_txn > (1u << 26))
+        return LTPG_ERR_INVALID;
+    if (cfg->max_ops_per_txn > LTPG_YCSB_MAX_OPS) return LTPG_ERR_INVALID;
+    ltpg_ctx *c = new (std::nothrow) ltpg_ctx();
+    if (!c) return LTPG_ERR_NOMEM;
+    c->cfg = *cfg;
+    if (c->cfg.max_ops_per_txn == 0) c->cfg.max_ops_per_txn = 16;
+    if (c->cfg.max_lines == 0) c->cfg.max_lines = c->cfg.max_txn * 10u;
+    c->device = cfg->device;
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, cfg->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->ctl, sizeof(DevCtl));
+    if (e == cudaSuccess) {
+        DevCtl h{};
+        h.epoch = 1;
+        e = cudaMemcpy(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        if (c->ctl) cudaFree(c->ctl);
+        if (c->own_stream) cudaStreamDestroy(c->own_stream);
+        delete c;
+        return LTPG_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    c->slots.resize(cfg->n_slots);
+    *out = c;
+    return LTPG_OK;
+}
+
+int ltpg_destroy(ltpg_ctx *c) {
+    if (!c) return LTPG_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    for (auto &s : c->slots) free_slot(s);
+    dev_free(c->ycsb.rows);
+    dev_free(c->ycsb.reg);
+    for (auto &t : c->tpcc.tab) dev_free(t);
+    dev_free(c->tpcc.reg);
+    dev_free(c->stage_map);
+    dev_free(c->bucket_counts);
+    dev_free(c->ctl);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return LTPG_OK;
+}
+
+const char *ltpg_last_error(const ltpg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int ltpg_set_stream(ltpg_ctx *c, void *stream) {
+    if (!c) return LTPG_ERR_INVALID;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return LTPG_OK;
+}
+void *ltpg_get_stream(ltpg_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int ltpg_sync(ltpg_ctx *c) {
+    if (!c) return LTPG_ERR_INVALID;
+    CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    return check_device_error(c);
+}
+
+void *ltpg_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+void ltpg_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+// ---- tables -----------------------------------------------------------------
+int ltpg_db_load_ycsb(ltpg_ctx *c, uint64_t seed, uint64_t n) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (n == 0 || n > (1ull << LTPG_YCSB_KEY_BITS)) return fail(c, LTPG_ERR_INVALID, "YCSB table size out of range");
+    CK(cudaSetDevice(c->device), "set device");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    drop_graphs(c);
+    dev_free(c->ycsb.rows);
+    dev_free(c->ycsb.reg);
+    c->ycsb.n = 0;
+    CK(dev_alloc(&c->ycsb.rows, n * LTPG_YCSB_FIELDS), "alloc YCSB table");
+    CK(dev_alloc(&c->ycsb.reg, n), "alloc YCSB registration table");
+    c->ycsb.n = n;
+    c->ycsb_seed = seed;
+    CK(ycsb_init_table(c), "init YCSB table");
+    return ltpg_sync(c);
+}
+
+int ltpg_db_load_tpcc(ltpg_ctx *c, uint64_t seed, uint32_t W) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (W == 0 || W > 4096) return fail(c, LTPG_ERR_INVALID, "warehouse count out of range");
+    CK(cudaSetDevice(c->device), "set device");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    drop_graphs(c);
+    for (auto &t : c->tpcc.tab) dev_free(t);
+    dev_free(c->tpcc.reg);
+    c->tpcc = TpccDb{};
+    uint64_t total = 0;
+    for (uint32_t t = 0; t < LTPG_TPCC_TABLES; ++t) {
+        c->tpcc.rows[t] = tpcc_rows(t, W);
+        c->tpcc.base[t] = total;
+        total += c->tpcc.rows[t];
+        CK(dev_alloc(&c->tpcc.tab[t], c->tpcc.rows[t] * TPCC_COLS[t]), "alloc TPC-C table");
+    }
+    if (total >= (1ull << 32)) return fail(c, LTPG_ERR_INVALID, "too many rows for 32-bit slots");
+    CK(dev_alloc(&c->tpcc.reg, total), "alloc TPC-C registration table");
+    c->tpcc.n_slots = total;
+    c->tpcc.W = W;
+    c->tpcc_seed = seed;
+    CK(tpcc_init_tables(c), "init TPC-C tables");
+    return ltpg_sync(c);
+}
+
+}  // extern "C"
+
+namespace {
+// table id: 0..8 TPC-C tables, 100 = YCSB table.
+int table_ptr(ltpg_ctx *c, uint32_t table, uint64_t **p, uint64_t *count) {
+    if (table == LTPG_TABLE_YCSB) {
+        if (!c->ycsb.rows) return fail(c, LTPG_ERR_STATE, "no YCSB table loaded");
+        *p = c->ycsb.rows;
+        *count = c->ycsb.n * LTPG_YCSB_FIELDS;
+        return LTPG_OK;
+    }
+    if (table < LTPG_TPCC_TABLES) {
+        if (!c->tpcc.W) return fail(c, LTPG_ERR_STATE, "no TPC-C tables loaded");
+        *p = c->tpcc.tab[table];
+        *count = c->tpcc.rows[table] * TPCC_COLS[table];
+        return LTPG_OK;
+    }
+    return fail(c, LTPG_ERR_INVALID, "unknown table id");
+}
+}  // namespace
+
+extern "C" {
+
+int ltpg_db_table_shape(ltpg_ctx *c, uint32_t table, uint64_t *rows, uint32_t *cols) {
+    if (!c || !rows || !cols) return LTPG_ERR_INVALID;
+    uint64_t *p;
+    uint64_t n;
+    int r = table_ptr(c, table, &p, &n);
+    if (r) return r;
+    *cols = table == LTPG_TABLE_YCSB ? LTPG_YCSB_FIELDS : TPCC_COLS[table];
+    *rows = n / *cols;
+    return LTPG_OK;
+}
+
+int ltpg_db_upload(ltpg_ctx *c, uint32_t table, const void *host, size_t bytes) {
+    if (!c || !host) return LTPG_ERR_INVALID;
+    uint64_t *p;
+    uint64_t n;
+    int r = table_ptr(c, table, &p, &n);
+    if (r) return r;
+    if (bytes != n * 8) return fail(c, LTPG_ERR_INVALID, "image size mismatch");
+    CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload table");
+    return ltpg_sync(c);
+}
+
+int ltpg_db_download(ltpg_ctx *c, uint32_t table, void *host, size_t bytes) {
+    if (!c || !host) return LTPG_ERR_INVALID;
+    uint64_t *p;
+    uint64_t n;
+    int r = table_ptr(c, table, &p, &n);
+    if (r) return r;
+    if (bytes != n * 8) return fail(c, LTPG_ERR_INVALID, "image size mismatch");
+    CK(cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, c->stream), "download table");
+    return ltpg_sync(c);
+}
+
+// ---- batches ---------------------------------------------------------------------
+int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (!c->ycsb.rows) return fail(c, LTPG_ERR_STATE, "no YCSB table loaded");
+    if (b->n_txn == 0 || b->n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
+    if (b->ops_per_txn == 0 || b->ops_per_txn > c->cfg.max_ops_per_txn || b->op_stride != ycsb_stride(b->ops_per_txn))
+        return fail(c, LTPG_ERR_INVALID, "bad ops_per_txn / op_stride");
+    if (!b->ops || !b->val_off || (b->n_updates && !b->vals)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    if (b->n_updates > (uint64_t)b->n_txn * b->ops_per_txn) return fail(c, LTPG_ERR_INVALID, "too many updates");
+    const uint64_t n_ops = (uint64_t)b->n_txn * b->op_stride;
+    const uint64_t cap_ops = (uint64_t)c->cfg.max_txn * ycsb_stride(c->cfg.max_ops_per_txn);
+    const uint64_t cap_vals = (uint64_t)c->cfg.max_txn * c->cfg.max_ops_per_txn;
+    if (!s->ops) {
+        CK(dev_alloc(&s->ops, cap_ops), "alloc ops");
+        CK(dev_alloc(&s->val_off, (uint64_t)c->cfg.max_txn + 1), "alloc val_off");
+        CK(dev_alloc(&s->vals, cap_vals), "alloc vals");
+        s->cap_ops = cap_ops;
+        s->cap_vals = cap_vals;
+        s->cap_txn_y = c->cfg.max_txn;
+    }
+    int r = ensure_outputs(c, *s, b->n_txn);
+    if (r) return r;
+    CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, c->stream), "upload ops");
+    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, c->stream),
+       "upload val_off");
+    if (b->n_updates)
+        CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, c->stream),
+           "upload vals");
+    if (s->workload != LTPG_WORKLOAD_YCSB || s->n_txn != b->n_txn || s->k != b->ops_per_txn) drop_graphs(c);
+    s->workload = LTPG_WORKLOAD_YCSB;
+    s->n_txn = b->n_txn;
+    s->k = b->ops_per_txn;
+    s->stride = b->op_stride;
+    s->n_updates = b->n_updates;
+    return LTPG_OK;
+}
+
+int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (!c->tpcc.W) return fail(c, LTPG_ERR_STATE, "no TPC-C tables loaded");
+    if (b->n_txn == 0 || b->n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
+    if (b->n_lines > c->cfg.max_lines) return fail(c, LTPG_ERR_INVALID, "batch has more lines than max_lines");
+    if (!b->txns || (b->n_lines && !b->lines)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    if (!s->txns) {
+        CK(dev_alloc(&s->txns, c->cfg.max_txn), "alloc txns");
+        CK(dev_alloc(&s->lines, (uint64_t)c->cfg.max_lines + 1), "alloc lines");
+        s->cap_txn_c = c->cfg.max_txn;
+        s->cap_lines = c->cfg.max_lines;
+    }
+    int r = ensure_outputs(c, *s, b->n_txn);
+    if (r) return r;
+    CK(cudaMemcpyAsync(s->txns, b->txns, (uint64_t)b->n_txn * sizeof(ltpg_tpcc_txn), cudaMemcpyHostToDevice,
+                       c->stream),
+       "upload txns");
+    if (b->n_lines)
+        CK(cudaMemcpyAsync(s->lines, b->lines, (uint64_t)b->n_lines * sizeof(ltpg_tpcc_line),
+                           cudaMemcpyHostToDevice, c->stream),
+           "upload lines");
+    if (s->workload != LTPG_WORKLOAD_TPCC || s->n_txn != b->n_txn) drop_graphs(c);
+    s->workload = LTPG_WORKLOAD_TPCC;
+    s->n_txn = b->n_txn;
+    s->n_lines = b->n_lines;
+    s->txn_base = b->txn_base;
+    return LTPG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int run_phase(ltpg_ctx *c, uint32_t slot, int phase) {
+    Slot *s = get_slot(c, slot);
+    if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    cudaError_t e;
+    if (s->workload == LTPG_WORKLOAD_YCSB) e = ycsb_phase(c, *s, phase);
+    else if (s->workload == LTPG_WORKLOAD_TPCC) e = tpcc_phase(c, *s, phase);
+    else return fail(c, LTPG_ERR_STATE, "slot holds no batch");
+    if (e != cudaSuccess) return cuda_fail(c, e, "phase launch");
+    return LTPG_OK;
+}
+
+int run_one(ltpg_ctx *c, uint32_t slot, int mode) {
+    Slot *s = get_slot(c, slot);
+    if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (mode == LTPG_MODE_PLAIN) {
+        for (int p = 0; p < 3; ++p) {
+            int r = run_phase(c, slot, p);
+            if (r) return r;
+        }
+        return LTPG_OK;
+    }
+    cudaError_t e;
+    if (s->workload == LTPG_WORKLOAD_YCSB) e = ycsb_run_tuned(c, *s, mode);
+    else if (s->workload == LTPG_WORKLOAD_TPCC) e = tpcc_run_tuned(c, *s, mode);
+    else return fail(c, LTPG_ERR_STATE, "slot holds no batch");
+    if (e != cudaSuccess) return cuda_fail(c, e, "tuned launch");
+    return LTPG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ltpg_execute_register(ltpg_ctx *c, uint32_t slot) { return run_phase(c, slot, 0); }
+int ltpg_check_conflict(ltpg_ctx *c, uint32_t slot) { return run_phase(c, slot, 1); }
+int ltpg_write_back(ltpg_ctx *c, uint32_t slot) { return run_phase(c, slot, 2); }
+
+int ltpg_run_batch(ltpg_ctx *c, uint32_t slot, int mode) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (mode == LTPG_MODE_GRAPH) return ltpg_run_batches(c, slot, 1, mode);
+    if (mode < LTPG_MODE_PLAIN || mode > LTPG_MODE_GRAPH) return fail(c, LTPG_ERR_INVALID, "bad mode");
+    return run_one(c, slot, mode);
+}
+
+int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (count == 0) return LTPG_OK;
+    if ((uint64_t)first + count > c->slots.size()) return fail(c, LTPG_ERR_INVALID, "slot range out of bounds");
+    if (mode != LTPG_MODE_GRAPH) {
+        for (uint32_t i = 0; i < count; ++i) {
+            int r = ltpg_run_batch(c, first + i, mode);
+            if (r) return r;
+        }
+        return LTPG_OK;
+    }
+    const int wl = c->slots[first].workload;
+    for (auto &g : c->graphs)
+        if (g.first == first && g.count == count && g.workload == wl) {
+            CK(cudaGraphLaunch(g.exec, c->stream), "graph launch");
+            return LTPG_OK;
+        }
+    // Capture the fused kernels of `count` batches into one graph.  The batch
+    // epoch lives in device memory and is advanced by the kernels themselves,
+    // so the graph can be replayed as is.
+    cudaStream_t cap = c->stream;
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int r = LTPG_OK;
+    for (uint32_t i = 0; i < count && r == LTPG_OK; ++i) r = run_one(c, first + i, LTPG_MODE_FUSED);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    if (r) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+    c->graphs.push_back({first, count, wl, exec});
+    CK(cudaGraphLaunch(exec, c->stream), "graph launch");
+    return LTPG_OK;
+}
+
+int ltpg_run_ycsb_host(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, int mode, uint32_t *host_bitmap) {
+    int r = ltpg_batch_upload_ycsb(c, slot, b);
+    if (r) return r;
+    r = ltpg_run_batch(c, slot, mode);
+    if (r) return r;
+    if (host_bitmap) {
+        Slot &s = c->slots[slot];
+        CK(cudaMemcpyAsync(host_bitmap, s.bitmap, ((uint64_t)s.n_txn + 31) / 32 * 4, cudaMemcpyDeviceToHost,
+                           c->stream),
+           "bitmap download");
+    }
+    return ltpg_sync(c);
+}
+
+int ltpg_run_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int mode, uint32_t *host_bitmap) {
+    int r = ltpg_batch_upload_tpcc(c, slot, b);
+    if (r) return r;
+    r = ltpg_run_batch(c, slot, mode);
+    if (r) return r;
+    if (host_bitmap) {
+        Slot &s = c->slots[slot];
+        CK(cudaMemcpyAsync(host_bitmap, s.bitmap, ((uint64_t)s.n_txn + 31) / 32 * 4, cudaMemcpyDeviceToHost,
+                           c->stream),
+           "bitmap download");
+    }
+    return ltpg_sync(c);
+}
+
+// ---- results -----------------------------------------------------------------
+int ltpg_commit_bitmap(ltpg_ctx *c, uint32_t slot, uint32_t *host_bits, size_t words) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !host_bits) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    const size_t need = ((size_t)s->n_txn + 31) / 32;
+    if (words < need) return fail(c, LTPG_ERR_INVALID, "bitmap buffer too small");
+    CK(cudaMemcpyAsync(host_bits, s->bitmap, need * 4, cudaMemcpyDeviceToHost, c->stream), "bitmap download");
+    return ltpg_sync(c);
+}
+
+int ltpg_txn_flags(ltpg_ctx *c, uint32_t slot, uint8_t *host, size_t n) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !host) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (n < s->n_txn) return fail(c, LTPG_ERR_INVALID, "flags buffer too small");
+    CK(cudaMemcpyAsync(host, s->flags, s->n_txn, cudaMemcpyDeviceToHost, c->stream), "flags download");
+    return ltpg_sync(c);
+}
+
+int ltpg_txn_results(ltpg_ctx *c, uint32_t slot, int64_t *host, size_t n) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !host) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (n < s->n_txn) return fail(c, LTPG_ERR_INVALID, "results buffer too small");
+    CK(cudaMemcpyAsync(host, s->results, (size_t)s->n_txn * 8, cudaMemcpyDeviceToHost, c->stream),
+       "results download");
+    return ltpg_sync(c);
+}
+
+int ltpg_batch_stats_get(ltpg_ctx *c, uint32_t slot, ltpg_batch_stats *out) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !out) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    DevStats h{};
+    CK(cudaMemcpyAsync(&h, s->stats, sizeof h, cudaMemcpyDeviceToHost, c->stream), "stats download");
+    int r = ltpg_sync(c);
+    if (r) return r;
+    out->n_txn = s->n_txn;
+    out->commits = h.commits;
+    out->raw = h.raw;
+    out->war = h.war;
+    out->waw = h.waw;
+    out->staged_ops = h.staged_ops;
+    out->total_ops = h.total_ops;
+    return LTPG_OK;
+}
+
+int ltpg_commit_bitmap_device(ltpg_ctx *c, uint32_t slot, const uint32_t **dev_bits) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !dev_bits) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    *dev_bits = s->bitmap;
+    return LTPG_OK;
+}
+
+int ltpg_set_launch(ltpg_ctx *c, uint32_t block, uint32_t tile, uint32_t ways) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (block && (block % 32 || block > 1024)) return fail(c, LTPG_ERR_INVALID, "block must be a multiple of 32, <= 1024");
+    if (ways > 8) return fail(c, LTPG_ERR_INVALID, "at most 8 staging ways");
+    for (LaunchCfg *l : {&c->launch_y, &c->launch_c}) {
+        if (block) l->block = block;
+        if (tile) l->tile = tile;
+        if (ways) l->ways = ways;
+    }
+    c->persist_blocks_y = c->persist_blocks_c = 0;
+    drop_graphs(c);
+    return LTPG_OK;
+}
+
+int ltpg_get_launch(ltpg_ctx *c, uint32_t *block, uint32_t *tile, uint32_t *ways) {
+    if (!c || !block || !tile || !ways) return LTPG_ERR_INVALID;
+    *block = c->launch_y.block;
+    *tile = c->launch_y.tile;
+    *ways = c->launch_y.ways;
+    return LTPG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+// engine.h — context and device-side structures shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "proto.h"
+
+namespace ltpg {
+
+// Device control block, one per context.
+//  epoch        tag of the batch being run (see slot_tag in proto.h); bumped on
+//               the device by the last block of a batch's final kernel, so a
+//               captured CUDA graph can be replayed without host involvement.
+//  done         completion counter of that final kernel.
+//  error        OR of LTPG device error bits (bounds, timeouts).
+//  err_index    first offending index, for the error message.
+//  barrier      generation counter of the persistent kernel's grid barrier.
+struct DevCtl {
+    uint32_t epoch;
+    uint32_t done;
+    uint32_t error;
+    uint32_t err_index;
+    uint32_t barrier_count;
+    uint32_t barrier_gen;
+    uint32_t pad[2];
+};
+constexpr uint32_t DERR_BOUNDS = 1u;
+constexpr uint32_t DERR_TIMEOUT = 2u;
+
+// Per-batch counters accumulated on the device (ltpg_batch_stats).
+struct DevStats {
+    unsigned long long commits, raw, war, waw, staged_ops, total_ops, pad[2];
+};
+
+// A registration slot: minimum read and write TID of a row, epoch-tagged.
+struct __align__(16) RegSlot {
+    unsigned long long r, w;
+};
+
+struct YcsbDb {
+    uint64_t n = 0;
+    uint64_t *rows = nullptr;  // n * 10 u64
+    RegSlot *reg = nullptr;    // n
+};
+
+struct TpccDb {
+    uint32_t W = 0;
+    uint64_t rows[LTPG_TPCC_TABLES] = {};
+    uint64_t *tab[LTPG_TPCC_TABLES] = {};
+    uint64_t n_slots = 0;
+    RegSlot *reg = nullptr;  // flat over all tables
+    uint64_t base[LTPG_TPCC_TABLES] = {};
+};
+
+// One device batch slot.
+struct Slot {
+    int workload = 0;
+    uint32_t n_txn = 0;
+    // YCSB
+    uint32_t k = 0, stride = 0, n_updates = 0;
+    uint32_t *ops = nullptr;
+    uint32_t *val_off = nullptr;
+    uint64_t *vals = nullptr;
+    uint64_t cap_ops = 0, cap_vals = 0, cap_txn_y = 0;
+    // TPC-C
+    uint32_t n_lines = 0;
+    uint64_t txn_base = 0;
+    ltpg_tpcc_txn *txns = nullptr;
+    ltpg_tpcc_line *lines = nullptr;
+    uint64_t cap_txn_c = 0, cap_lines = 0;
+    // outputs
+    uint8_t *flags = nullptr;
+    uint32_t *bitmap = nullptr;
+    int64_t *results = nullptr;
+    DevStats *stats = nullptr;
+    uint64_t cap_out = 0;
+};
+
+struct LaunchCfg {
+    uint32_t block = 256;   // threads per block of the tuned kernels
+    uint32_t tile = 0;      // transactions per block tile (0 = derived)
+    uint32_t ways = 4;      // shared-memory staging ways per bucket
+};
+
+}  // namespace ltpg
+
+struct ltpg_ctx {
+    int device = 0;
+    ltpg_config cfg{};
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    ltpg::DevCtl *ctl = nullptr;
+    ltpg::YcsbDb ycsb;
+    ltpg::TpccDb tpcc;
+    uint64_t ycsb_seed = 0, tpcc_seed = 0;
+    std::vector<ltpg::Slot> slots;
+    ltpg::LaunchCfg launch_y, launch_c;
+    int sm_count = 0;
+    // persistent-mode occupancy
+    int persist_blocks_y = 0, persist_blocks_c = 0;
+    // staging map (bucket -> way group), predictor output
+    uint16_t *stage_map = nullptr;
+    uint32_t *bucket_counts = nullptr;  // per-batch access counts per bucket
+    uint32_t stage_on = 0;
+    // cached CUDA graphs keyed by (first, count, workload)
+    struct GraphEntry {
+        uint32_t first, count;
+        int workload;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+};
+
+// Kernel launchers implemented in ycsb.cu / tpcc.cu.
+namespace ltpg {
+cudaError_t ycsb_init_table(ltpg_ctx *c);
+cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase);      // 0 exec, 1 check, 2 write-back
+cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode);   // fused / persistent
+cudaError_t tpcc_init_tables(ltpg_ctx *c);
+cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase);
+cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode);
+}  // namespace ltpg

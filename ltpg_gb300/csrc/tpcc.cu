@@ -1,0 +1,373 @@
+// tpcc.cu — TPC-C NewOrder + Payment executors: table image and plain path.
+//
+// Concurrency-control ops per transaction follow NEWORDER_NAMESPACE and
+// PAYMENT_NAMESPACE of the reference (TF/Execute_neworder.h:14-336,426-617,
+// TF/Execute_payment.h:39-303,390-536); see tpcc_op() in proto.h.  The
+// warehouse and district YTD updates of Payment are hot commutative adds that
+// neither register nor check (the "isFrequent" path, TF/Execute_payment.h:86-99,
+// 144-163); they are applied as exact int64 adds for committed Payments only.
+//
+// Transactions are ragged (5 + 3 * lines ops for NewOrder, 5 for Payment).  A
+// block takes a tile of transactions, lays their ops out back to back by an
+// in-tile prefix sum, and its threads walk that flat list, so short and long
+// transactions cost the same per op (the reference leaves lanes idle per
+// missing order line, TF/Execute_neworder.h:174-183).
+#include "devutil.cuh"
+
+namespace ltpg {
+
+struct TpccDev {
+    uint64_t *tab[LTPG_TPCC_TABLES];
+    uint64_t rows[LTPG_TPCC_TABLES];
+    uint64_t base[LTPG_TPCC_TABLES];
+    uint32_t W;
+    uint32_t strict;
+};
+
+static TpccDev make_dev(ltpg_ctx *c) {
+    TpccDev d{};
+    for (int t = 0; t < LTPG_TPCC_TABLES; ++t) {
+        d.tab[t] = c->tpcc.tab[t];
+        d.rows[t] = c->tpcc.rows[t];
+        d.base[t] = c->tpcc.base[t];
+    }
+    d.W = c->tpcc.W;
+    d.strict = (c->cfg.flags & LTPG_CFG_STRICT_INSERT) ? 1u : 0u;
+    return d;
+}
+
+__device__ __forceinline__ uint64_t *col_ptr(const TpccDev &db, uint32_t table, uint64_t row, uint32_t col) {
+    return db.tab[table] + row * tpcc_cols(table) + col;
+}
+__device__ __forceinline__ uint64_t ld_col(const TpccDev &db, uint32_t table, uint64_t row, uint32_t col) {
+    return __ldg(col_ptr(db, table, row, col));
+}
+
+// Field ranges of a transaction record (the keys the reference computes in
+// op_k_0 would silently alias other rows if a field were out of range).
+__device__ __forceinline__ bool txn_valid(const ltpg_tpcc_txn &x, uint32_t W, uint32_t n_lines) {
+    const uint32_t kind = tpcc_kind(x.kind_info);
+    if (x.w >= W || tpcc_d(x.kind_info) >= 10u || x.c_id >= 3000u) return false;
+    if (kind == LTPG_TPCC_NEWORDER) {
+        const uint32_t cnt = tpcc_ol_cnt(x.kind_info);
+        return cnt <= LTPG_TPCC_MAX_LINES && x.a < 30000u && x.b < 30000u && x.c < 450000u &&
+               (uint64_t)x.line_off + cnt <= n_lines;
+    }
+    if (kind == LTPG_TPCC_PAYMENT) return x.c_w < W && tpcc_c_d(x.kind_info) < 10u && x.a < 30000u;
+    return false;
+}
+__device__ __forceinline__ bool line_valid(const ltpg_tpcc_line &ln, uint32_t W) {
+    return ln.i_id < 100000u && ln.supply_w < W;
+}
+
+// ---- table image (Database::initial_data, TF/Database.h:349-451) ------------
+__global__ void tpcc_init_kernel(uint64_t *__restrict__ tab, uint64_t rows, uint32_t cols, uint32_t table,
+                                 uint64_t seed) {
+    const uint64_t total = rows * cols;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        tab[i] = tpcc_init_value(seed, table, i / cols, (uint32_t)(i % cols));
+}
+
+cudaError_t tpcc_init_tables(ltpg_ctx *c) {
+    for (uint32_t t = 0; t < LTPG_TPCC_TABLES; ++t) {
+        tpcc_init_kernel<<<c->sm_count * 8, 256, 0, c->stream>>>(c->tpcc.tab[t], c->tpcc.rows[t], tpcc_cols(t), t,
+                                                                  c->tpcc_seed);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemsetAsync(c->tpcc.reg, 0xFF, c->tpcc.n_slots * sizeof(RegSlot), c->stream);
+}
+
+constexpr uint32_t PT = 64;    // transactions per tile (plain path)
+constexpr uint32_t PBS = 256;  // threads per block (plain path)
+
+struct TileHdr {
+    ltpg_tpcc_txn x[PT];
+    uint32_t off[PT + 1];
+    uint32_t ok[PT];
+};
+
+// Loads a tile and lays out its ops (n_ops_of = ops per transaction).
+template <class F>
+__device__ __forceinline__ uint32_t load_tile(TileHdr &h, const ltpg_tpcc_txn *__restrict__ txns, uint32_t t0,
+                                              uint32_t nt, const TpccDev &db, uint32_t n_lines, DevCtl *ctl,
+                                              F n_ops_of) {
+    if (threadIdx.x < nt) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(txns + t0 + threadIdx.x);
+        const uint4 a = ld_nc_u4(p), b = ld_nc_u4(p + 1);
+        ltpg_tpcc_txn x;
+        x.kind_info = a.x; x.w = a.y; x.c_w = a.z; x.c_id = a.w;
+        x.a = b.x; x.b = b.y; x.c = b.z; x.line_off = b.w;
+        h.x[threadIdx.x] = x;
+        const bool ok = txn_valid(x, db.W, n_lines);
+        if (!ok) report_error(ctl, DERR_BOUNDS, t0 + threadIdx.x);
+        h.ok[threadIdx.x] = ok;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // warp 0: prefix sum of the tile's op counts
+        uint32_t carry = 0;
+        for (uint32_t base = 0; base < nt; base += 32) {
+            const uint32_t i = base + threadIdx.x;
+            const int n = i < nt ? (int)n_ops_of(i) : 0;
+            const int incl = warp_incl_scan(n);
+            if (i < nt) h.off[i] = carry + (uint32_t)(incl - n);
+            carry += (uint32_t)__shfl_sync(FULL, incl, 31);
+        }
+        if (threadIdx.x == 0) h.off[nt] = carry;
+    }
+    __syncthreads();
+    return h.off[nt];
+}
+
+// Transaction of flat op e: the last i with off[i] <= e.
+__device__ __forceinline__ uint32_t tile_owner(const TileHdr &h, uint32_t nt, uint32_t e) {
+    uint32_t lo = 0, hi = nt;  // off[lo] <= e < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (h.off[mid] <= e) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ ltpg_tpcc_line load_line(const ltpg_tpcc_line *__restrict__ lines, uint64_t idx) {
+    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(lines) + idx);
+    ltpg_tpcc_line ln;
+    ln.i_id = v.x;
+    ln.supply_w = (uint16_t)(v.y & 0xFFFFu);
+    ln.qty = (uint16_t)(v.y >> 16);
+    return ln;
+}
+
+// ---- plain phase 1: execute + register (KERNEL_EXECUTE, TF/tp.cu:24-54) ----
+__global__ void __launch_bounds__(PBS) tpcc_exec_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
+                                                       const ltpg_tpcc_line *__restrict__ lines, uint32_t n_lines,
+                                                       TpccDev db, RegSlot *__restrict__ reg,
+                                                       int64_t *__restrict__ results, DevCtl *ctl) {
+    __shared__ TileHdr h;
+    __shared__ unsigned long long sum[PT];
+    __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
+    __shared__ long long res[PT];
+    const uint64_t tag = slot_tag(ctl->epoch);
+    const uint32_t t0 = blockIdx.x * PT, nt = min(PT, B - t0);
+    if (threadIdx.x < PT) sum[threadIdx.x] = 0ull;
+    const uint32_t total = load_tile(h, txns, t0, nt, db, n_lines, ctl,
+                                     [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
+    for (uint32_t e = threadIdx.x; e < total; e += PBS) {
+        const uint32_t i = tile_owner(h, nt, e), j = e - h.off[i];
+        const ltpg_tpcc_txn &x = h.x[i];
+        const bool no = tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER;
+        ltpg_tpcc_line ln{0, 0, 0};
+        if (no && j >= 5) {
+            ln = load_line(lines, (uint64_t)x.line_off + (j - 5) / 3);
+            if (!line_valid(ln, db.W)) {
+                report_error(ctl, DERR_BOUNDS, t0 + i);
+                continue;
+            }
+        }
+        const TpccOp op = tpcc_op(x, j, ln, db.strict);
+        RegSlot *s = reg + db.base[op.table] + op.row;
+        const unsigned long long v = tag | (t0 + i);
+        if (op.flags & OPF_REG_R) red_min(&s->r, v);
+        if (op.flags & OPF_REG_W) red_min(&s->w, v);
+        // Reads of the execute phase (batch-start snapshot).
+        if (no) {
+            if (j == 0) wtax[i] = (uint32_t)ld_col(db, LTPG_T_WAREHOUSE, op.row, W_TAX);
+            else if (j == 1) dtax[i] = (uint32_t)ld_col(db, LTPG_T_DISTRICT, op.row, D_TAX);
+            else if (j == 2) disc[i] = (uint32_t)ld_col(db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
+            else if (op.table == LTPG_T_ITEM)
+                atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(db, LTPG_T_ITEM, op.row, I_PRICE));
+        } else if (j == 2) {
+            res[i] = (long long)ld_col(db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < nt) {
+        const uint32_t i = threadIdx.x;
+        int64_t r = 0;
+        if (h.ok[i])
+            r = tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER
+                    ? neworder_total((int64_t)sum[i], disc[i], wtax[i], dtax[i])
+                    : (int64_t)res[i];
+        results[t0 + i] = r;
+    }
+}
+
+// ---- plain phase 2: check (KERNEL_CHECK, TF/tp.cu:55-85) ---------------------
+__global__ void __launch_bounds__(PBS) tpcc_check_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
+                                                        const ltpg_tpcc_line *__restrict__ lines, uint32_t n_lines,
+                                                        TpccDev db, const RegSlot *__restrict__ reg,
+                                                        uint8_t *__restrict__ flags, DevCtl *ctl) {
+    __shared__ TileHdr h;
+    __shared__ uint32_t fl[PT];
+    const uint32_t epoch = ctl->epoch;
+    const uint32_t t0 = blockIdx.x * PT, nt = min(PT, B - t0);
+    if (threadIdx.x < PT) fl[threadIdx.x] = 0u;
+    const uint32_t total = load_tile(h, txns, t0, nt, db, n_lines, ctl,
+                                     [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
+    for (uint32_t e = threadIdx.x; e < total; e += PBS) {
+        const uint32_t i = tile_owner(h, nt, e), j = e - h.off[i];
+        const ltpg_tpcc_txn &x = h.x[i];
+        ltpg_tpcc_line ln{0, 0, 0};
+        if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER && j >= 5) {
+            ln = load_line(lines, (uint64_t)x.line_off + (j - 5) / 3);
+            if (!line_valid(ln, db.W)) continue;
+        }
+        const TpccOp op = tpcc_op(x, j, ln, db.strict);
+        const ulonglong2 s = ld_slot(reg + db.base[op.table] + op.row);
+        const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch), t = t0 + i;
+        uint32_t f = 0;
+        if ((op.flags & OPF_CHK_RAW) && wmin < t) f |= LTPG_FLAG_RAW;
+        if ((op.flags & OPF_CHK_WAR) && rmin < t) f |= LTPG_FLAG_WAR;
+        if ((op.flags & OPF_CHK_WAW) && wmin < t) f |= LTPG_FLAG_WAW;
+        if (f) atomicOr(&fl[i], f);
+    }
+    __syncthreads();
+    if (threadIdx.x < nt) {
+        uint32_t f = fl[threadIdx.x];
+        if (h.ok[threadIdx.x] && commits(f)) f |= LTPG_FLAG_COMMIT;
+        flags[t0 + threadIdx.x] = (uint8_t)f;
+    }
+}
+
+// Write op q of a committed transaction.  NewOrder: 0 ORDER insert, 1
+// NEW-ORDER insert, 2+2i stock update of line i, 3+2i ORDER-LINE insert of
+// line i.  Payment: 0 W_YTD add, 1 D_YTD add, 2 customer update, 3 HISTORY
+// insert.  Rows written here have exactly one committed writer in the batch
+// (a second one would have seen WAW), so plain read-modify-writes are safe;
+// the YTD adds are commutative and use atomics.
+__device__ __forceinline__ uint32_t tpcc_n_writes(uint32_t kind_info) {
+    return tpcc_kind(kind_info) == LTPG_TPCC_NEWORDER ? 2u + 2u * tpcc_ol_cnt(kind_info) : 4u;
+}
+
+template <bool kHotDirect>
+__device__ __forceinline__ void tpcc_apply_write(const TpccDev &db, const ltpg_tpcc_txn &x, uint32_t q,
+                                                 const ltpg_tpcc_line *__restrict__ lines, uint64_t date,
+                                                 long long *hot_w, long long *hot_d) {
+    const uint32_t d = tpcc_d(x.kind_info);
+    if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
+        const uint32_t cnt = tpcc_ol_cnt(x.kind_info);
+        if (q == 0) {
+            uint64_t *o = col_ptr(db, LTPG_T_ORDER, 30000ull * x.w + x.a, 0);
+            bool all_local = true;
+            for (uint32_t i = 0; i < cnt; ++i) all_local &= load_line(lines, (uint64_t)x.line_off + i).supply_w == x.w;
+            o[O_ID] = x.a; o[O_D_ID] = d; o[O_W_ID] = x.w; o[O_C_ID] = x.c_id;
+            o[O_ENTRY_D] = date; o[O_CARRIER_ID] = 0; o[O_OL_CNT] = cnt; o[O_ALL_LOCAL] = all_local;
+            return;
+        }
+        if (q == 1) {
+            uint64_t *o = col_ptr(db, LTPG_T_NEWORDER, 30000ull * x.w + x.b, 0);
+            o[NO_O_ID] = x.a; o[NO_D_ID] = d; o[NO_W_ID] = x.w;
+            return;
+        }
+        const uint32_t i = (q - 2) / 2;
+        const ltpg_tpcc_line ln = load_line(lines, (uint64_t)x.line_off + i);
+        const uint64_t srow = 100000ull * ln.supply_w + ln.i_id;
+        if ((q & 1u) == 0u) {
+            uint64_t *s = col_ptr(db, LTPG_T_STOCK, srow, 0);
+            s[S_QUANTITY] = stock_after(s[S_QUANTITY], ln.qty);
+            s[S_YTD] += ln.qty;
+            s[S_ORDER_CNT] += 1u;
+            s[S_REMOTE_CNT] += (ln.supply_w != x.w) ? 1u : 0u;
+        } else {
+            uint64_t *o = col_ptr(db, LTPG_T_ORDERLINE, tpcc_ol_row(x.w, x.c, i), 0);
+            o[OL_O_ID] = x.a; o[OL_D_ID] = d; o[OL_W_ID] = x.w; o[OL_NUMBER] = i + 1u;
+            o[OL_I_ID] = ln.i_id; o[OL_SUPPLY_W_ID] = ln.supply_w; o[OL_DELIVERY_D] = 0u;
+            o[OL_QUANTITY] = ln.qty;
+            o[OL_AMOUNT] = (uint64_t)ln.qty * ld_col(db, LTPG_T_ITEM, ln.i_id, I_PRICE);
+            o[OL_DIST_INFO] = ld_col(db, LTPG_T_STOCK, srow, S_DIST_01 + d);
+        }
+        return;
+    }
+    const int64_t amt = tpcc_amount(x);
+    const uint32_t c_d = tpcc_c_d(x.kind_info);
+    if (q == 0) {
+        if (kHotDirect) red_add_u64(reinterpret_cast<unsigned long long *>(col_ptr(db, LTPG_T_WAREHOUSE, x.w, W_YTD)),
+                                    (unsigned long long)amt);
+        else atomicAdd(reinterpret_cast<unsigned long long *>(hot_w + x.w), (unsigned long long)amt);
+    } else if (q == 1) {
+        if (kHotDirect)
+            red_add_u64(reinterpret_cast<unsigned long long *>(col_ptr(db, LTPG_T_DISTRICT, 10ull * x.w + d, D_YTD)),
+                        (unsigned long long)amt);
+        else atomicAdd(reinterpret_cast<unsigned long long *>(hot_d + 10u * x.w + d), (unsigned long long)amt);
+    } else if (q == 2) {
+        uint64_t *cst = col_ptr(db, LTPG_T_CUSTOMER, tpcc_cust_row(x.c_w, c_d, x.c_id), 0);
+        cst[C_BALANCE] = (uint64_t)((int64_t)cst[C_BALANCE] - amt);
+        cst[C_YTD_PAYMENT] = (uint64_t)((int64_t)cst[C_YTD_PAYMENT] + amt);
+        cst[C_PAYMENT_CNT] += 1u;
+    } else {
+        uint64_t *hh = col_ptr(db, LTPG_T_HISTORY, 30000ull * x.w + x.a, 0);
+        hh[H_C_ID] = x.c_id; hh[H_C_D_ID] = c_d; hh[H_C_W_ID] = x.c_w; hh[H_D_ID] = d;
+        hh[H_W_ID] = x.w; hh[H_AMOUNT] = (uint64_t)amt; hh[H_DATE] = date; hh[H_DATA] = 0u;
+    }
+}
+
+// ---- plain phase 3: write-back (KERNEL_WRITEBACK, TF/tp.cu:86-117) ----------
+__global__ void __launch_bounds__(PBS) tpcc_writeback_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
+                                                            const ltpg_tpcc_line *__restrict__ lines,
+                                                            uint32_t n_lines, uint64_t txn_base, TpccDev db,
+                                                            const uint8_t *__restrict__ flags,
+                                                            uint32_t *__restrict__ bitmap, DevStats *st,
+                                                            DevCtl *ctl) {
+    __shared__ TileHdr h;
+    __shared__ uint8_t fl[PT];
+    const uint32_t t0 = blockIdx.x * PT, nt = min(PT, B - t0);
+    if (threadIdx.x < PT) {
+        const uint32_t f = threadIdx.x < nt ? flags[t0 + threadIdx.x] : 0u;
+        fl[threadIdx.x] = (uint8_t)f;
+        const unsigned bal = __ballot_sync(FULL, (f & LTPG_FLAG_COMMIT) != 0u);
+        const unsigned braw = __ballot_sync(FULL, (f & LTPG_FLAG_RAW) != 0u);
+        const unsigned bwar = __ballot_sync(FULL, (f & LTPG_FLAG_WAR) != 0u);
+        const unsigned bwaw = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
+        if ((threadIdx.x & 31) == 0 && threadIdx.x < nt) {
+            bitmap[(t0 + threadIdx.x) >> 5] = bal;
+            if (bal) red_add_u64(&st->commits, __popc(bal));
+            if (braw) red_add_u64(&st->raw, __popc(braw));
+            if (bwar) red_add_u64(&st->war, __popc(bwar));
+            if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
+        }
+    }
+    __syncthreads();
+    const uint32_t total = load_tile(h, txns, t0, nt, db, n_lines, ctl, [&](uint32_t i) {
+        return (h.ok[i] && (fl[i] & LTPG_FLAG_COMMIT)) ? tpcc_n_writes(h.x[i].kind_info) : 0u;
+    });
+    for (uint32_t e = threadIdx.x; e < total; e += PBS) {
+        const uint32_t i = tile_owner(h, nt, e), q = e - h.off[i];
+        tpcc_apply_write<true>(db, h.x[i], q, lines, txn_base + t0 + i, nullptr, nullptr);
+    }
+    finish_batch(ctl);
+}
+
+cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase) {
+    const uint32_t B = s.n_txn;
+    if (B == 0) return cudaSuccess;
+    const TpccDev db = make_dev(c);
+    const uint32_t grid = (B + PT - 1) / PT;
+    if (phase == 0) {
+        cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
+        if (e != cudaSuccess) return e;
+        tpcc_exec_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, db, c->tpcc.reg, s.results,
+                                                     c->ctl);
+    } else if (phase == 1) {
+        tpcc_check_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, db, c->tpcc.reg, s.flags,
+                                                      c->ctl);
+    } else {
+        tpcc_writeback_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, s.txn_base, db, s.flags,
+                                                          s.bitmap, s.stats, c->ctl);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ltpg
+
+namespace ltpg {
+cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
+    (void)mode;
+    for (int p = 0; p < 3; ++p) {
+        cudaError_t e = tpcc_phase(c, s, p);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+}  // namespace ltpg

@@ -1,0 +1,211 @@
+// ycsb.cu — YCSB executor: table image, and the three-phase plain path.
+//
+// Follows YCSB_A_NAMESPACE of the reference (Y1/Execute.h:9-272): reads
+// register in the read table and are checked for RAW, updates register in the
+// write table and are checked for WAR and WAW (Y1/Execute.h:109-150), commit
+// iff !WAW && (!RAW || !WAR) (Y1/Execute.h:187).  Unlike the reference, an
+// update really writes its value into the table, and a read returns a checksum
+// of the row it read.
+#include "devutil.cuh"
+
+namespace ltpg {
+
+// ---- table image (YCSBDatabase::create_table, Y1/Database.h:348-375) --------
+__global__ void ycsb_init_kernel(uint64_t *__restrict__ rows, uint64_t n, uint64_t seed) {
+    const uint64_t total = n * LTPG_YCSB_FIELDS;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        rows[i] = hash3(seed, i / LTPG_YCSB_FIELDS, i % LTPG_YCSB_FIELDS);
+}
+
+cudaError_t ycsb_init_table(ltpg_ctx *c) {
+    const int blocks = c->sm_count * 8;
+    ycsb_init_kernel<<<blocks, 256, 0, c->stream>>>(c->ycsb.rows, c->ycsb.n, c->ycsb_seed);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(c->ycsb.reg, 0xFF, c->ycsb.n * sizeof(RegSlot), c->stream);
+}
+
+// Checksum contribution of read j of a transaction: xor of the row's fields
+// times (2j + 1).
+__device__ __forceinline__ unsigned long long row_digest(const uint64_t *__restrict__ rows, uint32_t key,
+                                                         uint32_t j) {
+    const char *p = reinterpret_cast<const char *>(rows + (uint64_t)key * LTPG_YCSB_FIELDS);
+    ulonglong2 a = ld_nc16(p), b = ld_nc16(p + 16), c = ld_nc16(p + 32), d = ld_nc16(p + 48),
+               e = ld_nc16(p + 64);
+    const unsigned long long x = a.x ^ a.y ^ b.x ^ b.y ^ c.x ^ c.y ^ d.x ^ d.y ^ e.x ^ e.y;
+    return x * (2ull * j + 1ull);
+}
+
+// ---- plain phase 1: execute + register (KERNEL_EXECUTE, Y1/ycsb.cu:9-24) -----
+// One thread per operation; a block holds `tile` whole transactions.
+__global__ void __launch_bounds__(256) ycsb_exec_plain(const uint32_t *__restrict__ ops, uint32_t B, uint32_t k,
+                                                       uint32_t stride, uint32_t tile,
+                                                       const uint64_t *__restrict__ rows, uint64_t n,
+                                                       RegSlot *__restrict__ reg, int64_t *__restrict__ results,
+                                                       DevCtl *ctl) {
+    __shared__ unsigned long long dig[256];
+    const uint64_t tag = slot_tag(ctl->epoch);
+    const uint32_t lt = threadIdx.x / k, j = threadIdx.x % k;
+    const uint32_t t = blockIdx.x * tile + lt;
+    if (threadIdx.x < tile) dig[threadIdx.x] = 0ull;
+    __syncthreads();
+    if (lt < tile && t < B) {
+        const uint32_t w = ops[(uint64_t)t * stride + j];
+        if (!ycsb_is_pad(w)) {
+            const uint32_t key = ycsb_key(w);
+            if (key >= n) {
+                report_error(ctl, DERR_BOUNDS, t);
+            } else if (ycsb_is_update(w)) {
+                red_min(&reg[key].w, tag | t);
+            } else {
+                red_min(&reg[key].r, tag | t);
+                atomicAdd(&dig[lt], row_digest(rows, key, j));
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < tile) {
+        const uint32_t tt = blockIdx.x * tile + threadIdx.x;
+        if (tt < B) results[tt] = (int64_t)dig[threadIdx.x];
+    }
+}
+
+// ---- plain phase 2: check (KERNEL_CHECK, Y1/ycsb.cu:25-40) -------------------
+__global__ void __launch_bounds__(256) ycsb_check_plain(const uint32_t *__restrict__ ops, uint32_t B, uint32_t k,
+                                                        uint32_t stride, uint32_t tile,
+                                                        const RegSlot *__restrict__ reg, uint64_t n,
+                                                        uint8_t *__restrict__ flags, DevCtl *ctl) {
+    __shared__ uint32_t fl[256];
+    const uint32_t epoch = ctl->epoch;
+    const uint32_t lt = threadIdx.x / k, j = threadIdx.x % k;
+    const uint32_t t = blockIdx.x * tile + lt;
+    if (threadIdx.x < tile) fl[threadIdx.x] = 0u;
+    __syncthreads();
+    if (lt < tile && t < B) {
+        const uint32_t w = ops[(uint64_t)t * stride + j];
+        if (!ycsb_is_pad(w) && ycsb_key(w) < n) {
+            const ulonglong2 s = ld_slot(reg + ycsb_key(w));
+            const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch);
+            uint32_t f = 0;
+            if (ycsb_is_update(w)) {
+                if (rmin < t) f |= LTPG_FLAG_WAR;
+                if (wmin < t) f |= LTPG_FLAG_WAW;
+            } else if (wmin < t) {
+                f |= LTPG_FLAG_RAW;
+            }
+            if (f) atomicOr(&fl[lt], f);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < tile) {
+        const uint32_t tt = blockIdx.x * tile + threadIdx.x;
+        if (tt < B) {
+            uint32_t f = fl[threadIdx.x];
+            if (commits(f)) f |= LTPG_FLAG_COMMIT;
+            flags[tt] = (uint8_t)f;
+        }
+    }
+}
+
+// Writes of one committed transaction, found by rank r among its updates.
+__device__ __forceinline__ void ycsb_apply_update(const uint32_t *__restrict__ ops, uint32_t t, uint32_t k,
+                                                  uint32_t stride, uint32_t r, uint64_t value,
+                                                  uint64_t *__restrict__ rows, uint64_t n) {
+    const uint32_t *w = ops + (uint64_t)t * stride;
+    uint32_t seen = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint32_t x = w[j];
+        if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
+        if (seen == r) {
+            const uint32_t key = ycsb_key(x), f = ycsb_field(x);
+            if (key < n && f < LTPG_YCSB_FIELDS) rows[(uint64_t)key * LTPG_YCSB_FIELDS + f] = value;
+            return;
+        }
+        ++seen;
+    }
+}
+
+// ---- plain phase 3: write-back (KERNEL_WRITEBACK, Y1/ycsb.cu:41-58) ----------
+// One thread per transaction.  The commit bitmap word of a warp is its ballot.
+// The warp's committed updates are compacted by a prefix sum over their counts
+// and scattered by all 32 lanes, so idle lanes of aborted or read-only
+// transactions take part in the stores.
+__global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__restrict__ flags, uint32_t B,
+                                                            const uint32_t *__restrict__ ops, uint32_t k,
+                                                            uint32_t stride, const uint32_t *__restrict__ val_off,
+                                                            const uint64_t *__restrict__ vals,
+                                                            uint64_t *__restrict__ rows, uint64_t n,
+                                                            uint32_t *__restrict__ bitmap, DevStats *st,
+                                                            DevCtl *ctl) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const uint32_t f = t < B ? flags[t] : 0u;
+    const bool com = (f & LTPG_FLAG_COMMIT) != 0u;
+    const unsigned bal = __ballot_sync(FULL, com);
+    const unsigned braw = __ballot_sync(FULL, (f & LTPG_FLAG_RAW) != 0u);
+    const unsigned bwar = __ballot_sync(FULL, (f & LTPG_FLAG_WAR) != 0u);
+    const unsigned bwaw = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
+    if (lane == 0 && t < B) {
+        bitmap[t >> 5] = bal;
+        if (bal) red_add_u64(&st->commits, __popc(bal));
+        if (braw) red_add_u64(&st->raw, __popc(braw));
+        if (bwar) red_add_u64(&st->war, __popc(bwar));
+        if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
+    }
+    uint32_t v0 = 0, nu = 0;
+    if (com) {
+        v0 = val_off[t];
+        nu = val_off[t + 1] - v0;
+    }
+    const int incl = warp_incl_scan((int)nu);
+    const unsigned total = (unsigned)__shfl_sync(FULL, incl, 31);
+    const uint32_t t_warp = t - lane;
+    for (unsigned base = 0; base < total; base += 32) {
+        const unsigned e = base + lane;
+        const int L = owner_lane(incl, e);
+        const int excl_L = __shfl_sync(FULL, incl, L) - __shfl_sync(FULL, (int)nu, L);
+        const uint32_t v0_L = (uint32_t)__shfl_sync(FULL, (int)v0, L);
+        if (e < total) {
+            const uint32_t r = e - (unsigned)excl_L;
+            ycsb_apply_update(ops, t_warp + L, k, stride, r, vals[v0_L + r], rows, n);
+        }
+    }
+    finish_batch(ctl);
+}
+
+static inline uint32_t plain_tile(uint32_t k) { return k >= 256 ? 1u : 256u / k; }
+
+cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase) {
+    const uint32_t B = s.n_txn;
+    if (B == 0) return cudaSuccess;
+    const uint32_t tile = plain_tile(s.k);
+    const uint32_t grid = (B + tile - 1) / tile;
+    if (phase == 0) {
+        cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
+        if (e != cudaSuccess) return e;
+        ycsb_exec_plain<<<grid, tile * s.k, 0, c->stream>>>(s.ops, B, s.k, s.stride, tile, c->ycsb.rows,
+                                                            c->ycsb.n, c->ycsb.reg, s.results, c->ctl);
+    } else if (phase == 1) {
+        ycsb_check_plain<<<grid, tile * s.k, 0, c->stream>>>(s.ops, B, s.k, s.stride, tile, c->ycsb.reg,
+                                                             c->ycsb.n, s.flags, c->ctl);
+    } else {
+        ycsb_writeback_plain<<<(B + 255) / 256, 256, 0, c->stream>>>(s.flags, B, s.ops, s.k, s.stride, s.val_off,
+                                                                     s.vals, c->ycsb.rows, c->ycsb.n, s.bitmap,
+                                                                     s.stats, c->ctl);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ltpg
+
+namespace ltpg {
+cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
+    (void)mode;
+    for (int p = 0; p < 3; ++p) {
+        cudaError_t e = ycsb_phase(c, s, p);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+}  // namespace ltpg

@@ -1,0 +1,186 @@
+"""GPU engine vs the oracle, bit-exact, through the C ABI (libltpg.so)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from kat import GOLDEN, load, mask_rows, tpcc_apply_expected, tpcc_batch, ycsb_batch, ycsb_expected_digest
+from ltpg_gb300 import Engine, LtpgError, TpccBatch, TpccGenerator, YcsbBatch, YcsbGenerator, abi
+
+pytestmark = pytest.mark.gpu
+MODES = ["plain", "fused", "persistent", "graph"]
+KY = load("kat_ycsb.json")
+KT = load("kat_tpcc.json")
+
+
+@pytest.fixture(scope="module")
+def eng(gpu):
+    e = Engine(device=0, n_slots=8, max_txn=1 << 17, max_ops_per_txn=32, max_lines=15 << 17)
+    yield e
+    e.close()
+
+
+def run_and_fetch(e, slot, batch, mode):
+    e.upload(slot, batch)
+    e.run_batch(slot, mode)
+    e.sync()
+    return (e.txn_flags(slot, batch.n_txn), e.commit_bitmap(slot, batch.n_txn), e.txn_results(slot, batch.n_txn))
+
+
+def assert_same(got, want):
+    gf, gb, gr = got
+    wf, wb, wr = want[:3]
+    assert np.array_equal(gf, wf), f"flags differ at {np.nonzero(gf != wf)[0][:10]}"
+    assert np.array_equal(gb, wb)
+    assert np.array_equal(gr, wr), f"results differ at {np.nonzero(gr != wr)[0][:10]}"
+
+
+# ---- YCSB -----------------------------------------------------------------------
+@pytest.mark.parametrize("mode", MODES)
+def test_ycsb_known_answers(eng, mode):
+    for case in KY["cases"]:
+        eng.load_ycsb(KY["seed"], KY["n_records"])
+        o = oracle.YcsbOracle(KY["seed"], KY["n_records"])
+        rows0 = o.rows.copy()
+        got = run_and_fetch(eng, 0, ycsb_batch(case), mode)
+        assert got[0].tolist() == case["flags"], case["name"]
+        assert np.array_equal(got[2], ycsb_expected_digest(rows0, case))
+        o.run(ycsb_batch(case))
+        assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows), case["name"]
+
+
+@pytest.mark.parametrize("B,k,upd,theta", [(1, 10, 50, 0.6), (31, 10, 50, 0.6), (32, 16, 50, 0.6),
+                                           (33, 16, 50, 0.9), (1000, 1, 50, 0.99), (1000, 32, 30, 0.99),
+                                           (4099, 7, 50, 0.0), (65536, 10, 50, 0.6)])
+@pytest.mark.parametrize("mode", MODES)
+def test_ycsb_vs_oracle(eng, B, k, upd, theta, mode):
+    n = 50000
+    eng.load_ycsb(17, n)
+    o = oracle.YcsbOracle(17, n)
+    g = YcsbGenerator(17, n, B, k, upd, theta)
+    for bid in range(3):  # several batches: epoch tags, image carried over
+        b = g.batch(bid)
+        got = run_and_fetch(eng, bid % 2, b, mode)
+        assert_same(got, o.run(b))
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+def test_ycsb_golden_fixture(eng):
+    z = np.load(os.path.join(GOLDEN, "gen_ycsb.npz"))
+    p = z["params"]
+    n, B, k = int(p[1]), int(p[2]), int(p[3])
+    eng.load_ycsb(int(p[0]), n)
+    for bid in range(int(z["n_batches"])):
+        b = YcsbBatch(z[f"ops{bid}"], z[f"val_off{bid}"], z[f"vals{bid}"], B, k)
+        got = run_and_fetch(eng, 0, b, "plain")
+        assert_same(got, (z[f"flags{bid}"], z[f"bitmap{bid}"], z[f"results{bid}"]))
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), z["rows_final"])
+
+
+def test_ycsb_graph_over_many_slots(eng):
+    """One CUDA graph over 6 batches in 6 slots, replayed twice; equals the
+    sequential replay of the 12 batches."""
+    n = 30000
+    eng.load_ycsb(5, n)
+    o = oracle.YcsbOracle(5, n)
+    g = YcsbGenerator(5, n, 20000, 16, 10, 0.99)
+    batches = [g.batch(i) for i in range(6)]
+    for rep in range(2):
+        for i, b in enumerate(batches):
+            eng.upload(i, b)
+        eng.run_batches(0, 6, "graph")
+        eng.sync()
+        for i, b in enumerate(batches):
+            want = o.run(b)
+            assert np.array_equal(eng.txn_flags(i, b.n_txn), want[0]), (rep, i)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+def test_ycsb_out_of_range_key_reports_error(eng):
+    eng.load_ycsb(1, 100)
+    bad = YcsbBatch.from_ops([[(3, 0, 0)], [(100, 1, 0)]], [[], [7]])
+    eng.upload(0, bad)
+    eng.run_batch(0, "plain")
+    with pytest.raises(LtpgError) as ei:
+        eng.sync()
+    assert ei.value.code == abi.ERR_BOUNDS
+    # the context stays usable and the table was not touched out of range
+    o = oracle.YcsbOracle(1, 100)
+    ok = YcsbBatch.from_ops([[(3, 1, 2)], [(4, 0, 0)]], [[9], []])
+    assert_same(run_and_fetch(eng, 0, ok, "plain"), o.run(ok))
+
+
+def test_ycsb_host_call_end_to_end(eng):
+    n = 20000
+    eng.load_ycsb(8, n)
+    o = oracle.YcsbOracle(8, n)
+    g = YcsbGenerator(8, n, 10000, 10, 50, 0.8)
+    for bid, mode in enumerate(MODES):
+        b = g.batch(bid)
+        bits = eng.run_host(1, b, mode)
+        assert np.array_equal(bits, o.run(b)[1])
+
+
+# ---- TPC-C --------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def eng_strict(gpu):
+    e = Engine(device=0, n_slots=2, max_txn=1 << 15, max_ops_per_txn=16, max_lines=15 << 15, strict_insert=True)
+    yield e
+    e.close()
+
+
+@pytest.mark.parametrize("strict", [False, True])
+@pytest.mark.parametrize("mode", MODES)
+def test_tpcc_known_answers(eng, eng_strict, strict, mode):
+    e = eng_strict if strict else eng
+    for case in KT["cases"]:
+        e.load_tpcc(KT["seed"], KT["warehouses"])
+        init = [e.download_table(t) for t in range(abi.TPCC_TABLES)]
+        flags = run_and_fetch(e, 0, tpcc_batch(case), mode)[0]
+        assert flags.tolist() == (case["strict_flags"] if strict else case["flags"]), case["name"]
+        want = tpcc_apply_expected(init, case, flags)
+        skip = case.get("unspecified_rows", [])
+        got = mask_rows([e.download_table(t) for t in range(abi.TPCC_TABLES)], skip)
+        want = mask_rows(want, skip)
+        for t in range(abi.TPCC_TABLES):
+            assert np.array_equal(got[t], want[t]), (case["name"], t)
+
+
+@pytest.mark.parametrize("W,B,no_pct", [(1, 1, 50), (1, 33, 50), (1, 4096, 50), (2, 20000, 50), (3, 9000, 100),
+                                        (2, 7000, 0)])
+@pytest.mark.parametrize("mode", MODES)
+def test_tpcc_vs_oracle(eng, W, B, no_pct, mode):
+    eng.load_tpcc(23, W)
+    o = oracle.TpccOracle(23, W)
+    g = TpccGenerator(23, W, B, neworder_pct=no_pct)
+    for bid in range(3):
+        b = g.next()
+        got = run_and_fetch(eng, bid % 2, b, mode)
+        assert_same(got, o.run(b))
+    for t in range(abi.TPCC_TABLES):
+        assert np.array_equal(eng.download_table(t), o.tables[t]), t
+
+
+def test_tpcc_golden_fixture(eng):
+    z = np.load(os.path.join(GOLDEN, "gen_tpcc.npz"))
+    p = z["params"]
+    eng.load_tpcc(int(p[0]), int(p[1]))
+    for bid in range(int(z["n_batches"])):
+        b = TpccBatch(z[f"txns{bid}"].view(TpccBatch.TXN_DTYPE), z[f"lines{bid}"].view(TpccBatch.LINE_DTYPE),
+                      int(z[f"txn_base{bid}"]))
+        got = run_and_fetch(eng, 0, b, "plain")
+        assert_same(got, (z[f"flags{bid}"], z[f"bitmap{bid}"], z[f"results{bid}"]))
+    for t in range(abi.TPCC_TABLES):
+        assert int(np.bitwise_xor.reduce(eng.download_table(t))) == int(z["xor"][t])
+
+
+def test_tpcc_invalid_record_reports_error(eng):
+    eng.load_tpcc(1, 1)
+    case = {"txns": [{"kind": "PAY", "w": 0, "d": 0, "c_w": 0, "c_d": 0, "c_id": 0, "a": 0, "amount": 5},
+                     {"kind": "PAY", "w": 3, "d": 0, "c_w": 0, "c_d": 0, "c_id": 0, "a": 0, "amount": 5}]}
+    eng.upload(0, tpcc_batch(case))
+    eng.run_batch(0, "plain")
+    with pytest.raises(LtpgError) as ei:
+        eng.sync()
+    assert ei.value.code == abi.ERR_BOUNDS
