@@ -271,11 +271,31 @@ int ltpg_batch_stats_get(ltpg_ctx *ctx, uint32_t slot, ltpg_batch_stats *out);
  * on the GPU). */
 int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev_bits);
 
-/* ---- tuning --------------------------------------------------------------- */
-/* Block size and transactions per block-tile used by the tuned kernels of the
- * current workload; 0 keeps the current value. */
-int ltpg_set_launch(ltpg_ctx *ctx, uint32_t block_threads, uint32_t tile_txn, uint32_t stage_ways);
-int ltpg_get_launch(ltpg_ctx *ctx, uint32_t *block_threads, uint32_t *tile_txn, uint32_t *stage_ways);
+/* ---- tuning ----------------------------------------------------------------
+ * Launch shape of the tuned kernels of one workload; the autotuner writes it.
+ * None of these settings can change a commit decision or the table image. */
+typedef struct {
+    uint32_t block_threads;   /* threads per block, multiple of 32, <= 512      */
+    uint32_t vec_per_thread;  /* 16-byte op vectors per thread per tile (YCSB)   */
+    uint32_t blocks_per_sm;   /* cap on resident blocks per SM, 0 = occupancy   */
+    uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
+    uint32_t filter;          /* 1 = read the slot before its atomicMin         */
+    uint32_t reserved;
+} ltpg_launch;
+int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
+int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);
+
+/* ---- measurement ------------------------------------------------------------- */
+/* Totals since ltpg_create: transactions committed (counted on the device by
+ * the write-back kernels) and kernels launched by the engine (a graph launch
+ * counts its kernels). */
+int ltpg_counters(ltpg_ctx *ctx, uint64_t *commits_total, uint64_t *kernel_launches);
+/* When on, every batch run records CUDA events around each of its kernels
+ * (also inside captured graphs); ltpg_kernel_times returns the durations in
+ * milliseconds of the last run of a slot: [execute, check, write-back] for the
+ * plain mode, [execute, check+write-back, 0] for the tuned modes. */
+int ltpg_set_profiling(ltpg_ctx *ctx, int on);
+int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms3);
 
 /* ---- hashing used by generators and the table image --------------------- */
 uint64_t ltpg_splitmix64(uint64_t x);

@@ -109,6 +109,29 @@ class TpccBatch:
         return self.n_txn * 32 + self.n_lines * 8
 
 
+def pinned_copy(batch):
+    """Copy of a batch whose arrays live in pinned host memory (ltpg_host_alloc),
+    so host<->device copies run at full link speed.  Keep the returned object
+    alive while the engine uses it."""
+    def pin(a):
+        n = max(a.nbytes, 16)
+        ptr = lib().ltpg_host_alloc(n)
+        if not ptr:
+            raise MemoryError("ltpg_host_alloc failed")
+        buf = (C.c_char * n).from_address(ptr)
+        out = np.frombuffer(buf, dtype=a.dtype, count=a.size)
+        out[:] = a
+        _PINNED[id(out)] = ptr
+        return out
+
+    if isinstance(batch, YcsbBatch):
+        return YcsbBatch(pin(batch.ops), pin(batch.val_off), pin(batch.vals), batch.n_txn, batch.ops_per_txn)
+    return TpccBatch(pin(batch.txns), pin(batch.lines), batch.txn_base)
+
+
+_PINNED = {}
+
+
 def _check(code, ctx=None):
     if code != abi.OK:
         msg = lib().ltpg_last_error(ctx).decode() if ctx else "invalid argument"
@@ -286,10 +309,32 @@ class Engine:
         self._ck(lib().ltpg_batch_stats_get(self._h, slot, C.byref(s)))
         return {k: getattr(s, k) for k, _ in abi.StatsC._fields_}
 
-    def set_launch(self, block=0, tile=0, ways=0):
-        self._ck(lib().ltpg_set_launch(self._h, block, tile, ways))
+    def set_launch(self, workload, **kw):
+        """Sets fields of the tuned launch shape (block_threads, vec_per_thread,
+        blocks_per_sm, stage_ways, filter) of workload 'ycsb' or 'tpcc'."""
+        wl = abi.WORKLOAD_YCSB if workload == "ycsb" else abi.WORKLOAD_TPCC
+        cur = abi.LaunchC()
+        self._ck(lib().ltpg_get_launch(self._h, wl, C.byref(cur)))
+        for k, v in kw.items():
+            setattr(cur, k, v)
+        self._ck(lib().ltpg_set_launch(self._h, wl, C.byref(cur)))
 
-    def get_launch(self):
-        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
-        self._ck(lib().ltpg_get_launch(self._h, C.byref(a), C.byref(b), C.byref(c)))
-        return a.value, b.value, c.value
+    def get_launch(self, workload):
+        wl = abi.WORKLOAD_YCSB if workload == "ycsb" else abi.WORKLOAD_TPCC
+        cur = abi.LaunchC()
+        self._ck(lib().ltpg_get_launch(self._h, wl, C.byref(cur)))
+        return {k: getattr(cur, k) for k, _ in abi.LaunchC._fields_ if k != "reserved"}
+
+    def counters(self):
+        """(transactions committed, kernels launched) since the engine was created."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._ck(lib().ltpg_counters(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_profiling(self, on=True):
+        self._ck(lib().ltpg_set_profiling(self._h, int(bool(on))))
+
+    def kernel_times(self, slot):
+        out = (C.c_float * 3)()
+        self._ck(lib().ltpg_kernel_times(self._h, slot, out))
+        return list(out)

@@ -46,6 +46,11 @@ class ConfigC(C.Structure):
                 ("max_ops_per_txn", C.c_uint32), ("max_lines", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class LaunchC(C.Structure):
+    _fields_ = [("block_threads", C.c_uint32), ("vec_per_thread", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class StatsC(C.Structure):
     _fields_ = [("n_txn", C.c_uint64), ("commits", C.c_uint64), ("raw", C.c_uint64), ("war", C.c_uint64),
                 ("waw", C.c_uint64), ("staged_ops", C.c_uint64), ("total_ops", C.c_uint64)]
@@ -90,8 +95,11 @@ SIGNATURES = {
     "ltpg_txn_results": (C.c_int, [P, U32, P, SZ]),
     "ltpg_batch_stats_get": (C.c_int, [P, U32, C.POINTER(StatsC)]),
     "ltpg_commit_bitmap_device": (C.c_int, [P, U32, C.POINTER(P)]),
-    "ltpg_set_launch": (C.c_int, [P, U32, U32, U32]),
-    "ltpg_get_launch": (C.c_int, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    "ltpg_set_launch": (C.c_int, [P, C.c_int, C.POINTER(LaunchC)]),
+    "ltpg_get_launch": (C.c_int, [P, C.c_int, C.POINTER(LaunchC)]),
+    "ltpg_counters": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
+    "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
+    "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),
     "ltpg_splitmix64": (U64, [U64]),
     "ltpg_hash3": (U64, [U64, U64, U64]),
 }

@@ -76,8 +76,12 @@ int check_device_error(ltpg_ctx *c) {
     DevCtl h;
     CK(cudaMemcpy(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost), "read control block");
     if (h.error == 0) return LTPG_OK;
-    const uint32_t zero = 0;
-    CK(cudaMemcpy(&c->ctl->error, &zero, sizeof zero, cudaMemcpyHostToDevice), "clear error");
+    // clear the error and any barrier / completion state a failed kernel left
+    h.error = 0;
+    h.err_index = 0;
+    h.done = 0;
+    h.barrier_count = 0;
+    CK(cudaMemcpy(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice), "clear error");
     char buf[160];
     if (h.error & DERR_TIMEOUT) {
         snprintf(buf, sizeof buf, "device wait timed out (index %u)", h.err_index);
@@ -87,12 +91,32 @@ int check_device_error(ltpg_ctx *c) {
     return fail(c, LTPG_ERR_BOUNDS, buf);
 }
 
+int ensure_prof_events(ltpg_ctx *c) {
+    const size_t need = c->slots.size() * 4;
+    while (c->prof_events.size() < need) {
+        cudaEvent_t ev;
+        CK(cudaEventCreate(&ev), "event create");
+        c->prof_events.push_back(ev);
+    }
+    return LTPG_OK;
+}
+
 Slot *get_slot(ltpg_ctx *c, uint32_t slot) {
     if (!c || slot >= c->slots.size()) return nullptr;
     return &c->slots[slot];
 }
 
 }  // namespace
+
+namespace ltpg {
+void prof_mark(ltpg_ctx *c, int i) {
+    if (!c->profiling) return;
+    const size_t k = (size_t)c->cur_slot * 4 + (size_t)i;
+    if (k >= c->prof_events.size()) return;
+    if (c->capturing) cudaEventRecordWithFlags(c->prof_events[k], c->stream, cudaEventRecordExternal);
+    else cudaEventRecord(c->prof_events[k], c->stream);
+}
+}  // namespace ltpg
 
 extern "C" {
 
@@ -134,6 +158,7 @@ int ltpg_destroy(ltpg_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graphs(c);
+    for (auto ev : c->prof_events) cudaEventDestroy(ev);
     for (auto &s : c->slots) free_slot(s);
     dev_free(c->ycsb.rows);
     dev_free(c->ycsb.reg);
@@ -345,6 +370,8 @@ namespace {
 int run_phase(ltpg_ctx *c, uint32_t slot, int phase) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    c->cur_slot = slot;
+    count_launch(c);
     cudaError_t e;
     if (s->workload == LTPG_WORKLOAD_YCSB) e = ycsb_phase(c, *s, phase);
     else if (s->workload == LTPG_WORKLOAD_TPCC) e = tpcc_phase(c, *s, phase);
@@ -356,10 +383,13 @@ int run_phase(ltpg_ctx *c, uint32_t slot, int phase) {
 int run_one(ltpg_ctx *c, uint32_t slot, int mode) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    c->cur_slot = slot;
     if (mode == LTPG_MODE_PLAIN) {
+        prof_mark(c, 0);
         for (int p = 0; p < 3; ++p) {
             int r = run_phase(c, slot, p);
             if (r) return r;
+            prof_mark(c, p + 1);
         }
         return LTPG_OK;
     }
@@ -401,6 +431,7 @@ int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
     for (auto &g : c->graphs)
         if (g.first == first && g.count == count && g.workload == wl) {
             CK(cudaGraphLaunch(g.exec, c->stream), "graph launch");
+            count_launch(c, g.kernels);
             return LTPG_OK;
         }
     // Capture the fused kernels of `count` batches into one graph.  The batch
@@ -408,8 +439,13 @@ int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
     // so the graph can be replayed as is.
     cudaStream_t cap = c->stream;
     CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const uint64_t launches0 = c->launches;
+    c->capturing = true;
     int r = LTPG_OK;
     for (uint32_t i = 0; i < count && r == LTPG_OK; ++i) r = run_one(c, first + i, LTPG_MODE_FUSED);
+    c->capturing = false;
+    const uint64_t kernels = c->launches - launches0;
+    c->launches = launches0;
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(cap, &graph);
     if (r) {
@@ -421,8 +457,9 @@ int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
-    c->graphs.push_back({first, count, wl, exec});
+    c->graphs.push_back({first, count, wl, exec, kernels});
     CK(cudaGraphLaunch(exec, c->stream), "graph launch");
+    count_launch(c, kernels);
     return LTPG_OK;
 }
 
@@ -505,25 +542,72 @@ int ltpg_commit_bitmap_device(ltpg_ctx *c, uint32_t slot, const uint32_t **dev_b
     return LTPG_OK;
 }
 
-int ltpg_set_launch(ltpg_ctx *c, uint32_t block, uint32_t tile, uint32_t ways) {
-    if (!c) return LTPG_ERR_INVALID;
-    if (block && (block % 32 || block > 1024)) return fail(c, LTPG_ERR_INVALID, "block must be a multiple of 32, <= 1024");
-    if (ways > 8) return fail(c, LTPG_ERR_INVALID, "at most 8 staging ways");
-    for (LaunchCfg *l : {&c->launch_y, &c->launch_c}) {
-        if (block) l->block = block;
-        if (tile) l->tile = tile;
-        if (ways) l->ways = ways;
-    }
-    c->persist_blocks_y = c->persist_blocks_c = 0;
+int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
+    if (!c || !cfg) return LTPG_ERR_INVALID;
+    if (workload != LTPG_WORKLOAD_YCSB && workload != LTPG_WORKLOAD_TPCC)
+        return fail(c, LTPG_ERR_INVALID, "unknown workload");
+    if (cfg->block_threads % 32 || cfg->block_threads < 32 || cfg->block_threads > 512)
+        return fail(c, LTPG_ERR_INVALID, "block_threads must be a multiple of 32 in [32, 512]");
+    if (cfg->vec_per_thread < 1 || cfg->vec_per_thread > 8) return fail(c, LTPG_ERR_INVALID, "vec_per_thread in [1, 8]");
+    if (cfg->stage_ways < 1 || cfg->stage_ways > 8) return fail(c, LTPG_ERR_INVALID, "stage_ways in [1, 8]");
+    LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
+    l.block = cfg->block_threads;
+    l.per_thread = cfg->vec_per_thread;
+    l.blocks_per_sm = cfg->blocks_per_sm;
+    l.ways = cfg->stage_ways;
+    l.filter = cfg->filter ? 1u : 0u;
     drop_graphs(c);
     return LTPG_OK;
 }
 
-int ltpg_get_launch(ltpg_ctx *c, uint32_t *block, uint32_t *tile, uint32_t *ways) {
-    if (!c || !block || !tile || !ways) return LTPG_ERR_INVALID;
-    *block = c->launch_y.block;
-    *tile = c->launch_y.tile;
-    *ways = c->launch_y.ways;
+int ltpg_get_launch(ltpg_ctx *c, int workload, ltpg_launch *cfg) {
+    if (!c || !cfg) return LTPG_ERR_INVALID;
+    if (workload != LTPG_WORKLOAD_YCSB && workload != LTPG_WORKLOAD_TPCC)
+        return fail(c, LTPG_ERR_INVALID, "unknown workload");
+    const LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
+    cfg->block_threads = l.block;
+    cfg->vec_per_thread = l.per_thread;
+    cfg->blocks_per_sm = l.blocks_per_sm;
+    cfg->stage_ways = l.ways;
+    cfg->filter = l.filter;
+    cfg->reserved = 0;
+    return LTPG_OK;
+}
+
+int ltpg_counters(ltpg_ctx *c, uint64_t *commits_total, uint64_t *kernel_launches) {
+    if (!c || !commits_total || !kernel_launches) return LTPG_ERR_INVALID;
+    unsigned long long v = 0;
+    CK(cudaMemcpyAsync(&v, &c->ctl->total_commits, sizeof v, cudaMemcpyDeviceToHost, c->stream), "counter download");
+    int r = ltpg_sync(c);
+    if (r) return r;
+    *commits_total = v;
+    *kernel_launches = c->launches;
+    return LTPG_OK;
+}
+
+int ltpg_set_profiling(ltpg_ctx *c, int on) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (on) {
+        int r = ensure_prof_events(c);
+        if (r) return r;
+    }
+    if (c->profiling != (on != 0)) drop_graphs(c);
+    c->profiling = on != 0;
+    return LTPG_OK;
+}
+
+int ltpg_kernel_times(ltpg_ctx *c, uint32_t slot, float *ms3) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !ms3) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (!c->profiling) return fail(c, LTPG_ERR_STATE, "profiling is off");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    cudaEvent_t *ev = &c->prof_events[(size_t)slot * 4];
+    for (int i = 0; i < 3; ++i) {
+        float ms = 0.f;
+        cudaError_t e = cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        ms3[i] = e == cudaSuccess ? ms : 0.f;
+        if (e != cudaSuccess) cudaGetLastError();
+    }
     return LTPG_OK;
 }
 

@@ -25,6 +25,8 @@ struct DevCtl {
     uint32_t barrier_count;
     uint32_t barrier_gen;
     uint32_t pad[2];
+    unsigned long long total_commits;
+    unsigned long long pad2;
 };
 constexpr uint32_t DERR_BOUNDS = 1u;
 constexpr uint32_t DERR_TIMEOUT = 2u;
@@ -79,9 +81,11 @@ struct Slot {
 };
 
 struct LaunchCfg {
-    uint32_t block = 256;   // threads per block of the tuned kernels
-    uint32_t tile = 0;      // transactions per block tile (0 = derived)
-    uint32_t ways = 4;      // shared-memory staging ways per bucket
+    uint32_t block = 256;        // threads per block of the tuned kernels
+    uint32_t per_thread = 2;     // 16-byte op vectors per thread per tile (YCSB)
+    uint32_t blocks_per_sm = 0;  // cap on resident blocks per SM (0 = occupancy)
+    uint32_t ways = 4;           // shared-memory staging entries per hot bucket
+    uint32_t filter = 1;         // read the slot before its atomicMin
 };
 
 }  // namespace ltpg
@@ -105,17 +109,28 @@ struct ltpg_ctx {
     uint16_t *stage_map = nullptr;
     uint32_t *bucket_counts = nullptr;  // per-batch access counts per bucket
     uint32_t stage_on = 0;
+    // measurement
+    uint64_t launches = 0;
+    bool profiling = false;
+    bool capturing = false;
+    uint32_t cur_slot = 0;
+    std::vector<cudaEvent_t> prof_events;  // 4 per slot
     // cached CUDA graphs keyed by (first, count, workload)
     struct GraphEntry {
         uint32_t first, count;
         int workload;
         cudaGraphExec_t exec;
+        uint64_t kernels;
     };
     std::vector<GraphEntry> graphs;
 };
 
 // Kernel launchers implemented in ycsb.cu / tpcc.cu.
 namespace ltpg {
+// Records profiling event i (0..3) of the slot being run, if profiling is on.
+void prof_mark(ltpg_ctx *c, int i);
+// Counts kernels launched by the engine.
+inline void count_launch(ltpg_ctx *c, uint64_t n = 1) { c->launches += n; }
 cudaError_t ycsb_init_table(ltpg_ctx *c);
 cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase);      // 0 exec, 1 check, 2 write-back
 cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode);   // fused / persistent

@@ -322,7 +322,10 @@ __global__ void __launch_bounds__(PBS) tpcc_writeback_plain(const ltpg_tpcc_txn 
         const unsigned bwaw = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
         if ((threadIdx.x & 31) == 0 && threadIdx.x < nt) {
             bitmap[(t0 + threadIdx.x) >> 5] = bal;
-            if (bal) red_add_u64(&st->commits, __popc(bal));
+            if (bal) {
+                red_add_u64(&st->commits, __popc(bal));
+                red_add_u64(&ctl->total_commits, __popc(bal));
+            }
             if (braw) red_add_u64(&st->raw, __popc(braw));
             if (bwar) red_add_u64(&st->war, __popc(bwar));
             if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
@@ -361,13 +364,284 @@ cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase) {
 
 }  // namespace ltpg
 
+
+// ============================================================================
+// Tuned path: the same tiles, with deduplicated + filtered registration, check
+// and write-back fused, and the hot W_YTD / D_YTD adds of a block summed in
+// shared memory and flushed once per block (one atomic per warehouse and per
+// district instead of one per Payment).
+// ============================================================================
+#include "stage.cuh"
+
 namespace ltpg {
-cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
-    (void)mode;
-    for (int p = 0; p < 3; ++p) {
-        cudaError_t e = tpcc_phase(c, s, p);
-        if (e != cudaSuccess) return e;
+
+constexpr uint32_t HOT_SMEM_MAX_W = 256;  // shared-memory YTD sums up to 256 warehouses
+
+struct TpccTunedArgs {
+    const ltpg_tpcc_txn *txns;
+    const ltpg_tpcc_line *lines;
+    uint32_t B, n_lines;
+    uint64_t txn_base;
+    TpccDev db;
+    RegSlot *reg;
+    int64_t *results;
+    uint8_t *flags;
+    uint32_t *bitmap;
+    DevStats *st;
+    DevCtl *ctl;
+    uint32_t filter;
+};
+
+__device__ __forceinline__ uint64_t ld_ca_u64t(const unsigned long long *p) {
+    uint64_t v;
+    asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr &h, uint64_t tag) {
+    __shared__ unsigned long long sum[PT];
+    __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
+    __shared__ long long res[PT];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
+        if (threadIdx.x < PT) sum[threadIdx.x] = 0ull;
+        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, a.n_lines, a.ctl,
+                                         [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
+        for (uint32_t base = 0; base < total; base += blockDim.x) {
+            const uint32_t e = base + threadIdx.x;
+            const bool act = e < total;
+            uint32_t i = 0, j = 0;
+            bool valid = act;
+            ltpg_tpcc_line ln{0, 0, 0};
+            TpccOp op{0, 0, 0};
+            if (act) {
+                i = tile_owner(h, nt, e);
+                j = e - h.off[i];
+                if (tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER && j >= 5) {
+                    ln = load_line(a.lines, (uint64_t)h.x[i].line_off + (j - 5) / 3);
+                    if (!line_valid(ln, a.db.W)) {
+                        report_error(a.ctl, DERR_BOUNDS, t0 + i);
+                        valid = false;
+                    }
+                }
+                if (valid) op = tpcc_op(h.x[i], j, ln, a.db.strict);
+            }
+            const uint64_t slot_idx = a.db.base[op.table] + op.row;
+            const unsigned long long mkey =
+                valid ? (slot_idx << 2) | ((op.flags & OPF_REG_W) ? 2ull : 1ull) : ~0ull;
+            const unsigned peers = __match_any_sync(FULL, mkey);
+            if (valid && (__ffs(peers) - 1) == (int)lane) {
+                RegSlot *s = a.reg + slot_idx;
+                unsigned long long *p = (op.flags & OPF_REG_W) ? &s->w : &s->r;
+                const unsigned long long mine = tag | (t0 + i);
+                if (!a.filter || ld_ca_u64t(p) > mine) red_min(p, mine);
+            }
+            if (valid) {
+                const ltpg_tpcc_txn &x = h.x[i];
+                if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
+                    if (j == 0) wtax[i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, op.row, W_TAX);
+                    else if (j == 1) dtax[i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, op.row, D_TAX);
+                    else if (j == 2) disc[i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
+                    else if (op.table == LTPG_T_ITEM)
+                        atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(a.db, LTPG_T_ITEM, op.row, I_PRICE));
+                } else if (j == 2) {
+                    res[i] = (long long)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < nt) {
+            const uint32_t i = threadIdx.x;
+            int64_t r = 0;
+            if (h.ok[i])
+                r = tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER
+                        ? neworder_total((int64_t)sum[i], disc[i], wtax[i], dtax[i])
+                        : (int64_t)res[i];
+            a.results[t0 + i] = r;
+        }
+        __syncthreads();
     }
+}
+
+// hot: 11 W int64 sums in shared memory (W <= HOT_SMEM_MAX_W), or null.
+__device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdr &h, uint32_t epoch,
+                                                   long long *hot) {
+    __shared__ uint32_t fl[PT];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    unsigned long long c_com = 0, c_raw = 0, c_war = 0, c_waw = 0;
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
+        if (threadIdx.x < PT) fl[threadIdx.x] = 0u;
+        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, a.n_lines, a.ctl,
+                                         [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
+        for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+            const uint32_t i = tile_owner(h, nt, e), j = e - h.off[i];
+            const ltpg_tpcc_txn &x = h.x[i];
+            ltpg_tpcc_line ln{0, 0, 0};
+            if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER && j >= 5) {
+                ln = load_line(a.lines, (uint64_t)x.line_off + (j - 5) / 3);
+                if (!line_valid(ln, a.db.W)) continue;
+            }
+            const TpccOp op = tpcc_op(x, j, ln, a.db.strict);
+            const ulonglong2 s = ld_slot(a.reg + a.db.base[op.table] + op.row);
+            const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch), t = t0 + i;
+            uint32_t f = 0;
+            if ((op.flags & OPF_CHK_RAW) && wmin < t) f |= LTPG_FLAG_RAW;
+            if ((op.flags & OPF_CHK_WAR) && rmin < t) f |= LTPG_FLAG_WAR;
+            if ((op.flags & OPF_CHK_WAW) && wmin < t) f |= LTPG_FLAG_WAW;
+            if (f) atomicOr(&fl[i], f);
+        }
+        __syncthreads();
+        if (threadIdx.x < PT) {
+            uint32_t f = threadIdx.x < nt ? fl[threadIdx.x] : 0u;
+            const bool com = threadIdx.x < nt && h.ok[threadIdx.x] && commits(f);
+            if (com) f |= LTPG_FLAG_COMMIT;
+            if (threadIdx.x < nt) {
+                a.flags[t0 + threadIdx.x] = (uint8_t)f;
+                fl[threadIdx.x] = f;
+            }
+            const unsigned bal = __ballot_sync(FULL, com);
+            const unsigned braw = __ballot_sync(FULL, (f & LTPG_FLAG_RAW) != 0u);
+            const unsigned bwar = __ballot_sync(FULL, (f & LTPG_FLAG_WAR) != 0u);
+            const unsigned bwaw = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
+            if (lane == 0 && threadIdx.x < nt) {
+                a.bitmap[(t0 + threadIdx.x) >> 5] = bal;
+                c_com += __popc(bal);
+                c_raw += __popc(braw);
+                c_war += __popc(bwar);
+                c_waw += __popc(bwaw);
+            }
+        }
+        __syncthreads();
+        // committed write ops, laid out back to back (ballot/prefix compaction)
+        if (threadIdx.x < 32) {
+            uint32_t carry = 0;
+            for (uint32_t b0 = 0; b0 < nt; b0 += 32) {
+                const uint32_t i = b0 + threadIdx.x;
+                const int n = (i < nt && (fl[i] & LTPG_FLAG_COMMIT)) ? (int)tpcc_n_writes(h.x[i].kind_info) : 0;
+                const int incl = warp_incl_scan(n);
+                if (i < nt) h.off[i] = carry + (uint32_t)(incl - n);
+                carry += (uint32_t)__shfl_sync(FULL, incl, 31);
+            }
+            if (threadIdx.x == 0) h.off[nt] = carry;
+        }
+        __syncthreads();
+        const uint32_t wtotal = h.off[nt];
+        for (uint32_t e = threadIdx.x; e < wtotal; e += blockDim.x) {
+            const uint32_t i = tile_owner(h, nt, e);
+            if (hot) tpcc_apply_write<false>(a.db, h.x[i], e - h.off[i], a.lines, a.txn_base + t0 + i, hot,
+                                             hot + a.db.W);
+            else tpcc_apply_write<true>(a.db, h.x[i], e - h.off[i], a.lines, a.txn_base + t0 + i, nullptr,
+                                        nullptr);
+        }
+        __syncthreads();
+    }
+    if (lane == 0) {
+        if (c_com) {
+            red_add_u64(&a.st->commits, c_com);
+            red_add_u64(&a.ctl->total_commits, c_com);
+        }
+        if (c_raw) red_add_u64(&a.st->raw, c_raw);
+        if (c_war) red_add_u64(&a.st->war, c_war);
+        if (c_waw) red_add_u64(&a.st->waw, c_waw);
+    }
+}
+
+__device__ __forceinline__ void hot_init(long long *hot, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) hot[i] = 0;
+    __syncthreads();
+}
+__device__ __forceinline__ void hot_flush(const TpccDev &db, const long long *hot) {
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < 11u * db.W; i += blockDim.x) {
+        const long long v = hot[i];
+        if (!v) continue;
+        uint64_t *p = i < db.W ? col_ptr(db, LTPG_T_WAREHOUSE, i, W_YTD) : col_ptr(db, LTPG_T_DISTRICT, i - db.W, D_YTD);
+        red_add_u64(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+    }
+}
+
+__global__ void __launch_bounds__(PBS) tpcc_exec_tuned(TpccTunedArgs a) {
+    __shared__ TileHdr h;
+    tpcc_exec_tiles(a, h, slot_tag(a.ctl->epoch));
+}
+
+__global__ void __launch_bounds__(PBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
+    __shared__ TileHdr h;
+    extern __shared__ __align__(16) long long hot_dyn[];
+    long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
+    if (hot) hot_init(hot, 11u * a.db.W);
+    tpcc_checkwb_tiles(a, h, a.ctl->epoch, hot);
+    if (hot) hot_flush(a.db, hot);
+    finish_batch(a.ctl);
+}
+
+__global__ void __launch_bounds__(PBS) tpcc_persistent(TpccTunedArgs a) {
+    __shared__ TileHdr h;
+    extern __shared__ __align__(16) long long hot_dyn[];
+    long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
+    const uint32_t epoch = a.ctl->epoch;
+    if (hot) hot_init(hot, 11u * a.db.W);
+    tpcc_exec_tiles(a, h, slot_tag(epoch));
+    if (grid_barrier(a.ctl, 2000000000ull)) tpcc_checkwb_tiles(a, h, epoch, hot);
+    if (hot) hot_flush(a.db, hot);
+    finish_batch(a.ctl);
+}
+
+cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
+    if (s.n_txn == 0) return cudaSuccess;
+    TpccTunedArgs a;
+    a.txns = s.txns;
+    a.lines = s.lines;
+    a.B = s.n_txn;
+    a.n_lines = s.n_lines;
+    a.txn_base = s.txn_base;
+    a.db = make_dev(c);
+    a.reg = c->tpcc.reg;
+    a.results = s.results;
+    a.flags = s.flags;
+    a.bitmap = s.bitmap;
+    a.st = s.stats;
+    a.ctl = c->ctl;
+    a.filter = c->launch_c.filter;
+    const size_t smem = a.db.W <= HOT_SMEM_MAX_W ? 11u * a.db.W * sizeof(long long) : 0u;
+    cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mode == LTPG_MODE_PERSISTENT
+                                                                  ? (const void *)tpcc_persistent
+                                                                  : (const void *)tpcc_checkwb_tuned,
+                                                      PBS, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (c->launch_c.blocks_per_sm && (int)c->launch_c.blocks_per_sm < per_sm) per_sm = (int)c->launch_c.blocks_per_sm;
+    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm * c->sm_count));
+    if (mode == LTPG_MODE_PERSISTENT) {
+        prof_mark(c, 0);
+        void *args[] = {&a};
+        count_launch(c);
+        e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent, dim3(grid), dim3(PBS), args, smem, c->stream);
+        if (e != cudaSuccess) return e;
+        prof_mark(c, 1);
+        prof_mark(c, 2);
+        prof_mark(c, 3);
+        return cudaSuccess;
+    }
+    prof_mark(c, 0);
+    count_launch(c);
+    tpcc_exec_tuned<<<grid, PBS, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 1);
+    count_launch(c);
+    tpcc_checkwb_tuned<<<grid, PBS, smem, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 2);
+    prof_mark(c, 3);
     return cudaSuccess;
 }
+
 }  // namespace ltpg

@@ -148,7 +148,10 @@ __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__res
     const unsigned bwaw = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
     if (lane == 0 && t < B) {
         bitmap[t >> 5] = bal;
-        if (bal) red_add_u64(&st->commits, __popc(bal));
+        if (bal) {
+            red_add_u64(&st->commits, __popc(bal));
+            red_add_u64(&ctl->total_commits, __popc(bal));
+        }
         if (braw) red_add_u64(&st->raw, __popc(braw));
         if (bwar) red_add_u64(&st->war, __popc(bwar));
         if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
@@ -199,13 +202,3 @@ cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase) {
 
 }  // namespace ltpg
 
-namespace ltpg {
-cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
-    (void)mode;
-    for (int p = 0; p < 3; ++p) {
-        cudaError_t e = ycsb_phase(c, s, p);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-}  // namespace ltpg
