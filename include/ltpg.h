@@ -297,6 +297,32 @@ int ltpg_counters(ltpg_ctx *ctx, uint64_t *commits_total, uint64_t *kernel_launc
 int ltpg_set_profiling(ltpg_ctx *ctx, int on);
 int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms3);
 
+/* ---- no-allocation batch -------------------------------------------------------
+ * This entry point has no counterpart in the reference.  It runs one whole YCSB
+ * batch (execute+register, check, write-back) on buffers the caller owns, and
+ * allocates no device memory.  It is for callers that cannot call cudaMalloc:
+ * a host runtime that owns all of the GPU's memory through its own fixed pool
+ * (a database or serving process), or a latency-critical thread, where
+ * cudaMalloc / cudaFree may block and cudaFree synchronises the whole device.
+ * All pointers are device pointers: rows (n_records x 10 uint64, updated in
+ * place), the batch arrays in the layout of ltpg_ycsb_batch, and the outputs
+ * flags[n_txn], bitmap[(n_txn+31)/32], results[n_txn].  stream may be NULL.
+ * Scratch (the registration table) is a static device array sized for at most
+ * LTPG_NOALLOC_MAX_RECORDS records (16 MiB), held on every GPU that loads the
+ * library until exit; larger tables are rejected with LTPG_ERR_INVALID.  The
+ * first call on a device sets that device up (it resolves the array's device
+ * address and initialises it), so make that first call before any stream
+ * capture.  All calls share the one scratch array, which keeps the previous
+ * call's contents (calls are told apart by an epoch tag, and the batch counters
+ * are cleared by each call): calls that overlap on the GPU race and give wrong
+ * results, so issue them one at a time.  Returns after the batch has finished;
+ * LTPG_ERR_BOUNDS if a key was out of range. */
+#define LTPG_NOALLOC_MAX_RECORDS (1u << 20)
+int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_records, const uint32_t *ops,
+                            const uint32_t *val_off, const uint64_t *vals, uint32_t n_txn,
+                            uint32_t ops_per_txn, uint8_t *flags, uint32_t *bitmap, int64_t *results,
+                            void *stream);
+
 /* ---- hashing used by generators and the table image --------------------- */
 uint64_t ltpg_splitmix64(uint64_t x);
 uint64_t ltpg_hash3(uint64_t seed, uint64_t a, uint64_t b);

@@ -18,6 +18,7 @@ TPCC_COLS = (9, 11, 21, 8, 3, 8, 10, 17, 5)
 TPCC_NEWORDER, TPCC_PAYMENT = 0, 1
 TPCC_MAX_LINES = 15
 CFG_STRICT_INSERT = 1
+NOALLOC_MAX_RECORDS = 1 << 20
 
 
 class YcsbBatchC(C.Structure):
@@ -100,6 +101,7 @@ SIGNATURES = {
     "ltpg_counters": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
     "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),
+    "ltpg_ycsb_batch_noalloc": (C.c_int, [C.c_int, P, U64, P, P, P, U32, U32, P, P, P, P]),
     "ltpg_splitmix64": (U64, [U64]),
     "ltpg_hash3": (U64, [U64, U64, U64]),
 }
