@@ -34,6 +34,10 @@ WORKLOADS = {
                     rotate_every=8, n_batches=32,
                     name="YCSB high contention: 10M x 10 uint64, 1,048,576 txn x 16 ops, 95/5, "
                          "Zipf theta=0.99, hot set rotating every 8 batches, 32 batches"),
+    "ycsb_hc_prof": dict(kind="ycsb", n_records=10_000_000, n_txn=1 << 18, ops=16, update_pct=5, theta=0.99,
+                         rotate_every=8, n_batches=4,
+                         name="YCSB high contention, profiling size: 10M x 10 uint64, 262,144 txn x 16 ops, "
+                              "95/5, Zipf theta=0.99, 4 batches"),
     "ycsb_small": dict(kind="ycsb", n_records=1_000_000, n_txn=65536, ops=10, update_pct=50, theta=0.6,
                        rotate_every=0, n_batches=32,
                        name="YCSB small: 1M x 10 uint64, 65,536 txn x 10 ops, 50/50, Zipf theta=0.6"),
@@ -212,10 +216,17 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
     eng = L.Engine(device=0, n_slots=n_slots, max_txn=w["n_txn"], max_ops_per_txn=w["ops"])
     res = {}
     try:
+        eng.load_ycsb(SEED, w["n_records"])
+        for i, b in enumerate(batches):
+            eng.upload(i, b)
         for mode in ["plain", args.mode]:
+            if mode != "plain":
+                from ltpg_gb300 import tune
+                wkey = f"{args.workload}|theta={theta}"
+                cfg, how = tune.apply_cached_or_tune(eng, "ycsb", wkey, list(range(min(8, n_slots))),
+                                                     lambda: eng.load_ycsb(SEED, w["n_records"]))
+                res["launch"] = dict(cfg, source=how)
             eng.load_ycsb(SEED, w["n_records"])
-            for i, b in enumerate(batches):
-                eng.upload(i, b)
             eng.sync()
             nxt = run_steps(eng, n_slots, args.warmup, mode)
             if mode != "plain" and want_extras:
@@ -227,6 +238,16 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                 kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
                 eng.set_profiling(False)
             res[mode] = dict(secs=secs, commits=commits, launches=launches, clocks=clk.summary(), kt=kt)
+        # access-pattern ceilings of this GPU (the practical rooflines of the kernels' parts)
+        if want_extras:
+            res["ceilings"] = {
+                "copy_GBs": eng.microbench("copy", 1 << 27) / 1e9,
+                "row_gather_5lane_GBs": eng.microbench("gather_coop", 16_000_000) / 1e9,
+                "row_gather_1thread_GBs": eng.microbench("gather_thread", 16_000_000) / 1e9,
+                "slot_load_G_per_s": eng.microbench("slot_load", 16_000_000) / 1e9,
+                "red_min_random_G_per_s": eng.microbench("red_random", 16_000_000) / 1e9,
+                "red_min_one_slot_G_per_s": eng.microbench("red_hot", 1_000_000) / 1e9,
+            }
         # bit-exactness of the tuned path against the plain path on the first batches
         exact = True
         if want_extras:
@@ -288,10 +309,16 @@ def tpcc_bench(args, w, dist, want_extras=True):
     eng = L.Engine(device=0, n_slots=n_slots, max_txn=w["n_txn"], max_ops_per_txn=16, max_lines=max_lines)
     res = {}
     try:
+        eng.load_tpcc(SEED, w["warehouses"])
+        for i, b in enumerate(batches):
+            eng.upload(i, b)
         for mode in ["plain", args.mode]:
+            if mode != "plain":
+                from ltpg_gb300 import tune
+                cfg, how = tune.apply_cached_or_tune(eng, "tpcc", args.workload, list(range(min(4, n_slots))),
+                                                     lambda: eng.load_tpcc(SEED, w["warehouses"]))
+                res["launch"] = dict(cfg, source=how)
             eng.load_tpcc(SEED, w["warehouses"])
-            for i, b in enumerate(batches):
-                eng.upload(i, b)
             eng.sync()
             nxt = run_steps(eng, n_slots, args.warmup, mode)
             if mode != "plain":
@@ -416,6 +443,8 @@ def main():
         theta = None
         res, exact, e2e, batches = tpcc_bench(args, w, dist)
     tuned, plain = res[args.mode], res["plain"]
+    launch = res.get("launch")
+    ceilings = res.get("ceilings")
     secs = reduce_max(dist, tuned["secs"])
     commits = reduce_sum(dist, tuned["commits"])
     value = commits / secs
@@ -455,10 +484,12 @@ def main():
                      "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_txn": kbytes,
                      "traffic": traffic * B if traffic else None,
-                     "kernel_ms": {"execute": exec_ms, "check_writeback": cwb_ms}},
+                     "kernel_ms": {"execute": exec_ms, "check_writeback": cwb_ms},
+                     "pattern_ceilings": ceilings},
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"]},
         "gpu_launches": int(tuned["launches"]),
+        "launch": launch,
         "clocks": tuned["clocks"],
     }
     if not args.no_cpu_baseline:

@@ -276,14 +276,30 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
  * None of these settings can change a commit decision or the table image. */
 typedef struct {
     uint32_t block_threads;   /* threads per block, multiple of 32, <= 512      */
-    uint32_t vec_per_thread;  /* 16-byte op vectors per thread per tile (YCSB)   */
+    uint32_t ops_per_thread;  /* YCSB op words per thread: 1, 2, 4 or 8         */
     uint32_t blocks_per_sm;   /* cap on resident blocks per SM, 0 = occupancy   */
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
     uint32_t filter;          /* 1 = read the slot before its atomicMin         */
-    uint32_t reserved;
+    uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any)    */
 } ltpg_launch;
 int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
 int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);
+
+/* ---- hot-key staging ----------------------------------------------------------
+ * Keys hash into LTPG_STAGE_BUCKETS buckets (ltpg_key_bucket).  Registrations of
+ * keys in a staged bucket are combined in shared memory per block and reach the
+ * global slot table as one atomic per key and block.  The staged set is chosen
+ * by the contention predictor or given here; it changes speed only, never a
+ * commit decision.  n = 0 turns staging off.  At most
+ * LTPG_STAGE_ENTRIES / stage_ways buckets are staged (extra ones are ignored). */
+#define LTPG_STAGE_BUCKETS 65536u
+#define LTPG_STAGE_ENTRIES 4096u
+uint32_t ltpg_key_bucket(uint32_t key);
+int ltpg_stage_set(ltpg_ctx *ctx, const uint32_t *buckets, uint32_t n);
+/* Per-bucket registration counts accumulated by the tuned execute kernels
+ * since the last reset (exact for staged buckets, sampled 1 in 16 and scaled
+ * for the others): LTPG_STAGE_BUCKETS uint32 values. */
+int ltpg_bucket_counts(ltpg_ctx *ctx, uint32_t *host_counts, int reset);
 
 /* ---- measurement ------------------------------------------------------------- */
 /* Totals since ltpg_create: transactions committed (counted on the device by
@@ -322,6 +338,15 @@ int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_records, cons
                             const uint32_t *val_off, const uint64_t *vals, uint32_t n_txn,
                             uint32_t ops_per_txn, uint8_t *flags, uint32_t *bitmap, int64_t *results,
                             void *stream);
+
+/* ---- access-pattern ceilings --------------------------------------------------
+ * Runs one access pattern of the engine's kernels alone and reports its rate:
+ * kind 0 streaming copy (bytes/s, read + write), 1 random 80-byte row reads by
+ * one thread per row (useful bytes/s), 2 the same with five lanes per row,
+ * 3 random 16-byte slot loads (loads/s), 4 atomicMin on random slots
+ * (atomics/s), 5 atomicMin on one slot (atomics/s).  n_items = rows, loads or
+ * atomics per launch (kind 0: 16-byte elements); iters = timed launches. */
+int ltpg_microbench(ltpg_ctx *ctx, int kind, uint64_t n_items, uint32_t iters, double *rate);
 
 /* ---- hashing used by generators and the table image --------------------- */
 uint64_t ltpg_splitmix64(uint64_t x);

@@ -48,6 +48,12 @@ def _p(a):
     return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
 
 
+def key_bucket(keys):
+    """Key-hash bucket of each key (the staging / predictor granularity)."""
+    k = np.asarray(keys, dtype=np.uint64)
+    return (((k * np.uint64(0x9E3779B1)) & np.uint64(0xFFFFFFFF)) >> np.uint64(16)).astype(np.uint32)
+
+
 class YcsbBatch:
     """A YCSB batch in the engine's format (see include/ltpg.h)."""
 
@@ -310,8 +316,8 @@ class Engine:
         return {k: getattr(s, k) for k, _ in abi.StatsC._fields_}
 
     def set_launch(self, workload, **kw):
-        """Sets fields of the tuned launch shape (block_threads, vec_per_thread,
-        blocks_per_sm, stage_ways, filter) of workload 'ycsb' or 'tpcc'."""
+        """Sets fields of the tuned launch shape (block_threads, ops_per_thread,
+        blocks_per_sm, stage_ways, filter, dedupe) of workload 'ycsb' or 'tpcc'."""
         wl = abi.WORKLOAD_YCSB if workload == "ycsb" else abi.WORKLOAD_TPCC
         cur = abi.LaunchC()
         self._ck(lib().ltpg_get_launch(self._h, wl, C.byref(cur)))
@@ -323,13 +329,32 @@ class Engine:
         wl = abi.WORKLOAD_YCSB if workload == "ycsb" else abi.WORKLOAD_TPCC
         cur = abi.LaunchC()
         self._ck(lib().ltpg_get_launch(self._h, wl, C.byref(cur)))
-        return {k: getattr(cur, k) for k, _ in abi.LaunchC._fields_ if k != "reserved"}
+        return {k: getattr(cur, k) for k, _ in abi.LaunchC._fields_}
+
+    def stage_set(self, buckets):
+        """Stages the given key-hash buckets in shared memory (empty list: off)."""
+        arr = np.ascontiguousarray(buckets, dtype=np.uint32)
+        self._ck(lib().ltpg_stage_set(self._h, _p(arr) if len(arr) else None, len(arr)))
+
+    def bucket_counts(self, reset=False):
+        out = np.empty(abi.STAGE_BUCKETS, dtype=np.uint32)
+        self._ck(lib().ltpg_bucket_counts(self._h, _p(out), int(bool(reset))))
+        return out
 
     def counters(self):
         """(transactions committed, kernels launched) since the engine was created."""
         a, b = C.c_uint64(), C.c_uint64()
         self._ck(lib().ltpg_counters(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    MICROBENCH = {"copy": 0, "gather_thread": 1, "gather_coop": 2, "slot_load": 3, "red_random": 4,
+                  "red_hot": 5}
+
+    def microbench(self, kind, n_items, iters=5):
+        """Rate of one access pattern alone (see ltpg_microbench in include/ltpg.h)."""
+        out = C.c_double()
+        self._ck(lib().ltpg_microbench(self._h, self.MICROBENCH[kind], n_items, iters, C.byref(out)))
+        return out.value
 
     def set_profiling(self, on=True):
         self._ck(lib().ltpg_set_profiling(self._h, int(bool(on))))

@@ -19,6 +19,8 @@ TPCC_NEWORDER, TPCC_PAYMENT = 0, 1
 TPCC_MAX_LINES = 15
 CFG_STRICT_INSERT = 1
 NOALLOC_MAX_RECORDS = 1 << 20
+STAGE_BUCKETS = 65536
+STAGE_ENTRIES = 4096
 
 
 class YcsbBatchC(C.Structure):
@@ -48,8 +50,8 @@ class ConfigC(C.Structure):
 
 
 class LaunchC(C.Structure):
-    _fields_ = [("block_threads", C.c_uint32), ("vec_per_thread", C.c_uint32), ("blocks_per_sm", C.c_uint32),
-                ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("reserved", C.c_uint32)]
+    _fields_ = [("block_threads", C.c_uint32), ("ops_per_thread", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("dedupe", C.c_uint32)]
 
 
 class StatsC(C.Structure):
@@ -98,10 +100,14 @@ SIGNATURES = {
     "ltpg_commit_bitmap_device": (C.c_int, [P, U32, C.POINTER(P)]),
     "ltpg_set_launch": (C.c_int, [P, C.c_int, C.POINTER(LaunchC)]),
     "ltpg_get_launch": (C.c_int, [P, C.c_int, C.POINTER(LaunchC)]),
+    "ltpg_key_bucket": (U32, [U32]),
+    "ltpg_stage_set": (C.c_int, [P, P, U32]),
+    "ltpg_bucket_counts": (C.c_int, [P, P, C.c_int]),
     "ltpg_counters": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
     "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),
     "ltpg_ycsb_batch_noalloc": (C.c_int, [C.c_int, P, U64, P, P, P, U32, U32, P, P, P, P]),
+    "ltpg_microbench": (C.c_int, [P, C.c_int, U64, U32, C.POINTER(C.c_double)]),
     "ltpg_splitmix64": (U64, [U64]),
     "ltpg_hash3": (U64, [U64, U64, U64]),
 }

@@ -22,6 +22,13 @@ __device__ __forceinline__ ulonglong2 ld_nc16(const void *p) {
     asm("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
     return v;
 }
+// Same load, kept in program order with the other volatile loads so that a
+// thread's independent row reads are all issued before the first is consumed.
+__device__ __forceinline__ ulonglong2 ld_nc16_issue(const void *p) {
+    ulonglong2 v;
+    asm volatile("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
 __device__ __forceinline__ uint4 ld_nc_u4(const void *p) {
     uint4 v;
     asm("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"

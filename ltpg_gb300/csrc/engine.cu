@@ -41,6 +41,7 @@ void free_slot(Slot &s) {
     dev_free(s.vals);
     dev_free(s.txns);
     dev_free(s.lines);
+    dev_free(s.dev_hdr);
     dev_free(s.flags);
     dev_free(s.bitmap);
     dev_free(s.results);
@@ -343,6 +344,7 @@ int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b)
     if (!s->txns) {
         CK(dev_alloc(&s->txns, c->cfg.max_txn), "alloc txns");
         CK(dev_alloc(&s->lines, (uint64_t)c->cfg.max_lines + 1), "alloc lines");
+        CK(dev_alloc(&s->dev_hdr, 2), "alloc slot header");
         s->cap_txn_c = c->cfg.max_txn;
         s->cap_lines = c->cfg.max_lines;
     }
@@ -355,6 +357,10 @@ int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b)
         CK(cudaMemcpyAsync(s->lines, b->lines, (uint64_t)b->n_lines * sizeof(ltpg_tpcc_line),
                            cudaMemcpyHostToDevice, c->stream),
            "upload lines");
+    s->host_hdr[0] = b->n_lines;
+    s->host_hdr[1] = b->txn_base;
+    CK(cudaMemcpyAsync(s->dev_hdr, s->host_hdr, sizeof s->host_hdr, cudaMemcpyHostToDevice, c->stream),
+       "upload slot header");
     if (s->workload != LTPG_WORKLOAD_TPCC || s->n_txn != b->n_txn) drop_graphs(c);
     s->workload = LTPG_WORKLOAD_TPCC;
     s->n_txn = b->n_txn;
@@ -548,14 +554,16 @@ int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
         return fail(c, LTPG_ERR_INVALID, "unknown workload");
     if (cfg->block_threads % 32 || cfg->block_threads < 32 || cfg->block_threads > 512)
         return fail(c, LTPG_ERR_INVALID, "block_threads must be a multiple of 32 in [32, 512]");
-    if (cfg->vec_per_thread < 1 || cfg->vec_per_thread > 8) return fail(c, LTPG_ERR_INVALID, "vec_per_thread in [1, 8]");
+    const uint32_t opt = cfg->ops_per_thread;
+    if (opt != 1 && opt != 2 && opt != 4 && opt != 8) return fail(c, LTPG_ERR_INVALID, "ops_per_thread in {1, 2, 4, 8}");
     if (cfg->stage_ways < 1 || cfg->stage_ways > 8) return fail(c, LTPG_ERR_INVALID, "stage_ways in [1, 8]");
     LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
     l.block = cfg->block_threads;
-    l.per_thread = cfg->vec_per_thread;
+    l.per_thread = cfg->ops_per_thread;
     l.blocks_per_sm = cfg->blocks_per_sm;
     l.ways = cfg->stage_ways;
     l.filter = cfg->filter ? 1u : 0u;
+    l.dedupe = cfg->dedupe ? 1u : 0u;
     drop_graphs(c);
     return LTPG_OK;
 }
@@ -566,11 +574,11 @@ int ltpg_get_launch(ltpg_ctx *c, int workload, ltpg_launch *cfg) {
         return fail(c, LTPG_ERR_INVALID, "unknown workload");
     const LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
     cfg->block_threads = l.block;
-    cfg->vec_per_thread = l.per_thread;
+    cfg->ops_per_thread = l.per_thread;
     cfg->blocks_per_sm = l.blocks_per_sm;
     cfg->stage_ways = l.ways;
     cfg->filter = l.filter;
-    cfg->reserved = 0;
+    cfg->dedupe = l.dedupe;
     return LTPG_OK;
 }
 
@@ -609,6 +617,44 @@ int ltpg_kernel_times(ltpg_ctx *c, uint32_t slot, float *ms3) {
         if (e != cudaSuccess) cudaGetLastError();
     }
     return LTPG_OK;
+}
+
+uint32_t ltpg_key_bucket(uint32_t key) { return (key * 0x9E3779B1u) >> 16; }
+
+int ltpg_stage_set(ltpg_ctx *c, const uint32_t *buckets, uint32_t n) {
+    if (!c || (n && !buckets)) return LTPG_ERR_INVALID;
+    if (!c->stage_map) {
+        CK(dev_alloc(&c->stage_map, LTPG_STAGE_BUCKETS), "alloc stage map");
+        CK(dev_alloc(&c->bucket_counts, LTPG_STAGE_BUCKETS), "alloc bucket counts");
+        CK(cudaMemset(c->bucket_counts, 0, LTPG_STAGE_BUCKETS * 4), "clear bucket counts");
+    }
+    std::vector<uint16_t> map(LTPG_STAGE_BUCKETS, 0xFFFFu);
+    const uint32_t ways = c->launch_y.ways ? c->launch_y.ways : 4u;
+    const uint32_t groups = LTPG_STAGE_ENTRIES / ways;
+    uint32_t g = 0;
+    for (uint32_t i = 0; i < n && g < groups; ++i) {
+        if (buckets[i] >= LTPG_STAGE_BUCKETS) return fail(c, LTPG_ERR_INVALID, "bucket out of range");
+        if (map[buckets[i]] == 0xFFFFu) map[buckets[i]] = (uint16_t)g++;
+    }
+    CK(cudaMemcpyAsync(c->stage_map, map.data(), LTPG_STAGE_BUCKETS * 2, cudaMemcpyHostToDevice, c->stream),
+       "upload stage map");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    const uint32_t on = n ? 1u : 0u;
+    if (on != c->stage_on) drop_graphs(c);
+    c->stage_on = on;
+    return LTPG_OK;
+}
+
+int ltpg_bucket_counts(ltpg_ctx *c, uint32_t *host, int reset) {
+    if (!c || !host) return LTPG_ERR_INVALID;
+    if (!c->bucket_counts) {
+        memset(host, 0, LTPG_STAGE_BUCKETS * 4);
+        return LTPG_OK;
+    }
+    CK(cudaMemcpyAsync(host, c->bucket_counts, LTPG_STAGE_BUCKETS * 4, cudaMemcpyDeviceToHost, c->stream),
+       "download bucket counts");
+    if (reset) CK(cudaMemsetAsync(c->bucket_counts, 0, LTPG_STAGE_BUCKETS * 4, c->stream), "reset counts");
+    return ltpg_sync(c);
 }
 
 }  // extern "C"

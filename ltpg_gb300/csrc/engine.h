@@ -71,6 +71,11 @@ struct Slot {
     uint64_t txn_base = 0;
     ltpg_tpcc_txn *txns = nullptr;
     ltpg_tpcc_line *lines = nullptr;
+    // {n_lines, txn_base} of the batch in the slot, read by the kernels from
+    // device memory so a captured graph stays valid when a new batch is
+    // uploaded into the slot.
+    uint64_t *dev_hdr = nullptr;
+    uint64_t host_hdr[2] = {0, 0};
     uint64_t cap_txn_c = 0, cap_lines = 0;
     // outputs
     uint8_t *flags = nullptr;
@@ -82,10 +87,11 @@ struct Slot {
 
 struct LaunchCfg {
     uint32_t block = 256;        // threads per block of the tuned kernels
-    uint32_t per_thread = 2;     // 16-byte op vectors per thread per tile (YCSB)
+    uint32_t per_thread = 1;     // YCSB op words per thread (1 = cooperative row reads, 2, 4, 8)
     uint32_t blocks_per_sm = 0;  // cap on resident blocks per SM (0 = occupancy)
     uint32_t ways = 4;           // shared-memory staging entries per hot bucket
     uint32_t filter = 1;         // read the slot before its atomicMin
+    uint32_t dedupe = 1;         // one atomic per key per warp
 };
 
 }  // namespace ltpg

@@ -11,8 +11,8 @@ struct StageEnt {
 };
 constexpr uint32_t STAGE_EMPTY = 0xFFFFFFFFu;
 constexpr uint32_t STAGE_NONE = 0xFFFFu;     // stage_map value of an unstaged bucket
-constexpr uint32_t STAGE_BUCKETS = 65536u;   // key-hash buckets seen by the predictor
-constexpr uint32_t STAGE_MAX_ENTRIES = 4096; // 64 KB of shared memory per block
+constexpr uint32_t STAGE_BUCKETS = LTPG_STAGE_BUCKETS;      // key-hash buckets seen by the predictor
+constexpr uint32_t STAGE_MAX_ENTRIES = LTPG_STAGE_ENTRIES;  // 64 KB of shared memory per block
 constexpr uint32_t COUNT_SAMPLE = 16u;       // unstaged ops are counted 1 in 16
 
 __device__ __forceinline__ uint32_t key_bucket(uint32_t key) { return (key * 0x9E3779B1u) >> 16; }

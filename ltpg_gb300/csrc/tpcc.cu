@@ -142,9 +142,11 @@ __device__ __forceinline__ ltpg_tpcc_line load_line(const ltpg_tpcc_line *__rest
 
 // ---- plain phase 1: execute + register (KERNEL_EXECUTE, TF/tp.cu:24-54) ----
 __global__ void __launch_bounds__(PBS) tpcc_exec_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
-                                                       const ltpg_tpcc_line *__restrict__ lines, uint32_t n_lines,
-                                                       TpccDev db, RegSlot *__restrict__ reg,
-                                                       int64_t *__restrict__ results, DevCtl *ctl) {
+                                                       const ltpg_tpcc_line *__restrict__ lines,
+                                                       const uint64_t *__restrict__ hdr, TpccDev db,
+                                                       RegSlot *__restrict__ reg, int64_t *__restrict__ results,
+                                                       DevCtl *ctl) {
+    const uint32_t n_lines = (uint32_t)hdr[0];
     __shared__ TileHdr h;
     __shared__ unsigned long long sum[PT];
     __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
@@ -196,9 +198,11 @@ __global__ void __launch_bounds__(PBS) tpcc_exec_plain(const ltpg_tpcc_txn *__re
 
 // ---- plain phase 2: check (KERNEL_CHECK, TF/tp.cu:55-85) ---------------------
 __global__ void __launch_bounds__(PBS) tpcc_check_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
-                                                        const ltpg_tpcc_line *__restrict__ lines, uint32_t n_lines,
-                                                        TpccDev db, const RegSlot *__restrict__ reg,
+                                                        const ltpg_tpcc_line *__restrict__ lines,
+                                                        const uint64_t *__restrict__ hdr, TpccDev db,
+                                                        const RegSlot *__restrict__ reg,
                                                         uint8_t *__restrict__ flags, DevCtl *ctl) {
+    const uint32_t n_lines = (uint32_t)hdr[0];
     __shared__ TileHdr h;
     __shared__ uint32_t fl[PT];
     const uint32_t epoch = ctl->epoch;
@@ -306,10 +310,12 @@ __device__ __forceinline__ void tpcc_apply_write(const TpccDev &db, const ltpg_t
 // ---- plain phase 3: write-back (KERNEL_WRITEBACK, TF/tp.cu:86-117) ----------
 __global__ void __launch_bounds__(PBS) tpcc_writeback_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
                                                             const ltpg_tpcc_line *__restrict__ lines,
-                                                            uint32_t n_lines, uint64_t txn_base, TpccDev db,
+                                                            const uint64_t *__restrict__ hdr, TpccDev db,
                                                             const uint8_t *__restrict__ flags,
                                                             uint32_t *__restrict__ bitmap, DevStats *st,
                                                             DevCtl *ctl) {
+    const uint32_t n_lines = (uint32_t)hdr[0];
+    const uint64_t txn_base = hdr[1];
     __shared__ TileHdr h;
     __shared__ uint8_t fl[PT];
     const uint32_t t0 = blockIdx.x * PT, nt = min(PT, B - t0);
@@ -350,14 +356,14 @@ cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase) {
     if (phase == 0) {
         cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
         if (e != cudaSuccess) return e;
-        tpcc_exec_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, db, c->tpcc.reg, s.results,
+        tpcc_exec_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, c->tpcc.reg, s.results,
                                                      c->ctl);
     } else if (phase == 1) {
-        tpcc_check_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, db, c->tpcc.reg, s.flags,
+        tpcc_check_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, c->tpcc.reg, s.flags,
                                                       c->ctl);
     } else {
-        tpcc_writeback_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.n_lines, s.txn_base, db, s.flags,
-                                                          s.bitmap, s.stats, c->ctl);
+        tpcc_writeback_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, s.flags, s.bitmap,
+                                                          s.stats, c->ctl);
     }
     return cudaGetLastError();
 }
@@ -380,8 +386,8 @@ constexpr uint32_t HOT_SMEM_MAX_W = 256;  // shared-memory YTD sums up to 256 wa
 struct TpccTunedArgs {
     const ltpg_tpcc_txn *txns;
     const ltpg_tpcc_line *lines;
-    uint32_t B, n_lines;
-    uint64_t txn_base;
+    const uint64_t *hdr;  // {n_lines, txn_base} of the slot
+    uint32_t B;
     TpccDev db;
     RegSlot *reg;
     int64_t *results;
@@ -399,6 +405,7 @@ __device__ __forceinline__ uint64_t ld_ca_u64t(const unsigned long long *p) {
 }
 
 __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr &h, uint64_t tag) {
+    const uint32_t n_lines = (uint32_t)a.hdr[0];
     __shared__ unsigned long long sum[PT];
     __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
     __shared__ long long res[PT];
@@ -407,7 +414,7 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr 
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
         if (threadIdx.x < PT) sum[threadIdx.x] = 0ull;
-        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, a.n_lines, a.ctl,
+        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl,
                                          [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
         for (uint32_t base = 0; base < total; base += blockDim.x) {
             const uint32_t e = base + threadIdx.x;
@@ -468,6 +475,8 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr 
 // hot: 11 W int64 sums in shared memory (W <= HOT_SMEM_MAX_W), or null.
 __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdr &h, uint32_t epoch,
                                                    long long *hot) {
+    const uint32_t n_lines = (uint32_t)a.hdr[0];
+    const uint64_t txn_base = a.hdr[1];
     __shared__ uint32_t fl[PT];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t n_tiles = (a.B + PT - 1) / PT;
@@ -475,7 +484,7 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
         if (threadIdx.x < PT) fl[threadIdx.x] = 0u;
-        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, a.n_lines, a.ctl,
+        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl,
                                          [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
         for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
             const uint32_t i = tile_owner(h, nt, e), j = e - h.off[i];
@@ -532,9 +541,9 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
         const uint32_t wtotal = h.off[nt];
         for (uint32_t e = threadIdx.x; e < wtotal; e += blockDim.x) {
             const uint32_t i = tile_owner(h, nt, e);
-            if (hot) tpcc_apply_write<false>(a.db, h.x[i], e - h.off[i], a.lines, a.txn_base + t0 + i, hot,
+            if (hot) tpcc_apply_write<false>(a.db, h.x[i], e - h.off[i], a.lines, txn_base + t0 + i, hot,
                                              hot + a.db.W);
-            else tpcc_apply_write<true>(a.db, h.x[i], e - h.off[i], a.lines, a.txn_base + t0 + i, nullptr,
+            else tpcc_apply_write<true>(a.db, h.x[i], e - h.off[i], a.lines, txn_base + t0 + i, nullptr,
                                         nullptr);
         }
         __syncthreads();
@@ -596,9 +605,8 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     TpccTunedArgs a;
     a.txns = s.txns;
     a.lines = s.lines;
+    a.hdr = s.dev_hdr;
     a.B = s.n_txn;
-    a.n_lines = s.n_lines;
-    a.txn_base = s.txn_base;
     a.db = make_dev(c);
     a.reg = c->tpcc.reg;
     a.results = s.results;

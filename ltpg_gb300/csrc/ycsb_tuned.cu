@@ -82,7 +82,7 @@ __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long
                 if (kStage && valid) {
                     const uint32_t b = key_bucket(key);
                     const uint32_t g = __ldg(a.stage_map + b);
-                    if (g != STAGE_NONE) {
+                    if (g != STAGE_NONE && (g + 1) * a.ways <= a.stage_entries) {
                         StageEnt *e = stage_find(tab, g, a.ways, key);
                         if (e) {
                             atomicMin(upd ? &e->wmin : &e->rmin, t);
@@ -247,6 +247,230 @@ __device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *
     }
 }
 
+// ---- fast execute+register: transactions of 2^m words, no block barriers -----
+// Each thread takes OPS consecutive op words of one transaction (one 4-, 8- or
+// 16-byte load); the lpt = stride / OPS lanes of a transaction are adjacent and
+// aligned inside a warp, so the per-transaction read checksum is a segmented
+// shuffle reduction and the kernel needs no shared memory outside staging.
+// All row loads and slot reads of a thread's ops are issued before any of them
+// is consumed, to keep many requests in flight per SM.
+template <int OPS>
+struct OpVec;
+template <>
+struct OpVec<1> {
+    static __device__ __forceinline__ void load(const uint32_t *p, uint32_t *w) { w[0] = __ldg(p); }
+};
+template <>
+struct OpVec<2> {
+    static __device__ __forceinline__ void load(const uint32_t *p, uint32_t *w) {
+        uint2 v;
+        asm("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+        w[0] = v.x;
+        w[1] = v.y;
+    }
+};
+template <>
+struct OpVec<4> {
+    static __device__ __forceinline__ void load(const uint32_t *p, uint32_t *w) {
+        const uint4 v = ld_nc_u4(p);
+        w[0] = v.x;
+        w[1] = v.y;
+        w[2] = v.z;
+        w[3] = v.w;
+    }
+};
+
+template <int OPS, bool kStage, bool kFilter, bool kDedupe>
+__global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t lpt) {
+    extern __shared__ __align__(16) char smem[];
+    StageEnt *tab = reinterpret_cast<StageEnt *>(smem);
+    const uint64_t tag = slot_tag(a.ctl->epoch);
+    const uint32_t lane = threadIdx.x & 31;
+    if (kStage) {
+        stage_init(tab, a.stage_entries);
+        __syncthreads();
+    }
+    const uint32_t nv = a.B * lpt;  // op vectors in the batch
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < nv; base += step) {
+        const uint32_t v = base + threadIdx.x;
+        const bool act = v < nv;
+        uint32_t w[OPS];
+        if (act) OpVec<OPS>::load(a.ops + (uint64_t)v * OPS, w);
+        else
+#pragma unroll
+            for (int q = 0; q < OPS; ++q) w[q] = LTPG_YCSB_OP_PAD;
+        const uint32_t t = v / lpt;
+        const uint32_t j0 = (v % lpt) * OPS;
+        bool rd[OPS], need[OPS];
+        uint32_t key[OPS];
+#pragma unroll
+        for (int q = 0; q < OPS; ++q) {
+            bool valid = act && !ycsb_is_pad(w[q]);
+            key[q] = ycsb_key(w[q]);
+            if (valid && key[q] >= a.n) {
+                report_error(a.ctl, DERR_BOUNDS, t);
+                valid = false;
+            }
+            rd[q] = valid && !ycsb_is_update(w[q]);
+            need[q] = valid;
+            if (kStage && valid) {
+                const uint32_t b = key_bucket(key[q]);
+                const uint32_t g = __ldg(a.stage_map + b);
+                if (g != STAGE_NONE && (g + 1) * a.ways <= a.stage_entries) {
+                    StageEnt *e = stage_find(tab, g, a.ways, key[q]);
+                    if (e) {
+                        atomicMin(ycsb_is_update(w[q]) ? &e->wmin : &e->rmin, t);
+                        atomicAdd(&e->cnt, 1u);
+                        need[q] = false;
+                    }
+                }
+                if (need[q] && (t % COUNT_SAMPLE) == 0u) atomicAdd(a.bucket_counts + b, COUNT_SAMPLE);
+            }
+        }
+        // issue every load of this thread's ops
+        ulonglong2 r[OPS][5];
+        uint64_t cur[OPS];
+#pragma unroll
+        for (int q = 0; q < OPS; ++q) {
+            const char *p = reinterpret_cast<const char *>(a.rows + (uint64_t)key[q] * LTPG_YCSB_FIELDS);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) r[q][i] = rd[q] ? ld_nc16_issue(p + 16 * i) : make_ulonglong2(0ull, 0ull);
+            unsigned long long *slot = ycsb_is_update(w[q]) ? &a.reg[key[q]].w : &a.reg[key[q]].r;
+            cur[q] = (kFilter && need[q]) ? ld_ca_u64(slot) : ~0ull;
+        }
+        // registration: optionally one atomic per distinct (key, kind) of the
+        // warp, optionally skipped when the slot already holds a smaller value
+#pragma unroll
+        for (int q = 0; q < OPS; ++q) {
+            bool leader = need[q];
+            if (kDedupe) {
+                const uint32_t mkey = need[q] ? (key[q] | (ycsb_is_update(w[q]) ? 0x80000000u : 0u)) : 0xFFFFFFFFu;
+                const unsigned peers = __match_any_sync(FULL, mkey);
+                // lanes are in transaction order, so the lowest peer holds the smallest TID
+                leader = need[q] && (__ffs(peers) - 1) == (int)lane;
+            }
+            const unsigned long long mine = tag | t;
+            if (leader && cur[q] > mine)
+                red_min(ycsb_is_update(w[q]) ? &a.reg[key[q]].w : &a.reg[key[q]].r, mine);
+        }
+        unsigned long long part = 0;
+#pragma unroll
+        for (int q = 0; q < OPS; ++q) {
+            const unsigned long long x = r[q][0].x ^ r[q][0].y ^ r[q][1].x ^ r[q][1].y ^ r[q][2].x ^ r[q][2].y ^
+                                         r[q][3].x ^ r[q][3].y ^ r[q][4].x ^ r[q][4].y;
+            part += rd[q] ? x * (2ull * (j0 + q) + 1ull) : 0ull;
+        }
+        for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+        if (act && (v % lpt) == 0u) a.results[t] = (int64_t)part;
+    }
+    if (kStage) {
+        __syncthreads();
+        const uint32_t ops = stage_flush(tab, a.stage_entries, a.reg, tag, a.bucket_counts);
+        if (ops) red_add_u64(&a.st->staged_ops, ops);
+    }
+}
+
+// ---- cooperative execute+register: one op per lane, rows read by 5 lanes ----
+// A warp takes 32 consecutive op words (whole transactions, the stride being a
+// power of two <= 32).  Each lane registers its own op; then the rows of the
+// warp's reads are fetched six at a time, five lanes per row, each lane one
+// contiguous 16-byte chunk, so a row costs one or two cache-line requests
+// instead of five.  The five chunks are xor-folded within their lane group and
+// handed back to the lane that owns the op.
+template <bool kStage, bool kFilter, bool kDedupe>
+__device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt *tab, uint64_t tag) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lpt = a.stride;  // lanes per transaction
+    const uint64_t nw = (uint64_t)a.B * a.stride;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t grp = lane / 5, chunk = lane % 5;  // row-read lane groups (6 x 5 lanes)
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
+        const uint64_t v = base + threadIdx.x;
+        const bool act = v < nw;
+        const uint32_t w = act ? __ldg(a.ops + v) : LTPG_YCSB_OP_PAD;
+        const uint32_t t = (uint32_t)(v / lpt);
+        const uint32_t j = (uint32_t)(v % lpt);
+        bool valid = act && !ycsb_is_pad(w);
+        const uint32_t key = ycsb_key(w);
+        if (valid && key >= a.n) {
+            report_error(a.ctl, DERR_BOUNDS, t);
+            valid = false;
+        }
+        const bool upd = ycsb_is_update(w);
+        const bool rd = valid && !upd;
+        bool need = valid;
+        if (kStage && valid) {
+            const uint32_t b = key_bucket(key);
+            const uint32_t g = __ldg(a.stage_map + b);
+            if (g != STAGE_NONE && (g + 1) * a.ways <= a.stage_entries) {
+                StageEnt *e = stage_find(tab, g, a.ways, key);
+                if (e) {
+                    atomicMin(upd ? &e->wmin : &e->rmin, t);
+                    atomicAdd(&e->cnt, 1u);
+                    need = false;
+                }
+            }
+            if (need && (t % COUNT_SAMPLE) == 0u) atomicAdd(a.bucket_counts + b, COUNT_SAMPLE);
+        }
+        // row chunks of the warp's reads: round r covers ops 6r .. 6r+5
+        const unsigned rdmask = __ballot_sync(FULL, rd);
+        ulonglong2 ch[6];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const uint32_t src = (uint32_t)r * 6u + grp;
+            const uint32_t k_src = __shfl_sync(FULL, key, src & 31u);
+            const bool go = grp < 6 && src < 32 && ((rdmask >> src) & 1u);
+            ch[r] = go ? ld_nc16_issue(reinterpret_cast<const char *>(a.rows + (uint64_t)k_src * LTPG_YCSB_FIELDS) +
+                                       16u * chunk)
+                       : make_ulonglong2(0ull, 0ull);
+        }
+        uint64_t cur = ~0ull;
+        unsigned long long *slot = upd ? &a.reg[key].w : &a.reg[key].r;
+        if (kFilter && need) cur = ld_ca_u64(slot);
+        bool leader = need;
+        if (kDedupe) {
+            const unsigned peers = __match_any_sync(FULL, need ? (key | (upd ? 0x80000000u : 0u)) : 0xFFFFFFFFu);
+            leader = need && (__ffs(peers) - 1) == (int)lane;
+        }
+        const unsigned long long mine = tag | t;
+        if (leader && cur > mine) red_min(slot, mine);
+        // fold the five chunks of each row onto its group's first lane (5g),
+        // then hand the row's xor to the lane that owns the op
+        unsigned long long x = 0;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const unsigned long long c0 = ch[r].x ^ ch[r].y;
+            unsigned long long c = c0 ^ __shfl_down_sync(FULL, c0, 1);  // lane 5g: chunks 0,1
+            c ^= __shfl_down_sync(FULL, c, 2);                          // lane 5g: chunks 0..3
+            const unsigned long long rowx = c ^ __shfl_down_sync(FULL, c0, 4);  // + chunk 4
+            const uint32_t op0 = (uint32_t)r * 6u;
+            const unsigned long long got = __shfl_sync(FULL, rowx, ((lane - op0) * 5u) & 31u);
+            if (lane >= op0 && lane < op0 + 6u) x = got;
+        }
+        unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
+        for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+        if (act && j == 0u) a.results[t] = (int64_t)part;
+    }
+}
+
+template <bool kStage, bool kFilter, bool kDedupe>
+__global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
+    extern __shared__ __align__(16) char smem[];
+    StageEnt *tab = reinterpret_cast<StageEnt *>(smem);
+    const uint64_t tag = slot_tag(a.ctl->epoch);
+    if (kStage) {
+        stage_init(tab, a.stage_entries);
+        __syncthreads();
+    }
+    coop_exec_loop<kStage, kFilter, kDedupe>(a, tab, tag);
+    if (kStage) {
+        __syncthreads();
+        const uint32_t ops = stage_flush(tab, a.stage_entries, a.reg, tag, a.bucket_counts);
+        if (ops) red_add_u64(&a.st->staged_ops, ops);
+    }
+}
+
 // Shared memory layout: [dig: tile u64][fl: tile u32][wbuf: warps*128*16 B][stage table]
 __host__ __device__ __forceinline__ size_t ycsb_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage_entries) {
     const size_t a = ((size_t)tile * 8 + 15) / 16 * 16;
@@ -307,7 +531,12 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         stage_init(p.tab, a.stage_entries);
         __syncthreads();
     }
-    exec_tiles<kStage>(a, p.dig, p.tab, tag);
+    if (a.stride <= 32 && (a.stride & (a.stride - 1)) == 0) {
+        if (a.filter) coop_exec_loop<kStage, true, true>(a, p.tab, tag);
+        else coop_exec_loop<kStage, false, true>(a, p.tab, tag);
+    } else {
+        exec_tiles<kStage>(a, p.dig, p.tab, tag);
+    }
     if (kStage) {
         __syncthreads();
         const uint32_t ops = stage_flush(p.tab, a.stage_entries, a.reg, tag, a.bucket_counts);
@@ -325,11 +554,85 @@ static uint32_t tuned_tile(uint32_t stride, uint32_t threads, uint32_t per_threa
     return t < 32u ? 32u : t;
 }
 
+// Launches the barrier-free execute kernel when stride / ops-per-thread is a
+// power of two <= 32; returns false (nothing launched) otherwise.
+template <int OPS>
+static void launch_fast_t(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, uint32_t lpt) {
+    const LaunchCfg &L = c->launch_y;
+    const size_t smem = stage ? (size_t)a.stage_entries * sizeof(StageEnt) : 0;
+    void (*k)(YcsbTunedArgs, uint32_t);
+    const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
+    switch (sel) {
+    case 0: k = ycsb_exec_fast<OPS, false, false, false>; break;
+    case 1: k = ycsb_exec_fast<OPS, false, false, true>; break;
+    case 2: k = ycsb_exec_fast<OPS, false, true, false>; break;
+    case 3: k = ycsb_exec_fast<OPS, false, true, true>; break;
+    case 4: k = ycsb_exec_fast<OPS, true, false, false>; break;
+    case 5: k = ycsb_exec_fast<OPS, true, false, true>; break;
+    case 6: k = ycsb_exec_fast<OPS, true, true, false>; break;
+    default: k = ycsb_exec_fast<OPS, true, true, true>; break;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (L.blocks_per_sm && (int)L.blocks_per_sm < per_sm) per_sm = (int)L.blocks_per_sm;
+    const uint64_t nv = (uint64_t)a.B * lpt;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nv + 255) / 256, (uint64_t)per_sm * c->sm_count);
+    k<<<grid, 256, smem, c->stream>>>(a, lpt);
+}
+
+static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
+    const LaunchCfg &L = c->launch_y;
+    const size_t smem = stage ? (size_t)a.stage_entries * sizeof(StageEnt) : 0;
+    void (*k)(YcsbTunedArgs);
+    const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
+    switch (sel) {
+    case 0: k = ycsb_exec_coop<false, false, false>; break;
+    case 1: k = ycsb_exec_coop<false, false, true>; break;
+    case 2: k = ycsb_exec_coop<false, true, false>; break;
+    case 3: k = ycsb_exec_coop<false, true, true>; break;
+    case 4: k = ycsb_exec_coop<true, false, false>; break;
+    case 5: k = ycsb_exec_coop<true, false, true>; break;
+    case 6: k = ycsb_exec_coop<true, true, false>; break;
+    default: k = ycsb_exec_coop<true, true, true>; break;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (L.blocks_per_sm && (int)L.blocks_per_sm < per_sm) per_sm = (int)L.blocks_per_sm;
+    const uint64_t nw = (uint64_t)a.B * a.stride;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nw + 255) / 256, (uint64_t)per_sm * c->sm_count);
+    k<<<grid, 256, smem, c->stream>>>(a);
+}
+
+// Launch shapes of the execute phase, by ops_per_thread: 1 = cooperative row
+// reads (ycsb_exec_coop), 2 / 4 = per-thread row reads (ycsb_exec_fast);
+// 8 = block tiles (ycsb_exec_tuned), which also serve strides that are not a
+// power of two.
+static bool launch_fast_exec(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
+    const uint32_t opt = c->launch_y.per_thread ? c->launch_y.per_thread : 4u;
+    if (opt >= 8) return false;
+    if (opt == 1 && a.stride <= 32 && (a.stride & (a.stride - 1)) == 0) {
+        launch_coop(c, a, stage);
+        return true;
+    }
+    const uint32_t ops = std::max<uint32_t>(2u, std::min<uint32_t>(opt, 4u));
+    if (a.stride % ops) return false;
+    const uint32_t lpt = a.stride / ops;
+    if (lpt == 0 || lpt > 32 || (lpt & (lpt - 1))) return false;
+    if (ops == 1) launch_fast_t<1>(c, a, stage, lpt);
+    else if (ops == 2) launch_fast_t<2>(c, a, stage, lpt);
+    else launch_fast_t<4>(c, a, stage, lpt);
+    return true;
+}
+
 cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     if (s.n_txn == 0) return cudaSuccess;
     const LaunchCfg &L = c->launch_y;
     const uint32_t threads = L.block;
-    const uint32_t per_thread = L.per_thread ? L.per_thread : 2u;
+    const uint32_t per_thread = std::max<uint32_t>(1u, (L.per_thread ? L.per_thread : 4u) / 4u);
     YcsbTunedArgs a;
     a.ops = s.ops;
     a.val_off = s.val_off;
@@ -353,6 +656,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.stage_entries = stage ? STAGE_MAX_ENTRIES / a.ways * a.ways : 0u;
     a.filter = L.filter;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
+    const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
     if (e != cudaSuccess) return e;
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
@@ -383,11 +687,18 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     }
     prof_mark(c, 0);
     count_launch(c);
-    exec_k<<<grid, threads, smem, c->stream>>>(a);
+    if (!launch_fast_exec(c, a, stage)) {
+        exec_k<<<grid, threads, smem, c->stream>>>(a);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 1);
     count_launch(c);
-    ycsb_checkwb_tuned<<<grid, threads, smem, c->stream>>>(a);
+    int per_sm_cwb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cwb, ycsb_checkwb_tuned, (int)threads, smem_cwb);
+    if (e != cudaSuccess) return e;
+    if (per_sm_cwb < 1) per_sm_cwb = 1;
+    const uint32_t grid_cwb = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm_cwb * c->sm_count));
+    ycsb_checkwb_tuned<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 2);
     prof_mark(c, 3);

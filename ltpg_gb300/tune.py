@@ -1,0 +1,130 @@
+"""Autotuner for the tuned kernels' launch shape.
+
+Searches ops per thread, blocks per SM, the slot-read filter and the staging
+ways on the batches already uploaded to an engine, times each candidate with
+CUDA events on the engine's stream, and keeps the fastest.  Every candidate's
+commit bitmaps are compared with the plain path's on the same batch before it
+may win: a launch shape can change speed, never a commit decision.  Results are
+cached per (GPU, workload) in ltpg_gb300/tuned_launch.json.
+"""
+import itertools
+import json
+import os
+
+import numpy as np
+
+from . import abi
+
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned_launch.json")
+
+
+def _gpu_name():
+    try:
+        import torch
+        return torch.cuda.get_device_name(0)
+    except Exception:
+        return "unknown"
+
+
+def _key(workload_key):
+    return f"{_gpu_name()}|{workload_key}"
+
+
+def load_cached(workload_key):
+    if not os.path.exists(CACHE):
+        return None
+    try:
+        return json.load(open(CACHE)).get(_key(workload_key))
+    except (OSError, ValueError):
+        return None
+
+
+def save_cached(workload_key, cfg):
+    data = {}
+    if os.path.exists(CACHE):
+        try:
+            data = json.load(open(CACHE))
+        except (OSError, ValueError):
+            data = {}
+    data[_key(workload_key)] = cfg
+    with open(CACHE + ".tmp", "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(CACHE + ".tmp", CACHE)
+
+
+def candidates(workload, staging=False):
+    if workload == "ycsb":
+        grid = itertools.product([1, 2, 4], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
+        return [dict(block_threads=256, ops_per_thread=o, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w)
+                for o, b, f, d, w in grid]
+    return [dict(block_threads=256, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=1, stage_ways=4)
+            for b, f in itertools.product([0, 2, 4, 6], [0, 1])]
+
+
+def _time_batches(eng, slots, reps, mode, torch):
+    stream = torch.cuda.ExternalStream(eng.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eng.sync()
+    ev0.record(stream)
+    for _ in range(reps):
+        for s in slots:
+            eng.run_batch(s, mode)
+    ev1.record(stream)
+    eng.sync()
+    return ev0.elapsed_time(ev1) / (reps * len(slots))
+
+
+def autotune(eng, workload, slots, reload, mode="fused", reps=3, staging=False, verify_slot=None, log=None):
+    """Times every candidate launch shape on the uploaded batches in `slots`.
+
+    reload(): restores the table image (used before each verification run so
+    plain and tuned start from the same state).  Returns (best_cfg, table)."""
+    import torch
+    wl = "ycsb" if workload == "ycsb" else "tpcc"
+    vslot = slots[0] if verify_slot is None else verify_slot
+    n = None
+    # reference bitmap of the plain path
+    reload()
+    eng.run_batch(vslot, "plain")
+    eng.sync()
+    st = eng.stats(vslot)
+    n = int(st["n_txn"])
+    want = eng.commit_bitmap(vslot, n)
+    table = []
+    best = None
+    for cfg in candidates(wl, staging):
+        try:
+            eng.set_launch(wl, **cfg)
+        except Exception as e:  # an invalid shape for this GPU
+            table.append((cfg, None, str(e)))
+            continue
+        reload()
+        eng.run_batch(vslot, mode)
+        eng.sync()
+        ok = np.array_equal(eng.commit_bitmap(vslot, n), want)
+        if not ok:
+            table.append((cfg, None, "bitmap differs from the plain path"))
+            continue
+        _time_batches(eng, slots, 1, mode, torch)  # warm
+        ms = _time_batches(eng, slots, reps, mode, torch)
+        table.append((cfg, ms, "ok"))
+        if log:
+            log(f"{cfg} {ms:.4f} ms/batch")
+        if best is None or ms < best[1]:
+            best = (cfg, ms)
+    if best is None:
+        raise RuntimeError("no launch shape reproduced the plain path's commit bitmap")
+    eng.set_launch(wl, **best[0])
+    return dict(best[0], ms_per_batch=best[1]), table
+
+
+def apply_cached_or_tune(eng, workload, workload_key, slots, reload, **kw):
+    """Uses the cached launch shape for this GPU and workload, else tunes and caches."""
+    wl = "ycsb" if workload == "ycsb" else "tpcc"
+    cfg = load_cached(workload_key)
+    if cfg:
+        eng.set_launch(wl, **{k: v for k, v in cfg.items() if k in dict(abi.LaunchC._fields_)})
+        return cfg, "cache"
+    best, _ = autotune(eng, workload, slots, reload, **kw)
+    save_cached(workload_key, best)
+    return best, "tuned"

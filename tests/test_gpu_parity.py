@@ -184,3 +184,87 @@ def test_tpcc_invalid_record_reports_error(eng):
     with pytest.raises(LtpgError) as ei:
         eng.sync()
     assert ei.value.code == abi.ERR_BOUNDS
+
+
+# ---- tuning never changes outcomes ------------------------------------------------------
+@pytest.mark.parametrize("opt,filt,dd,bps", [(1, 0, 0, 0), (1, 1, 1, 2), (2, 0, 1, 1), (4, 1, 0, 0), (8, 1, 1, 0),
+                                             (4, 0, 0, 3)])
+@pytest.mark.parametrize("k", [4, 7, 10, 16, 32])
+def test_launch_shapes_do_not_change_outcomes(eng, opt, filt, dd, bps, k):
+    n = 40000
+    eng.load_ycsb(31, n)
+    o = oracle.YcsbOracle(31, n)
+    g = YcsbGenerator(31, n, 9000, k, 10, 0.99)
+    saved = eng.get_launch("ycsb")
+    try:
+        eng.set_launch("ycsb", ops_per_thread=opt, filter=filt, dedupe=dd, blocks_per_sm=bps)
+        for bid, mode in enumerate(["fused", "persistent", "graph"]):
+            b = g.batch(bid)
+            assert_same(run_and_fetch(eng, bid % 2, b, mode), o.run(b))
+        assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+    finally:
+        eng.set_launch("ycsb", **saved)
+
+
+@pytest.mark.parametrize("ways", [1, 2, 4])
+def test_staging_does_not_change_outcomes(eng, ways):
+    """Stage the hottest buckets (and, in a second round, every bucket, so that
+    most keys collide and fall back to the global path): results stay bit-exact
+    and the staged registrations are counted."""
+    from ltpg_gb300 import key_bucket
+    n = 100000
+    eng.load_ycsb(41, n)
+    o = oracle.YcsbOracle(41, n)
+    g = YcsbGenerator(41, n, 30000, 16, 5, 0.99, rotate_every=2)
+    saved = eng.get_launch("ycsb")
+    try:
+        eng.set_launch("ycsb", stage_ways=ways)
+        for bid in range(6):
+            b = g.batch(bid)
+            keys = (b.ops.reshape(b.n_txn, -1)[:, :16] & ((1 << 27) - 1)).ravel()
+            cnt = np.bincount(key_bucket(keys), minlength=abi.STAGE_BUCKETS)
+            staged = np.argsort(-cnt, kind="stable")[:abi.STAGE_ENTRIES // ways] if bid < 3 else \
+                np.arange(abi.STAGE_BUCKETS)
+            eng.stage_set(staged)
+            mode = ["fused", "persistent", "graph"][bid % 3]
+            assert_same(run_and_fetch(eng, bid % 2, b, mode), o.run(b))
+            st = eng.stats(bid % 2)
+            assert st["staged_ops"] > 0
+        assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+        counts = eng.bucket_counts(reset=True)
+        assert counts.sum() > 0
+    finally:
+        eng.stage_set([])
+        eng.set_launch("ycsb", **saved)
+
+
+def test_graph_replay_after_reupload(eng):
+    """A graph captured for a slot stays correct when a different batch (other
+    line count, other transaction numbers) is uploaded into that slot."""
+    eng.load_tpcc(61, 2)
+    o = oracle.TpccOracle(61, 2)
+    g = TpccGenerator(61, 2, 6000)
+    batches = [g.next() for _ in range(4)]
+    for b in batches[:2]:                # both slots in use before any capture
+        eng.upload(batches.index(b), b)
+    for i, b in enumerate(batches):
+        eng.upload(i % 2, b)
+        eng.run_batch(i % 2, "graph")
+        eng.sync()
+        assert_same((eng.txn_flags(i % 2, b.n_txn), eng.commit_bitmap(i % 2, b.n_txn),
+                     eng.txn_results(i % 2, b.n_txn)), o.run(b))
+    for t in range(abi.TPCC_TABLES):
+        assert np.array_equal(eng.download_table(t), o.tables[t]), t
+    n = 20000
+    eng.load_ycsb(62, n)
+    yo = oracle.YcsbOracle(62, n)
+    yg = YcsbGenerator(62, n, 5000, 16, 20, 0.9)
+    yb = [yg.batch(i) for i in range(4)]
+    eng.upload(0, yb[0])
+    eng.upload(1, yb[1])
+    for i, b in enumerate(yb):
+        eng.upload(i % 2, b)
+        eng.run_batch(i % 2, "graph")
+        eng.sync()
+        assert np.array_equal(eng.txn_flags(i % 2, b.n_txn), yo.run(b)[0])
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), yo.rows)
