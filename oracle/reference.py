@@ -1,0 +1,168 @@
+"""The reference's own kernels, run on our batches (GPU parity pin).
+
+TEST INFRASTRUCTURE ONLY.  Loads the cubins and struct layouts made by
+oracle/ref_build.py (oracle/_ref/) and runs them through ref_harness.cu:
+  RefY1  LTPG/YCSB/1 as shipped: 10,000 transactions x (9 reads + 1 write)
+         over 1,000,000 records (Y1/Predefine.h:8-12).  Its Zipfian mode routes
+         key 0 around registration (Y1/Genericfunction.h:163-187), so batches
+         for it use keys 1 .. N-1.
+  RefTF  LTPG/TPCC-allopt-final as shipped: 65,536 Payments (NEWORDER_PERCENT
+         = 0), 64 warehouses (TF/Predefine.h:8-10), customers by id.
+Both return per-transaction flags rebuilt from the reference's conflict
+counters raw / war / waw (the commit flag from its own rule,
+TF/Execute_payment.h:607, Y1/Execute.h:187).
+"""
+import ctypes as C
+import json
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.join(HERE, "_ref")
+BUILD = os.path.join(HERE, "_build")
+HARNESS = os.path.join(BUILD, "libref_harness.so")
+_lib = None
+
+
+def available():
+    return all(os.path.exists(os.path.join(REF, f)) for f in ["y1.cubin", "y1_layout.json", "tf.cubin",
+                                                             "tf_layout.json"])
+
+
+def build_harness(force=False):
+    src = os.path.join(HERE, "ref_harness.cu")
+    if not force and os.path.exists(HARNESS) and os.path.getmtime(HARNESS) >= os.path.getmtime(src):
+        return HARNESS
+    os.makedirs(BUILD, exist_ok=True)
+    home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    stubs = os.path.join(home, "lib64", "stubs")
+    cmd = [os.path.join(home, "bin", "nvcc"), "-shared", "-Xcompiler", "-fPIC", "-O2", src, "-o", HARNESS + ".tmp",
+           "-L" + stubs, "-lcuda"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    os.replace(HARNESS + ".tmp", HARNESS)
+    return HARNESS
+
+
+def _harness():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build_harness())
+        _lib.ref_launch.restype = C.c_int
+        _lib.ref_launch.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_uint),
+                                    C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_int), C.c_char_p, C.c_int]
+    return _lib
+
+
+def _launch(prog, layout, bufs, copy_back):
+    n = len(bufs)
+    names = (C.c_char_p * 3)(*[k.encode() for k in layout["kernels"]])
+    grids = (C.c_uint * 3)(*layout["grids"])
+    blocks = (C.c_uint * 3)(*layout["blocks"])
+    sizes = (C.c_uint64 * n)(*[b.nbytes for b in bufs])
+    ptrs = (C.c_void_p * n)(*[b.ctypes.data for b in bufs])
+    cb = (C.c_int * n)(*copy_back)
+    err = C.create_string_buffer(256)
+    rc = _harness().ref_launch(os.path.join(REF, f"{prog}.cubin").encode(), 3, names, grids, blocks, n, sizes, ptrs,
+                               cb, err, 256)
+    if rc:
+        raise RuntimeError(f"reference kernels failed: {err.value.decode()}")
+
+
+def _flags(raw, war, waw):
+    f = (raw > 0).astype(np.uint8) | ((war > 0).astype(np.uint8) << 1) | ((waw > 0).astype(np.uint8) << 2)
+    com = (waw == 0) & ((raw == 0) | (war == 0))
+    return f | (com.astype(np.uint8) << 3)
+
+
+def covered_txns(layout, warps_per_group, batch):
+    """Transactions whose every op the reference's launch grids reach.  Each
+    kernel gives every 32 transactions a group of warps (one per op role); its
+    grid, fixed at compile time as roles * B / 512 + 1 blocks, can end inside
+    the last group, whose missing warps then never run."""
+    full = min((g * b // 32) // w for g, b, w in zip(layout["grids"], layout["blocks"], warps_per_group))
+    return min(batch, full * 32)
+
+
+class RefY1:
+    def __init__(self):
+        self.L = json.load(open(os.path.join(REF, "y1_layout.json")))
+        self.B = self.L["batch"]
+        self.n = self.L["table"]
+        self.reads = self.L["reads"]
+        writes = self.L["ops"] - self.reads
+        # warp roles per 32 transactions: execute 2 per op, check reads + 2 per
+        # write, write-back 1 + writes (Y1/Predefine.h:31-35, Y1/Execute.h:79-252)
+        self.covered = covered_txns(self.L, [2 * self.L["ops"], self.reads + 2 * writes, 1 + writes], self.B)
+
+    def run(self, read_keys, write_keys):
+        """read_keys: (B, reads) uint32, write_keys: (B,) uint32, TID = row index.
+        Returns the reference's flags and its COMMIT_AND_ABORT marks."""
+        L, B = self.L, self.B
+        s, q, lg = L["set"], L["query"], L["log"]
+        set_b = np.zeros(s["size"], dtype=np.uint8)
+        query = np.zeros(q["size"], dtype=np.uint8)
+        qv = query.view(np.uint32)
+        # SoA, op-major: LOC_R[op * B + NO] (Y1/Execute.h:20), LOC_W[op * B + NO], TID[NO]
+        qv[q["loc_r"] // 4:q["loc_r"] // 4 + self.reads * B] = np.asarray(read_keys, dtype=np.uint32).T.ravel()
+        qv[q["loc_w"] // 4:q["loc_w"] // 4 + B] = np.asarray(write_keys, dtype=np.uint32)
+        qv[q["tid"] // 4:q["tid"] // 4 + B] = np.arange(B, dtype=np.uint32)
+        log = np.zeros(lg["size"], dtype=np.uint8)
+        log[:lg["ytd"]] = 0xFF  # registration tables cleared as clear_LOG does (Y1/Database.h:321-326)
+        snap = np.zeros(L["snapshot"], dtype=np.uint8)
+        index = np.zeros(max(1, L["index"]), dtype=np.uint8)
+        _launch("y1", L, [set_b, query, log, snap, index], [1, 0, 0, 0, 0])
+        sv = set_b.view(np.uint32)
+        raw = sv[s["raw"] // 4:s["raw"] // 4 + B]
+        war = sv[s["war"] // 4:s["war"] // 4 + B]
+        waw = sv[s["waw"] // 4:s["waw"] // 4 + B]
+        mark = sv[s["commit"] // 4:s["commit"] // 4 + B]
+        return _flags(raw, war, waw), mark
+
+
+class RefTF:
+    def __init__(self):
+        self.L = json.load(open(os.path.join(REF, "tf_layout.json")))
+        self.B = self.L["payment_cnt"]
+        self.W = self.L["warehouses"]
+        # 147 / 93 / 67 warp roles per 32 transactions (TF/Predefine.h:38-40)
+        self.covered = covered_txns(self.L, [147, 93, 67], self.B)
+
+    def run(self, txns):
+        """txns: Payment records (TpccBatch.TXN_DTYPE) of one batch, TID = index."""
+        L, B = self.L, self.B
+        ps, pq, lg = L["payment_set"], L["payment_query"], L["log"]
+        assert len(txns) == B
+        query = np.zeros(pq["size"], dtype=np.uint8)
+        qv = query.view(np.uint32)
+
+        def put(field, values):
+            qv[pq[field] // 4:pq[field] // 4 + B] = np.asarray(values, dtype=np.uint32)
+
+        ki = txns["kind_info"]
+        put("W_ID", txns["w"])
+        put("D_ID", (ki >> 16) & 0xFF)
+        put("C_ID", txns["c_id"])
+        put("C_LAST", np.zeros(B))
+        put("isName", np.zeros(B))
+        put("C_D_ID", ki >> 24)
+        put("C_W_ID", txns["c_w"])
+        put("H_AMOUNT", txns["b"])
+        put("H_ID", txns["a"])
+        put("TID", np.arange(B))
+        pset = np.zeros(ps["size"], dtype=np.uint8)
+        nset = np.zeros(max(16, L["neworder_set"]), dtype=np.uint8)
+        nquery = np.zeros(max(16, L["neworder_query"]), dtype=np.uint8)
+        log = np.zeros(lg["size"], dtype=np.uint8)
+        log[:lg["w_ytd"]] = 0xFF  # clear_LOG (TF/Database.h:78-102)
+        snap = np.zeros(L["snapshot"], dtype=np.uint8)
+        index = np.zeros(max(16, L["index"]), dtype=np.uint8)
+        # argument order of KERNEL_EXECUTE / CHECK / WRITEBACK (TF/tp.cu:24-30)
+        _launch("tf", L, [nset, pset, nquery, query, log, snap, index], [0, 1, 0, 0, 0, 0, 0])
+        sv = pset.view(np.uint32)
+        raw = sv[ps["raw"] // 4:ps["raw"] // 4 + B]
+        war = sv[ps["war"] // 4:ps["war"] // 4 + B]
+        waw = sv[ps["waw"] // 4:ps["waw"] // 4 + B]
+        return _flags(raw, war, waw)

@@ -1,0 +1,94 @@
+"""The reference's own CUDA kernels on our batches: the parity pin.
+
+The reference ships no tests and no golden vectors, so its kernels themselves
+are the pin.  oracle/ref_build.py compiles LTPG/YCSB/1 and
+LTPG/TPCC-allopt-final as shipped (sm_103a cubins plus struct layouts from
+their own headers); oracle/reference.py feeds them our batches.  Their
+per-transaction conflict flags must equal the oracle's and the engine's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import reference
+from ltpg_gb300 import Engine, TpccGenerator, YcsbBatch, YcsbGenerator, abi
+
+pytestmark = pytest.mark.gpu
+KEY_MASK = (1 << abi.YCSB_KEY_BITS) - 1
+
+
+@pytest.fixture(scope="module")
+def ref(gpu):
+    if not reference.available():
+        pytest.skip("reference kernels not built: oracle/_ref is made by oracle/ref_build.py where the "
+                    "reference sources are")
+    return True
+
+
+def _ycsb_batch(read_keys, write_keys, values):
+    B = len(write_keys)
+    ops = np.full((B, 12), abi.YCSB_OP_PAD, dtype=np.uint32)
+    ops[:, :9] = read_keys
+    ops[:, 9] = np.uint32(0x80000000) | write_keys.astype(np.uint32)
+    val_off = np.arange(B + 1, dtype=np.uint32)
+    return YcsbBatch(ops.ravel(), val_off, values, B, 10)
+
+
+@pytest.mark.parametrize("theta", [0.0, 0.6, 0.99])
+def test_reference_ycsb_flags_match(ref, theta):
+    r = reference.RefY1()
+    B, n = r.B, r.n
+    assert (B, n, r.reads) == (10000, 1000000, 9)
+    eng = Engine(device=0, n_slots=1, max_txn=B, max_ops_per_txn=10)
+    try:
+        eng.load_ycsb(5, n)
+        o = oracle.YcsbOracle(5, n)
+        g = YcsbGenerator(5, n - 1, B, 10, 0, theta)  # keys 0 .. n-2, shifted to 1 .. n-1 below
+        for bid in range(2):
+            b = g.batch(bid)
+            keys = (b.ops.reshape(B, b.op_stride)[:, :10] & KEY_MASK).astype(np.uint32) + 1
+            ref_flags, mark = r.run(keys[:, :9], keys[:, 9])
+            ours = _ycsb_batch(keys[:, :9], keys[:, 9], np.arange(B, dtype=np.uint64) + 7)
+            want = o.run(ours)[0]
+            # the reference's grids reach every op of the first 9,984 transactions
+            # only (covered_txns); the last 16 lose their write registration and
+            # checks.  Missing registrations of larger TIDs cannot change the
+            # flags of smaller ones, so the covered prefix is exact.
+            c = r.covered
+            assert c == 9984
+            assert np.array_equal(ref_flags[:c], want[:c]), np.nonzero(ref_flags[:c] != want[:c])[0][:10]
+            assert np.array_equal(mark[:c].astype(bool), (want[:c] & abi.FLAG_COMMIT) != 0)
+            for mode in ["plain", "graph"]:
+                eng.upload(0, ours)
+                eng.run_batch(0, mode)
+                eng.sync()
+            # the engine ran the batch twice (plain, graph) on an evolving image;
+            # flags depend only on the keys, not on the values
+            assert np.array_equal(eng.txn_flags(0, B), want)
+            assert 0 < int((want & abi.FLAG_COMMIT != 0).sum()) <= B
+    finally:
+        eng.close()
+
+
+def test_reference_payment_flags_match(ref):
+    r = reference.RefTF()
+    B, W = r.B, r.W
+    assert (B, W) == (65536, 64)
+    g = TpccGenerator(9, W, B, neworder_pct=0)
+    o = oracle.TpccOracle(9, W)
+    eng = Engine(device=0, n_slots=1, max_txn=B, max_ops_per_txn=16, max_lines=16)
+    try:
+        eng.load_tpcc(9, W)
+        for _ in range(2):
+            b = g.next()
+            ref_flags = r.run(b.txns)
+            want = o.run(b)[0]
+            assert r.covered == B  # TF's grids reach every Payment op
+            assert np.array_equal(ref_flags, want), np.nonzero(ref_flags != want)[0][:10]
+            eng.upload(0, b)
+            eng.run_batch(0, "graph")
+            eng.sync()
+            assert np.array_equal(eng.txn_flags(0, B), want)
+            assert (want & abi.FLAG_WAW).any() and (want & abi.FLAG_COMMIT).any()
+    finally:
+        eng.close()
