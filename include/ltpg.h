@@ -288,18 +288,47 @@ int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);
 /* ---- hot-key staging ----------------------------------------------------------
  * Keys hash into LTPG_STAGE_BUCKETS buckets (ltpg_key_bucket).  Registrations of
  * keys in a staged bucket are combined in shared memory per block and reach the
- * global slot table as one atomic per key and block.  The staged set is chosen
+ * global slot table as one atomic per key and block; a staged key's row
+ * checksum is kept with its entry, so later reads of it in the block skip the
+ * row read.  The staged set is chosen
  * by the contention predictor or given here; it changes speed only, never a
  * commit decision.  n = 0 turns staging off.  At most
  * LTPG_STAGE_ENTRIES / stage_ways buckets are staged (extra ones are ignored). */
 #define LTPG_STAGE_BUCKETS 65536u
-#define LTPG_STAGE_ENTRIES 4096u
+#define LTPG_STAGE_ENTRIES 1024u
 uint32_t ltpg_key_bucket(uint32_t key);
 int ltpg_stage_set(ltpg_ctx *ctx, const uint32_t *buckets, uint32_t n);
 /* Per-bucket registration counts accumulated by the tuned execute kernels
  * since the last reset (exact for staged buckets, sampled 1 in 16 and scaled
  * for the others): LTPG_STAGE_BUCKETS uint32 values. */
 int ltpg_bucket_counts(ltpg_ctx *ctx, uint32_t *host_counts, int reset);
+
+/* ---- contention predictor -----------------------------------------------------
+ * A small MLP (4 -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation) predicts
+ * each key-hash bucket's registration count in the next batch from its counts
+ * in the last 4 batches, and its top buckets become the staged set.  It is
+ * trained online on the GPU (one Adam step per batch on 4,096 buckets, label =
+ * the latest batch's counts).  When enabled it runs after every tuned YCSB
+ * batch (inside CUDA graphs too).  It changes which keys are staged, never a
+ * commit decision.  No counterpart in the reference. */
+typedef struct {
+    uint32_t enable;       /* 0 turns the predictor and staging off            */
+    uint32_t train;        /* 1 = train online, 0 = frozen weights            */
+    uint32_t stage;        /* 1 = stage the predicted top buckets             */
+    uint32_t train_every;  /* reserved, 1                                     */
+    float lr;              /* Adam learning rate (default 3e-3)                */
+    uint32_t pad;
+    uint64_t seed;         /* initial weights                                  */
+} ltpg_predictor_cfg;
+#define LTPG_PRED_PARAMS 4545 /* packed FP32: W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3 */
+int ltpg_predictor_enable(ltpg_ctx *ctx, const ltpg_predictor_cfg *cfg);
+int ltpg_predictor_stats(ltpg_ctx *ctx, float *last_loss, uint64_t *train_steps);
+int ltpg_predictor_get_params(ltpg_ctx *ctx, float *host, size_t n);
+int ltpg_predictor_set_params(ltpg_ctx *ctx, const float *host, size_t n);
+/* Test hooks: forward pass on given features (n <= 4096, [n][4] log1p counts),
+ * and the gradient of mean((y - t)^2) with respect to the packed parameters. */
+int ltpg_predictor_forward(ltpg_ctx *ctx, const float *host_x, uint32_t n, float *host_y);
+int ltpg_predictor_gradients(ltpg_ctx *ctx, const float *host_x, const float *host_t, uint32_t n, float *host_grad);
 
 /* ---- measurement ------------------------------------------------------------- */
 /* Totals since ltpg_create: transactions committed (counted on the device by

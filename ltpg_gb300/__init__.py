@@ -341,6 +341,37 @@ class Engine:
         self._ck(lib().ltpg_bucket_counts(self._h, _p(out), int(bool(reset))))
         return out
 
+    def predictor(self, enable=True, train=True, stage=True, lr=3e-3, seed=1):
+        """Turns the contention predictor on (it then runs after every tuned YCSB batch)."""
+        cfg = abi.PredictorC(int(enable), int(train), int(stage), 1, lr, 0, seed)
+        self._ck(lib().ltpg_predictor_enable(self._h, C.byref(cfg)))
+
+    def predictor_stats(self):
+        loss, steps = C.c_float(), C.c_uint64()
+        self._ck(lib().ltpg_predictor_stats(self._h, C.byref(loss), C.byref(steps)))
+        return {"loss": loss.value, "train_steps": steps.value}
+
+    def predictor_params(self, values=None):
+        if values is None:
+            out = np.empty(abi.PRED_PARAMS, dtype=np.float32)
+            self._ck(lib().ltpg_predictor_get_params(self._h, _p(out), len(out)))
+            return out
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        self._ck(lib().ltpg_predictor_set_params(self._h, _p(v), len(v)))
+
+    def predictor_forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty(len(x), dtype=np.float32)
+        self._ck(lib().ltpg_predictor_forward(self._h, _p(x), len(x), _p(out)))
+        return out
+
+    def predictor_gradients(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        out = np.empty(abi.PRED_PARAMS, dtype=np.float32)
+        self._ck(lib().ltpg_predictor_gradients(self._h, _p(x), _p(t), len(x), _p(out)))
+        return out
+
     def counters(self):
         """(transactions committed, kernels launched) since the engine was created."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -20,7 +20,8 @@ TPCC_MAX_LINES = 15
 CFG_STRICT_INSERT = 1
 NOALLOC_MAX_RECORDS = 1 << 20
 STAGE_BUCKETS = 65536
-STAGE_ENTRIES = 4096
+STAGE_ENTRIES = 1024
+PRED_PARAMS = 4545
 
 
 class YcsbBatchC(C.Structure):
@@ -52,6 +53,11 @@ class ConfigC(C.Structure):
 class LaunchC(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("ops_per_thread", C.c_uint32), ("blocks_per_sm", C.c_uint32),
                 ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("dedupe", C.c_uint32)]
+
+
+class PredictorC(C.Structure):
+    _fields_ = [("enable", C.c_uint32), ("train", C.c_uint32), ("stage", C.c_uint32), ("train_every", C.c_uint32),
+                ("lr", C.c_float), ("pad", C.c_uint32), ("seed", C.c_uint64)]
 
 
 class StatsC(C.Structure):
@@ -103,6 +109,12 @@ SIGNATURES = {
     "ltpg_key_bucket": (U32, [U32]),
     "ltpg_stage_set": (C.c_int, [P, P, U32]),
     "ltpg_bucket_counts": (C.c_int, [P, P, C.c_int]),
+    "ltpg_predictor_enable": (C.c_int, [P, C.POINTER(PredictorC)]),
+    "ltpg_predictor_stats": (C.c_int, [P, C.POINTER(C.c_float), C.POINTER(U64)]),
+    "ltpg_predictor_get_params": (C.c_int, [P, P, SZ]),
+    "ltpg_predictor_set_params": (C.c_int, [P, P, SZ]),
+    "ltpg_predictor_forward": (C.c_int, [P, P, U32, P]),
+    "ltpg_predictor_gradients": (C.c_int, [P, P, P, U32, P]),
     "ltpg_counters": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
     "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),

@@ -110,6 +110,7 @@ Slot *get_slot(ltpg_ctx *c, uint32_t slot) {
 }  // namespace
 
 namespace ltpg {
+void drop_graphs_ctx(ltpg_ctx *c) { drop_graphs(c); }
 void prof_mark(ltpg_ctx *c, int i) {
     if (!c->profiling) return;
     const size_t k = (size_t)c->cur_slot * 4 + (size_t)i;
@@ -160,12 +161,15 @@ int ltpg_destroy(ltpg_ctx *c) {
     cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     for (auto ev : c->prof_events) cudaEventDestroy(ev);
+    predictor_free(c);
     for (auto &s : c->slots) free_slot(s);
     dev_free(c->ycsb.rows);
     dev_free(c->ycsb.reg);
     for (auto &t : c->tpcc.tab) dev_free(t);
     dev_free(c->tpcc.reg);
     dev_free(c->stage_map);
+    dev_free(c->stage_bits);
+    dev_free(c->stage_rank);
     dev_free(c->bucket_counts);
     dev_free(c->ctl);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -625,19 +629,39 @@ int ltpg_stage_set(ltpg_ctx *c, const uint32_t *buckets, uint32_t n) {
     if (!c || (n && !buckets)) return LTPG_ERR_INVALID;
     if (!c->stage_map) {
         CK(dev_alloc(&c->stage_map, LTPG_STAGE_BUCKETS), "alloc stage map");
+        CK(dev_alloc(&c->stage_bits, LTPG_STAGE_BUCKETS / 32), "alloc stage bits");
+        CK(dev_alloc(&c->stage_rank, LTPG_STAGE_BUCKETS / 32), "alloc stage rank");
         CK(dev_alloc(&c->bucket_counts, LTPG_STAGE_BUCKETS), "alloc bucket counts");
         CK(cudaMemset(c->bucket_counts, 0, LTPG_STAGE_BUCKETS * 4), "clear bucket counts");
     }
-    std::vector<uint16_t> map(LTPG_STAGE_BUCKETS, 0xFFFFu);
+    // the first LTPG_STAGE_ENTRIES / ways distinct buckets of the list are staged;
+    // a staged bucket's group is its rank among the staged buckets
     const uint32_t ways = c->launch_y.ways ? c->launch_y.ways : 4u;
     const uint32_t groups = LTPG_STAGE_ENTRIES / ways;
-    uint32_t g = 0;
-    for (uint32_t i = 0; i < n && g < groups; ++i) {
+    std::vector<uint32_t> bits(LTPG_STAGE_BUCKETS / 32, 0u), rank(LTPG_STAGE_BUCKETS / 32, 0u);
+    uint32_t taken = 0;
+    for (uint32_t i = 0; i < n && taken < groups; ++i) {
         if (buckets[i] >= LTPG_STAGE_BUCKETS) return fail(c, LTPG_ERR_INVALID, "bucket out of range");
-        if (map[buckets[i]] == 0xFFFFu) map[buckets[i]] = (uint16_t)g++;
+        uint32_t &w = bits[buckets[i] >> 5];
+        const uint32_t bit = 1u << (buckets[i] & 31u);
+        if (!(w & bit)) {
+            w |= bit;
+            ++taken;
+        }
+    }
+    std::vector<uint16_t> map(LTPG_STAGE_BUCKETS, 0xFFFFu);
+    uint32_t acc = 0;
+    for (uint32_t wi = 0; wi < LTPG_STAGE_BUCKETS / 32; ++wi) {
+        rank[wi] = acc;
+        for (uint32_t bi = 0; bi < 32; ++bi)
+            if (bits[wi] >> bi & 1u) map[wi * 32 + bi] = (uint16_t)acc++;
     }
     CK(cudaMemcpyAsync(c->stage_map, map.data(), LTPG_STAGE_BUCKETS * 2, cudaMemcpyHostToDevice, c->stream),
        "upload stage map");
+    CK(cudaMemcpyAsync(c->stage_bits, bits.data(), LTPG_STAGE_BUCKETS / 8, cudaMemcpyHostToDevice, c->stream),
+       "upload stage bits");
+    CK(cudaMemcpyAsync(c->stage_rank, rank.data(), LTPG_STAGE_BUCKETS / 8, cudaMemcpyHostToDevice, c->stream),
+       "upload stage rank");
     CK(cudaStreamSynchronize(c->stream), "sync");
     const uint32_t on = n ? 1u : 0u;
     if (on != c->stage_on) drop_graphs(c);

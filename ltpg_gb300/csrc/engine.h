@@ -96,6 +96,8 @@ struct LaunchCfg {
 
 }  // namespace ltpg
 
+struct ltpg_predictor_state;
+
 struct ltpg_ctx {
     int device = 0;
     ltpg_config cfg{};
@@ -113,8 +115,13 @@ struct ltpg_ctx {
     int persist_blocks_y = 0, persist_blocks_c = 0;
     // staging map (bucket -> way group), predictor output
     uint16_t *stage_map = nullptr;
+    uint32_t *stage_bits = nullptr;  // staged-bucket bitmap (65536 bits)
+    uint32_t *stage_rank = nullptr;  // staged buckets before each bitmap word
     uint32_t *bucket_counts = nullptr;  // per-batch access counts per bucket
     uint32_t stage_on = 0;
+    // contention predictor (predictor.cu)
+    ltpg_predictor_state *pred = nullptr;
+    uint32_t pred_on = 0, pred_train = 0;
     // measurement
     uint64_t launches = 0;
     bool profiling = false;
@@ -135,6 +142,11 @@ struct ltpg_ctx {
 namespace ltpg {
 // Records profiling event i (0..3) of the slot being run, if profiling is on.
 void prof_mark(ltpg_ctx *c, int i);
+// Drops the cached CUDA graphs (launch settings changed).
+void drop_graphs_ctx(ltpg_ctx *c);
+// Predictor step after a tuned YCSB batch (predictor.cu).
+cudaError_t predictor_after_batch(ltpg_ctx *c);
+void predictor_free(ltpg_ctx *c);
 // Counts kernels launched by the engine.
 inline void count_launch(ltpg_ctx *c, uint64_t n = 1) { c->launches += n; }
 cudaError_t ycsb_init_table(ltpg_ctx *c);

@@ -5,20 +5,34 @@
 
 namespace ltpg {
 
-// One staged row: its key and the minimum read / write TIDs seen by this block.
-struct StageEnt {
+// One staged row: its key, the minimum read / write TIDs seen by this block,
+// the number of registrations it absorbed, and the row's checksum once some
+// read of it in this block has loaded the row (dig_ok = 1).
+struct __align__(16) StageEnt {
     uint32_t key, rmin, wmin, cnt;
+    unsigned long long dig;
+    uint32_t dig_ok, pad;
 };
 constexpr uint32_t STAGE_EMPTY = 0xFFFFFFFFu;
 constexpr uint32_t STAGE_NONE = 0xFFFFu;     // stage_map value of an unstaged bucket
 constexpr uint32_t STAGE_BUCKETS = LTPG_STAGE_BUCKETS;      // key-hash buckets seen by the predictor
-constexpr uint32_t STAGE_MAX_ENTRIES = LTPG_STAGE_ENTRIES;  // 64 KB of shared memory per block
+constexpr uint32_t STAGE_MAX_ENTRIES = LTPG_STAGE_ENTRIES;  // 32 KB of shared memory per block
 constexpr uint32_t COUNT_SAMPLE = 16u;       // unstaged ops are counted 1 in 16
 
 __device__ __forceinline__ uint32_t key_bucket(uint32_t key) { return (key * 0x9E3779B1u) >> 16; }
 
+// Staged-bucket set in compact form: one bit per bucket and, per 32-bucket
+// word, the number of staged buckets before it.  The group of a staged bucket
+// is its rank among the staged buckets.
+constexpr uint32_t STAGE_WORDS = STAGE_BUCKETS / 32u;
+__device__ __forceinline__ uint32_t stage_group(const uint32_t *bits, const uint32_t *rank, uint32_t b) {
+    const uint32_t w = bits[b >> 5], bit = 1u << (b & 31u);
+    return (w & bit) ? rank[b >> 5] + __popc(w & (bit - 1u)) : STAGE_NONE;
+}
+
 __device__ __forceinline__ void stage_init(StageEnt *tab, uint32_t n) {
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) tab[i] = StageEnt{STAGE_EMPTY, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u};
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        tab[i] = StageEnt{STAGE_EMPTY, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0ull, 0u, 0u};
 }
 
 // Finds or claims the entry of `key` among the `ways` entries of group g.

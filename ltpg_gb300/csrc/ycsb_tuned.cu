@@ -32,6 +32,8 @@ struct YcsbTunedArgs {
     DevStats *st;
     DevCtl *ctl;
     const uint16_t *stage_map;
+    const uint32_t *stage_bits;
+    const uint32_t *stage_rank;
     uint32_t *bucket_counts;
     uint32_t ways, stage_entries;
     uint32_t filter;
@@ -379,9 +381,12 @@ __global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t 
 // instead of five.  The five chunks are xor-folded within their lane group and
 // handed back to the lane that owns the op.
 template <bool kStage, bool kFilter, bool kDedupe>
-__device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt *tab, uint64_t tag) {
+__device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt *tab, const uint32_t *sbits,
+                                               const uint32_t *srank, uint64_t tag) {
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lanes_below = (1u << lane) - 1u;
     const uint32_t lpt = a.stride;  // lanes per transaction
+    const uint32_t groups = a.ways ? a.stage_entries / a.ways : 0u;
     const uint64_t nw = (uint64_t)a.B * a.stride;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     const uint32_t grp = lane / 5, chunk = lane % 5;  // row-read lane groups (6 x 5 lanes)
@@ -399,54 +404,73 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
         }
         const bool upd = ycsb_is_update(w);
         const bool rd = valid && !upd;
-        bool need = valid;
+        StageEnt *e = nullptr;
+        bool have_dig = false;
+        unsigned long long x = 0;
         if (kStage && valid) {
             const uint32_t b = key_bucket(key);
-            const uint32_t g = __ldg(a.stage_map + b);
-            if (g != STAGE_NONE && (g + 1) * a.ways <= a.stage_entries) {
-                StageEnt *e = stage_find(tab, g, a.ways, key);
-                if (e) {
-                    atomicMin(upd ? &e->wmin : &e->rmin, t);
-                    atomicAdd(&e->cnt, 1u);
-                    need = false;
-                }
+            const uint32_t g = stage_group(sbits, srank, b);
+            if (g < groups) e = stage_find(tab, g, a.ways, key);
+            if (!e && (t % COUNT_SAMPLE) == 0u) atomicAdd(a.bucket_counts + b, COUNT_SAMPLE);
+            if (e && rd && *reinterpret_cast<volatile uint32_t *>(&e->dig_ok)) {
+                __threadfence_block();
+                x = *reinterpret_cast<volatile unsigned long long *>(&e->dig);
+                have_dig = true;
             }
-            if (need && (t % COUNT_SAMPLE) == 0u) atomicAdd(a.bucket_counts + b, COUNT_SAMPLE);
         }
-        // row chunks of the warp's reads: round r covers ops 6r .. 6r+5
-        const unsigned rdmask = __ballot_sync(FULL, rd);
+        // one row read per distinct key of the warp: peers share the leader's
+        unsigned peers = 1u << lane;
+        if (kDedupe || kStage) peers = __match_any_sync(FULL, valid ? (key | (upd ? 0x80000000u : 0u)) : 0xFFFFFFFFu);
+        const uint32_t leader_lane = (uint32_t)__ffs(peers) - 1u;
+        const bool leader = valid && leader_lane == lane;
+        // rows still to read, compacted: round r reads the (6r + g)-th of them
+        const unsigned need = __ballot_sync(FULL, rd && !have_dig && leader);
+        const uint32_t n_need = __popc(need);
         ulonglong2 ch[6];
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
-            const uint32_t src = (uint32_t)r * 6u + grp;
+            const uint32_t idx = (uint32_t)r * 6u + grp;
+            const bool go = grp < 6 && idx < n_need;
+            const uint32_t src = go ? __fns(need, 0, (int)idx + 1) : 0u;
             const uint32_t k_src = __shfl_sync(FULL, key, src & 31u);
-            const bool go = grp < 6 && src < 32 && ((rdmask >> src) & 1u);
             ch[r] = go ? ld_nc16_issue(reinterpret_cast<const char *>(a.rows + (uint64_t)k_src * LTPG_YCSB_FIELDS) +
                                        16u * chunk)
                        : make_ulonglong2(0ull, 0ull);
         }
+        // registration: staged rows in shared memory, the rest through the
+        // warp dedupe and the slot filter
+        const bool need_global = valid && !e;
         uint64_t cur = ~0ull;
         unsigned long long *slot = upd ? &a.reg[key].w : &a.reg[key].r;
-        if (kFilter && need) cur = ld_ca_u64(slot);
-        bool leader = need;
-        if (kDedupe) {
-            const unsigned peers = __match_any_sync(FULL, need ? (key | (upd ? 0x80000000u : 0u)) : 0xFFFFFFFFu);
-            leader = need && (__ffs(peers) - 1) == (int)lane;
+        if (kFilter && need_global) cur = ld_ca_u64(slot);
+        if (kStage && e && leader) {
+            atomicMin(upd ? &e->wmin : &e->rmin, t);
+            atomicAdd(&e->cnt, (uint32_t)__popc(peers));
         }
         const unsigned long long mine = tag | t;
-        if (leader && cur > mine) red_min(slot, mine);
+        if (need_global && (kDedupe ? leader : true) && cur > mine) red_min(slot, mine);
         // fold the five chunks of each row onto its group's first lane (5g),
         // then hand the row's xor to the lane that owns the op
-        unsigned long long x = 0;
+        const uint32_t my_rank = __popc(need & lanes_below);
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
+            if ((uint32_t)r * 6u >= n_need) break;  // warp-uniform
             const unsigned long long c0 = ch[r].x ^ ch[r].y;
             unsigned long long c = c0 ^ __shfl_down_sync(FULL, c0, 1);  // lane 5g: chunks 0,1
             c ^= __shfl_down_sync(FULL, c, 2);                          // lane 5g: chunks 0..3
             const unsigned long long rowx = c ^ __shfl_down_sync(FULL, c0, 4);  // + chunk 4
             const uint32_t op0 = (uint32_t)r * 6u;
-            const unsigned long long got = __shfl_sync(FULL, rowx, ((lane - op0) * 5u) & 31u);
-            if (lane >= op0 && lane < op0 + 6u) x = got;
+            const unsigned long long got = __shfl_sync(FULL, rowx, ((my_rank - op0) * 5u) & 31u);
+            if (((need >> lane) & 1u) && my_rank >= op0 && my_rank < op0 + 6u) x = got;
+        }
+        {
+            const unsigned long long from_leader = __shfl_sync(FULL, x, leader_lane);
+            if (!have_dig) x = from_leader;
+        }
+        if (kStage && e && rd && !have_dig && leader) {  // publish the checksum for later reads in this block
+            e->dig = x;
+            __threadfence_block();
+            *reinterpret_cast<volatile uint32_t *>(&e->dig_ok) = 1u;
         }
         unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
         for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
@@ -457,13 +481,19 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
 template <bool kStage, bool kFilter, bool kDedupe>
 __global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
-    StageEnt *tab = reinterpret_cast<StageEnt *>(smem);
+    uint32_t *sbits = reinterpret_cast<uint32_t *>(smem);
+    uint32_t *srank = sbits + STAGE_WORDS;
+    StageEnt *tab = reinterpret_cast<StageEnt *>(srank + STAGE_WORDS);
     const uint64_t tag = slot_tag(a.ctl->epoch);
     if (kStage) {
+        for (uint32_t i = threadIdx.x; i < STAGE_WORDS; i += blockDim.x) {
+            sbits[i] = __ldg(a.stage_bits + i);
+            srank[i] = __ldg(a.stage_rank + i);
+        }
         stage_init(tab, a.stage_entries);
         __syncthreads();
     }
-    coop_exec_loop<kStage, kFilter, kDedupe>(a, tab, tag);
+    coop_exec_loop<kStage, kFilter, kDedupe>(a, tab, sbits, srank, tag);
     if (kStage) {
         __syncthreads();
         const uint32_t ops = stage_flush(tab, a.stage_entries, a.reg, tag, a.bucket_counts);
@@ -532,8 +562,8 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         __syncthreads();
     }
     if (a.stride <= 32 && (a.stride & (a.stride - 1)) == 0) {
-        if (a.filter) coop_exec_loop<kStage, true, true>(a, p.tab, tag);
-        else coop_exec_loop<kStage, false, true>(a, p.tab, tag);
+        if (a.filter) coop_exec_loop<kStage, true, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
+        else coop_exec_loop<kStage, false, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
     } else {
         exec_tiles<kStage>(a, p.dig, p.tab, tag);
     }
@@ -584,7 +614,7 @@ static void launch_fast_t(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, uint3
 
 static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
     const LaunchCfg &L = c->launch_y;
-    const size_t smem = stage ? (size_t)a.stage_entries * sizeof(StageEnt) : 0;
+    const size_t smem = stage ? 2 * STAGE_WORDS * sizeof(uint32_t) + (size_t)a.stage_entries * sizeof(StageEnt) : 0;
     void (*k)(YcsbTunedArgs);
     const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
     switch (sel) {
@@ -649,11 +679,14 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.bitmap = s.bitmap;
     a.st = s.stats;
     a.ctl = c->ctl;
-    const bool stage = c->stage_on && c->stage_map && c->bucket_counts;
+    const bool stage = (c->stage_on || c->pred_on) && c->stage_map && c->bucket_counts;
     a.stage_map = c->stage_map;
+    a.stage_bits = c->stage_bits;
+    a.stage_rank = c->stage_rank;
     a.bucket_counts = c->bucket_counts;
     a.ways = L.ways ? L.ways : 4u;
-    a.stage_entries = stage ? STAGE_MAX_ENTRIES / a.ways * a.ways : 0u;
+    // with the predictor counting but staging off, the staging table is empty
+    a.stage_entries = (stage && c->stage_on) ? STAGE_MAX_ENTRIES / a.ways * a.ways : 0u;
     a.filter = L.filter;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
     const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
@@ -682,6 +715,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         if (e != cudaSuccess) return e;
         prof_mark(c, 1);
         prof_mark(c, 2);
+        if ((e = predictor_after_batch(c)) != cudaSuccess) return e;
         prof_mark(c, 3);
         return cudaSuccess;
     }
@@ -701,6 +735,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     ycsb_checkwb_tuned<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 2);
+    if ((e = predictor_after_batch(c)) != cudaSuccess) return e;
     prof_mark(c, 3);
     return cudaSuccess;
 }
