@@ -330,6 +330,45 @@ int ltpg_predictor_set_params(ltpg_ctx *ctx, const float *host, size_t n);
 int ltpg_predictor_forward(ltpg_ctx *ctx, const float *host_x, uint32_t n, float *host_y);
 int ltpg_predictor_gradients(ltpg_ctx *ctx, const float *host_x, const float *host_t, uint32_t n, float *host_grad);
 
+/* ---- serving loop ---------------------------------------------------------------
+ * Continuous batching over two engines, one holding the TPC-C tables and one
+ * the YCSB table.  Requests arrive open-loop (Poisson at `rate` per second for
+ * `duration_s`), tpcc_pct % TPC-C (drawn in order from a pool made by the
+ * generator with *tp) and the rest YCSB (pool from *yp).  A batch closes at
+ * max_batch requests or when its first request has waited deadline_ms, and
+ * only when a device slot is free; the slots in flight are limited by the
+ * engines' slots and by budget_bytes (registration tables + batch buffers).
+ * The TPC-C and YCSB parts of a batch run concurrently on two streams and the
+ * next batch's upload overlaps the current kernels.  Latency = arrival to the
+ * commit bitmap in host memory, over committed requests.  No counterpart in
+ * the reference.  With `record` non-null, the batch boundaries and
+ * every request's flags and result are kept for replay (free with
+ * ltpg_serve_record_free). */
+typedef struct {
+    double rate;            /* arrivals per second                       */
+    double duration_s;      /* arrival window                            */
+    double deadline_ms;     /* batch closing deadline (2.0)              */
+    uint64_t budget_bytes;  /* device budget, 0 = no limit (40 GB)       */
+    uint64_t seed;
+    uint32_t max_batch;     /* batch closing size (262,144)              */
+    uint32_t tpcc_pct;      /* share of TPC-C requests (70)              */
+    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT      */
+    uint32_t slots;         /* batches in flight (<= engine slots)       */
+} ltpg_serve_cfg;
+typedef struct {
+    uint64_t submitted, committed, batches, slots, waited_for_slot;
+    double wall_s, throughput, mean_batch, mean_ms, p50_ms, p99_ms, p999_ms;
+} ltpg_serve_stats;
+typedef struct ltpg_serve_record ltpg_serve_record;
+int ltpg_serve_run(ltpg_ctx *tpcc_ctx, ltpg_ctx *ycsb_ctx, const ltpg_serve_cfg *cfg, const ltpg_tpcc_params *tp,
+                   const ltpg_ycsb_params *yp, ltpg_serve_stats *out, ltpg_serve_record **record);
+/* Record: batches[4 * i .. 4 * i + 3] = TPC-C pool start, count, YCSB pool
+ * start, count of batch i (pool index = order of arrival within the type). */
+int ltpg_serve_record_sizes(const ltpg_serve_record *r, uint64_t *n_batches, uint64_t *n_tpcc, uint64_t *n_ycsb);
+int ltpg_serve_record_get(const ltpg_serve_record *r, uint64_t *batches, uint8_t *tpcc_flags, int64_t *tpcc_results,
+                          uint8_t *ycsb_flags, int64_t *ycsb_results);
+int ltpg_serve_record_free(ltpg_serve_record *r);
+
 /* ---- measurement ------------------------------------------------------------- */
 /* Totals since ltpg_create: transactions committed (counted on the device by
  * the write-back kernels) and kernels launched by the engine (a graph launch

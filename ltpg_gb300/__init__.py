@@ -394,3 +394,37 @@ class Engine:
         out = (C.c_float * 3)()
         self._ck(lib().ltpg_kernel_times(self._h, slot, out))
         return list(out)
+
+
+def serve(tpcc_engine, ycsb_engine, rate, duration_s, tpcc_params, ycsb_params, deadline_ms=2.0,
+          max_batch=262144, tpcc_pct=70, mode="fused", budget_bytes=40 << 30, slots=4, seed=1, record=False):
+    """Runs the continuous-batching request loop (see ltpg_serve_run in include/ltpg.h).
+
+    tpcc_params / ycsb_params: dicts of TpccGenerator / YcsbGenerator arguments
+    (seed, warehouses, n_txn, ...) describing the request pools.  Returns the
+    stats dict, and with record=True also the replay record."""
+    cfg = abi.ServeCfgC(rate, duration_s, deadline_ms, budget_bytes, seed, max_batch, tpcc_pct,
+                        MODES[mode] if isinstance(mode, str) else mode, slots)
+    tp = abi.TpccParamsC(tpcc_params["seed"], tpcc_params["warehouses"], tpcc_params.get("n_txn", 262144),
+                         tpcc_params.get("neworder_pct", 50), tpcc_params.get("remote_line_pct", 1),
+                         tpcc_params.get("remote_pay_pct", 15))
+    yp = abi.YcsbParamsC(ycsb_params["seed"], ycsb_params["n_records"], ycsb_params.get("n_txn", 262144),
+                         ycsb_params.get("ops_per_txn", 10), ycsb_params.get("update_pct", 50),
+                         ycsb_params.get("rotate_every", 0), ycsb_params.get("theta", 0.9))
+    st = abi.ServeStatsC()
+    rec = C.c_void_p()
+    code = lib().ltpg_serve_run(tpcc_engine._h, ycsb_engine._h, C.byref(cfg), C.byref(tp), C.byref(yp),
+                                C.byref(st), C.byref(rec) if record else None)
+    _check(code, tpcc_engine._h)
+    stats = {k: getattr(st, k) for k, _ in abi.ServeStatsC._fields_}
+    if not record:
+        return stats
+    nb, nc, ny = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    lib().ltpg_serve_record_sizes(rec, C.byref(nb), C.byref(nc), C.byref(ny))
+    out = {"batches": np.zeros((nb.value, 4), dtype=np.uint64),
+           "tpcc_flags": np.zeros(nc.value, dtype=np.uint8), "tpcc_results": np.zeros(nc.value, dtype=np.int64),
+           "ycsb_flags": np.zeros(ny.value, dtype=np.uint8), "ycsb_results": np.zeros(ny.value, dtype=np.int64)}
+    lib().ltpg_serve_record_get(rec, _p(out["batches"]), _p(out["tpcc_flags"]), _p(out["tpcc_results"]),
+                                _p(out["ycsb_flags"]), _p(out["ycsb_results"]))
+    lib().ltpg_serve_record_free(rec)
+    return stats, out

@@ -60,6 +60,19 @@ class PredictorC(C.Structure):
                 ("lr", C.c_float), ("pad", C.c_uint32), ("seed", C.c_uint64)]
 
 
+class ServeCfgC(C.Structure):
+    _fields_ = [("rate", C.c_double), ("duration_s", C.c_double), ("deadline_ms", C.c_double),
+                ("budget_bytes", C.c_uint64), ("seed", C.c_uint64), ("max_batch", C.c_uint32),
+                ("tpcc_pct", C.c_uint32), ("mode", C.c_uint32), ("slots", C.c_uint32)]
+
+
+class ServeStatsC(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("committed", C.c_uint64), ("batches", C.c_uint64),
+                ("slots", C.c_uint64), ("waited_for_slot", C.c_uint64), ("wall_s", C.c_double),
+                ("throughput", C.c_double), ("mean_batch", C.c_double), ("mean_ms", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double)]
+
+
 class StatsC(C.Structure):
     _fields_ = [("n_txn", C.c_uint64), ("commits", C.c_uint64), ("raw", C.c_uint64), ("war", C.c_uint64),
                 ("waw", C.c_uint64), ("staged_ops", C.c_uint64), ("total_ops", C.c_uint64)]
@@ -115,6 +128,11 @@ SIGNATURES = {
     "ltpg_predictor_set_params": (C.c_int, [P, P, SZ]),
     "ltpg_predictor_forward": (C.c_int, [P, P, U32, P]),
     "ltpg_predictor_gradients": (C.c_int, [P, P, P, U32, P]),
+    "ltpg_serve_run": (C.c_int, [P, P, C.POINTER(ServeCfgC), C.POINTER(TpccParamsC), C.POINTER(YcsbParamsC),
+                                 C.POINTER(ServeStatsC), C.POINTER(P)]),
+    "ltpg_serve_record_sizes": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64)]),
+    "ltpg_serve_record_get": (C.c_int, [P, P, P, P, P, P]),
+    "ltpg_serve_record_free": (C.c_int, [P]),
     "ltpg_counters": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
     "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),
