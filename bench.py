@@ -50,7 +50,7 @@ SEED = 20261203
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=1024)
     ap.add_argument("--warmup", type=int, default=32)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ycsb_hc", choices=sorted(WORKLOADS))
@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--cpu-batches", type=int, default=2, help="batches in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=32)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
+    ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
+    ap.add_argument("--serve-seconds", type=float, default=0.25)
     return ap.parse_args()
 
 
@@ -517,6 +520,10 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
                                 "sample": f"{min(args.cpu_batches, len(batches))} whole batches of {B} txn, "
                                           f"single-threaded oracle replay, {s:.1f} s"}
+    if not args.no_predictor and w["kind"] == "ycsb" and w["n_txn"] >= (1 << 18):
+        line["predictor"] = predictor_section(w, batches)
+    if not args.no_serving and args.workload == "ycsb_hc":
+        line["serving"] = serving_section(args)
     if args.sweep and w["kind"] == "ycsb":
         sweep = {}
         for th in [0.0, 0.6, 0.8, 0.99]:
@@ -525,6 +532,69 @@ def main():
                               "plain": r["plain"]["commits"] / r["plain"]["secs"]}
         line["theta_sweep"] = sweep
     print(json.dumps(line), flush=True)
+
+
+def serving_section(args):
+    """Serving loop (configs[4]): Poisson arrivals at 1M / 5M / 20M txn/s, 70 %
+    TPC-C (W = 64) and 30 % YCSB (1M records, 10 ops, 50/50, theta 0.9), batches
+    closing at 262,144 requests or 2 ms, 40 GB device budget; plain vs tuned."""
+    import ltpg_gb300 as L
+    tp = dict(seed=SEED, warehouses=64, n_txn=262144)
+    yp = dict(seed=SEED + 1, n_records=1_000_000, n_txn=262144, ops_per_txn=10, update_pct=50, theta=0.9)
+    c = L.Engine(device=0, n_slots=4, max_txn=262144, max_ops_per_txn=16, max_lines=15 * 262144)
+    y = L.Engine(device=0, n_slots=4, max_txn=262144, max_ops_per_txn=10)
+    out = {}
+    try:
+        for rate in [1e6, 5e6, 2e7]:
+            for mode in ["plain", "fused"]:
+                c.load_tpcc(tp["seed"], tp["warehouses"])
+                y.load_ycsb(yp["seed"], yp["n_records"])
+                st = L.serve(c, y, rate=rate, duration_s=args.serve_seconds, tpcc_params=tp, ycsb_params=yp,
+                             deadline_ms=2.0, max_batch=262144, tpcc_pct=70, mode=mode, budget_bytes=40 << 30,
+                             slots=4)
+                out[f"{rate / 1e6:g}M/s {'tuned' if mode != 'plain' else 'plain'}"] = {
+                    "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "p999_ms": st["p999_ms"],
+                    "committed_per_s": st["throughput"], "submitted": st["submitted"],
+                    "commit_rate": st["committed"] / max(1, st["submitted"]), "batches": st["batches"],
+                    "mean_batch": st["mean_batch"], "slot_waits": st["waited_for_slot"]}
+    finally:
+        c.close()
+        y.close()
+    return out
+
+
+def predictor_section(w, batches):
+    """Predictor-guided staging on the benchmark stream: staging hit rate and
+    execute-kernel time, trained vs untrained vs no staging, with the slot
+    filter off (the warp-aggregated path the predictor complements) and on."""
+    import ltpg_gb300 as L
+    out = {}
+    n_slots = 8
+    for filt in [0, 1]:
+        for name, kw in [("trained", dict(train=True, stage=True)), ("untrained", dict(train=False, stage=True)),
+                         ("no_staging", None)]:
+            e = L.Engine(device=0, n_slots=n_slots, max_txn=w["n_txn"], max_ops_per_txn=w["ops"])
+            try:
+                e.load_ycsb(SEED, w["n_records"])
+                e.set_launch("ycsb", ops_per_thread=1, filter=filt, dedupe=1, stage_ways=1, blocks_per_sm=0)
+                if kw:
+                    e.predictor(enable=True, seed=7, **kw)
+                e.set_profiling(True)
+                hits, ms = [], []
+                for i, b in enumerate(batches[:24]):
+                    e.upload(i % n_slots, b)
+                    e.run_batch(i % n_slots, "fused")
+                    e.sync()
+                    if i >= 8:
+                        hits.append(e.stats(i % n_slots)["staged_ops"] / (b.n_txn * w["ops"]))
+                        ms.append(e.kernel_times(i % n_slots)[0])
+                out[f"filter{filt}_{name}"] = {"staging_hit_rate": float(np.mean(hits)),
+                                               "execute_ms": float(np.mean(ms))}
+                if kw and kw["train"]:
+                    out[f"filter{filt}_{name}"]["loss"] = e.predictor_stats()["loss"]
+            finally:
+                e.close()
+    return out
 
 
 def tpcc_bytes_per_txn():
