@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
     ap.add_argument("--serve-seconds", type=float, default=0.25)
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference's own kernels / the engine on the reference's compiled shapes")
     return ap.parse_args()
 
 
@@ -390,6 +392,85 @@ def cpu_baseline_tpcc(w, batches, n_batches):
     return commits / secs, secs, commits
 
 
+# ---- the reference's compiled batch shapes -------------------------------------------
+# LTPG/YCSB/1 is compiled for 10,000 transactions x (9 reads + 1 write) over
+# 1,000,000 records; LTPG/TPCC-allopt-final for 65,536 Payments over 64
+# warehouses.  Both arms build the same batches here: the reference arm times
+# the reference's own kernels on them, our arm times the engine.
+REF_Y1 = dict(n_records=1_000_000, n_txn=10_000, theta=0.99)
+REF_TF = dict(warehouses=64, n_txn=65_536)
+
+
+def ref_shape_batches():
+    from ltpg_gb300 import TpccGenerator, YcsbBatch, YcsbGenerator, abi
+    B, n = REF_Y1["n_txn"], REF_Y1["n_records"]
+    g = YcsbGenerator(SEED, n - 1, B, 10, 0, REF_Y1["theta"])
+    b = g.batch(0)
+    # keys 1 .. n-1: the reference routes key 0 around registration in its Zipf mode
+    keys = (b.ops.reshape(B, b.op_stride)[:, :10] & ((1 << abi.YCSB_KEY_BITS) - 1)).astype(np.uint32) + 1
+    ops = np.full((B, 12), abi.YCSB_OP_PAD, dtype=np.uint32)
+    ops[:, :9] = keys[:, :9]
+    ops[:, 9] = np.uint32(0x80000000) | keys[:, 9]
+    yb = YcsbBatch(ops.ravel(), np.arange(B + 1, dtype=np.uint32), np.arange(B, dtype=np.uint64) + 7, B, 10)
+    tb = TpccGenerator(SEED, REF_TF["warehouses"], REF_TF["n_txn"], neworder_pct=0).next()
+    return keys, yb, tb
+
+
+def reference_gpu(iters):
+    """The reference's own three kernels (LTPG/YCSB/1, LTPG/TPCC-allopt-final,
+    compiled for sm_103a) on its compiled shapes, CUDA events around each
+    kernel, its per-batch clears outside the timed span."""
+    from oracle import reference
+    if not reference.available():
+        return {"unavailable": "reference cubins not built (oracle/_ref is made where the reference sources are)"}
+    keys, _, tb = ref_shape_batches()
+    out = {}
+    r = reference.RefY1()
+    flags, mark, ms = r.run(keys[:, :9], keys[:, 9], iters=iters)
+    commits = int((flags[:r.covered] & 8 != 0).sum())
+    out["ycsb_10k_x10"] = {"batch_txn": r.B, "covered_txn": r.covered, "ms_per_batch": sum(ms),
+                           "kernel_ms": ms, "commits": commits, "committed_per_s": commits / (sum(ms) * 1e-3),
+                           "theta": REF_Y1["theta"], "iters": iters}
+    t = reference.RefTF()
+    flags, ms = t.run(tb.txns, iters=iters)
+    commits = int((flags & 8 != 0).sum())
+    out["payment_65536"] = {"batch_txn": t.B, "ms_per_batch": sum(ms), "kernel_ms": ms, "commits": commits,
+                            "committed_per_s": commits / (sum(ms) * 1e-3), "iters": iters}
+    return out
+
+
+def engine_on_ref_shapes(iters):
+    """The engine on the batches reference_gpu() times, plain and graph mode,
+    the same batch in every slot, CUDA events around `iters` batches."""
+    import torch
+
+    import ltpg_gb300 as L
+    _, yb, tb = ref_shape_batches()
+    out = {}
+    for name, load, b, kw in [("ycsb_10k_x10", lambda e: e.load_ycsb(SEED, REF_Y1["n_records"]), yb,
+                               dict(max_ops_per_txn=10)),
+                              ("payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), tb,
+                               dict(max_ops_per_txn=16, max_lines=16))]:
+        n_slots = 8
+        e = L.Engine(device=0, n_slots=n_slots, max_txn=b.n_txn, **kw)
+        try:
+            load(e)
+            for s in range(n_slots):
+                e.upload(s, b)
+            res = {}
+            for mode in ["plain", "graph"]:
+                nxt = run_steps(e, n_slots, 16, mode)
+                secs, commits, launches, _ = timed(e, torch, n_slots, iters, mode, nxt, None)
+                res[mode] = {"ms_per_batch": secs * 1e3 / iters, "committed_per_s": commits / secs,
+                             "launches_per_batch": launches / iters}
+            res["commits"] = commits // iters
+            res["batch_txn"] = b.n_txn
+            out[name] = res
+        finally:
+            e.close()
+    return out
+
+
 # ---- reference arm: the protocol's CPU replay on all host threads ------------------
 def reference_arm(args, w, rank):
     if rank != 0:
@@ -439,6 +520,11 @@ def reference_arm(args, w, rank):
             "cpu_baseline": {"value": v, "unit": "txn/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t_start}
+    if not args.no_reference_gpu:
+        try:
+            line["reference_gpu"] = reference_gpu(200)
+        except Exception as exc:  # the CPU arm's line stands on its own
+            line["reference_gpu"] = {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
     print(json.dumps(line), flush=True)
 
 
@@ -522,6 +608,8 @@ def main():
                                           f"single-threaded oracle replay, {s:.1f} s"}
     if not args.no_predictor and w["kind"] == "ycsb" and w["n_txn"] >= (1 << 18):
         line["predictor"] = predictor_section(w, batches)
+    if not args.no_reference_gpu and args.workload == "ycsb_hc":
+        line["reference_shapes"] = engine_on_ref_shapes(200)
     if not args.no_serving and args.workload == "ycsb_hc":
         line["serving"] = serving_section(args)
     if args.sweep and w["kind"] == "ycsb":

@@ -56,6 +56,10 @@ extern "C" {
 #define LTPG_FLAG_WAR 0x2u
 #define LTPG_FLAG_WAW 0x4u
 #define LTPG_FLAG_COMMIT 0x8u
+/* A Payment by customer last name whose (name, nth) matched no customer: it
+ * registers nothing, does not commit and returns 0 (the reference has no such
+ * outcome; its lookup falls back to C_ID 0, TF/Genericfunction.h:37,72-74). */
+#define LTPG_FLAG_NOT_FOUND 0x10u
 
 /* ---- YCSB ----------------------------------------------------------------
  * Table: n_records rows of 10 uint64 fields, row-major (80 B per row).
@@ -117,10 +121,17 @@ typedef struct {
 #define LTPG_TPCC_MAX_LINES 15
 
 /* 32-byte transaction record.  kind_info: bits 0..7 kind, 8..15 order-line
- * count, 16..23 district, 24..31 customer district (Payment).
+ * count (NewOrder) or LTPG_PAY_* bits (Payment), 16..23 district, 24..31
+ * customer district (Payment).
  * NewOrder: a = O_ID, b = NO_ID, c = first OL_ID.   Payment: a = H_ID,
  * b/c = low/high 32 bits of the amount in cents (int64).
+ * Payment by last name (LTPG_PAY_BY_NAME): c_id holds the reference's C_LAST
+ * query word, (name << 8) | nth (TF/Query.h:176-181), and the customer is the
+ * nth (0-based) one of district (c_w, customer district) whose C_LAST column
+ * equals name, in C_ID order; it replaces the reference's KERNEL_CID /
+ * __FIND_CID_INDEX pre-phase (TF/tp.cu:11-23, TF/Genericfunction.h:29-77).
  * line_off = number of order lines of all earlier transactions of the batch. */
+#define LTPG_PAY_BY_NAME 0x100u
 typedef struct {
     uint32_t kind_info;
     uint32_t w;
@@ -153,6 +164,9 @@ typedef struct {
     uint32_t neworder_pct; /* share of NewOrder, rest Payment         */
     uint32_t remote_line_pct; /* NewOrder remote supply, per line (1)  */
     uint32_t remote_pay_pct;  /* Payment remote customer (15)          */
+    uint32_t by_name_pct;     /* Payment by last name (0; TPC-C: 60)  */
+    uint64_t table_seed;      /* seed of the loaded tables: by-name queries
+                                 name the customer a by-id Payment would pick */
 } ltpg_tpcc_params;
 
 /* ---- engine context ---------------------------------------------------- */
@@ -171,6 +185,12 @@ typedef struct {
  * WAR check (TF/Execute_neworder.h:115,639-646); that is the default here.
  * With this flag the insert registers and checks as a write. */
 #define LTPG_CFG_STRICT_INSERT 0x1u
+/* By-name Payments resolve the customer with the reference's own arithmetic
+ * (TF/Genericfunction.h:29-77 as its lane 0 computes it: that lane tests
+ * every 32nd customer, counts each match 32 times, then walks back from the
+ * end of its last block of 32, skipping position 0; no match gives C_ID 0)
+ * instead of the nth-customer rule.  For parity with the reference only. */
+#define LTPG_CFG_REF_NAME_LOOKUP 0x2u
 
 typedef struct {
     uint64_t n_txn;

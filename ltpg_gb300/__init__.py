@@ -174,8 +174,12 @@ class YcsbGenerator:
 class TpccGenerator:
     """Deterministic, stateful TPC-C NewOrder/Payment batches (draw in order)."""
 
-    def __init__(self, seed, warehouses, n_txn, neworder_pct=50, remote_line_pct=1, remote_pay_pct=15):
-        self.params = abi.TpccParamsC(seed, warehouses, n_txn, neworder_pct, remote_line_pct, remote_pay_pct)
+    def __init__(self, seed, warehouses, n_txn, neworder_pct=50, remote_line_pct=1, remote_pay_pct=15,
+                 by_name_pct=0, table_seed=None):
+        """by_name_pct: share of Payments that name their customer by last name;
+        table_seed: seed the tables were loaded with (default: seed)."""
+        self.params = abi.TpccParamsC(seed, warehouses, n_txn, neworder_pct, remote_line_pct, remote_pay_pct,
+                                      by_name_pct, seed if table_seed is None else table_seed)
         h = C.c_void_p()
         _check(lib().ltpg_gen_create_tpcc(C.byref(self.params), C.byref(h)))
         self._h = h
@@ -202,9 +206,10 @@ class Engine:
     """One GPU context: tables, batch slots, phases, results."""
 
     def __init__(self, device=0, n_slots=2, max_txn=1 << 16, max_ops_per_txn=16, max_lines=0,
-                 strict_insert=False):
+                 strict_insert=False, ref_name_lookup=False):
         cfg = abi.ConfigC(device, n_slots, max_txn, max_ops_per_txn, max_lines,
-                          abi.CFG_STRICT_INSERT if strict_insert else 0)
+                          (abi.CFG_STRICT_INSERT if strict_insert else 0) |
+                          (abi.CFG_REF_NAME_LOOKUP if ref_name_lookup else 0))
         h = C.c_void_p()
         code = lib().ltpg_create(C.byref(cfg), C.byref(h))
         if code != abi.OK:
@@ -407,7 +412,8 @@ def serve(tpcc_engine, ycsb_engine, rate, duration_s, tpcc_params, ycsb_params, 
                         MODES[mode] if isinstance(mode, str) else mode, slots)
     tp = abi.TpccParamsC(tpcc_params["seed"], tpcc_params["warehouses"], tpcc_params.get("n_txn", 262144),
                          tpcc_params.get("neworder_pct", 50), tpcc_params.get("remote_line_pct", 1),
-                         tpcc_params.get("remote_pay_pct", 15))
+                         tpcc_params.get("remote_pay_pct", 15), tpcc_params.get("by_name_pct", 0),
+                         tpcc_params.get("table_seed", tpcc_params["seed"]))
     yp = abi.YcsbParamsC(ycsb_params["seed"], ycsb_params["n_records"], ycsb_params.get("n_txn", 262144),
                          ycsb_params.get("ops_per_txn", 10), ycsb_params.get("update_pct", 50),
                          ycsb_params.get("rotate_every", 0), ycsb_params.get("theta", 0.9))

@@ -6,7 +6,8 @@ ERR_INVALID, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_TIMEOUT, ERR_BOUNDS = 1, 2, 3, 
 WORKLOAD_YCSB, WORKLOAD_TPCC = 1, 2
 MODE_PLAIN, MODE_FUSED, MODE_PERSISTENT, MODE_GRAPH = 0, 1, 2, 3
 MODES = {"plain": MODE_PLAIN, "fused": MODE_FUSED, "persistent": MODE_PERSISTENT, "graph": MODE_GRAPH}
-FLAG_RAW, FLAG_WAR, FLAG_WAW, FLAG_COMMIT = 1, 2, 4, 8
+FLAG_RAW, FLAG_WAR, FLAG_WAW, FLAG_COMMIT, FLAG_NOT_FOUND = 1, 2, 4, 8, 16
+PAY_BY_NAME = 0x100
 YCSB_FIELDS = 10
 YCSB_OP_PAD = 0xFFFFFFFF
 YCSB_KEY_BITS = 27
@@ -18,6 +19,7 @@ TPCC_COLS = (9, 11, 21, 8, 3, 8, 10, 17, 5)
 TPCC_NEWORDER, TPCC_PAYMENT = 0, 1
 TPCC_MAX_LINES = 15
 CFG_STRICT_INSERT = 1
+CFG_REF_NAME_LOOKUP = 2
 NOALLOC_MAX_RECORDS = 1 << 20
 STAGE_BUCKETS = 65536
 STAGE_ENTRIES = 1024
@@ -42,7 +44,8 @@ class TpccBatchC(C.Structure):
 
 class TpccParamsC(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("warehouses", C.c_uint32), ("n_txn", C.c_uint32),
-                ("neworder_pct", C.c_uint32), ("remote_line_pct", C.c_uint32), ("remote_pay_pct", C.c_uint32)]
+                ("neworder_pct", C.c_uint32), ("remote_line_pct", C.c_uint32), ("remote_pay_pct", C.c_uint32),
+                ("by_name_pct", C.c_uint32), ("table_seed", C.c_uint64)]
 
 
 class ConfigC(C.Structure):

@@ -167,6 +167,7 @@ int ltpg_destroy(ltpg_ctx *c) {
     dev_free(c->ycsb.reg);
     for (auto &t : c->tpcc.tab) dev_free(t);
     dev_free(c->tpcc.reg);
+    dev_free(c->tpcc.name_idx);
     dev_free(c->stage_map);
     dev_free(c->stage_bits);
     dev_free(c->stage_rank);
@@ -227,6 +228,7 @@ int ltpg_db_load_tpcc(ltpg_ctx *c, uint64_t seed, uint32_t W) {
     drop_graphs(c);
     for (auto &t : c->tpcc.tab) dev_free(t);
     dev_free(c->tpcc.reg);
+    dev_free(c->tpcc.name_idx);
     c->tpcc = TpccDb{};
     uint64_t total = 0;
     for (uint32_t t = 0; t < LTPG_TPCC_TABLES; ++t) {
@@ -237,10 +239,12 @@ int ltpg_db_load_tpcc(ltpg_ctx *c, uint64_t seed, uint32_t W) {
     }
     if (total >= (1ull << 32)) return fail(c, LTPG_ERR_INVALID, "too many rows for 32-bit slots");
     CK(dev_alloc(&c->tpcc.reg, total), "alloc TPC-C registration table");
+    CK(dev_alloc(&c->tpcc.name_idx, c->tpcc.rows[LTPG_T_CUSTOMER]), "alloc customer name index");
     c->tpcc.n_slots = total;
     c->tpcc.W = W;
     c->tpcc_seed = seed;
     CK(tpcc_init_tables(c), "init TPC-C tables");
+    CK(tpcc_build_name_index(c), "build customer name index");
     return ltpg_sync(c);
 }
 
@@ -286,6 +290,7 @@ int ltpg_db_upload(ltpg_ctx *c, uint32_t table, const void *host, size_t bytes) 
     if (r) return r;
     if (bytes != n * 8) return fail(c, LTPG_ERR_INVALID, "image size mismatch");
     CK(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, c->stream), "upload table");
+    if (table == LTPG_T_CUSTOMER) CK(tpcc_build_name_index(c), "build customer name index");
     return ltpg_sync(c);
 }
 

@@ -54,6 +54,9 @@ struct TpccDb {
     uint64_t n_slots = 0;
     RegSlot *reg = nullptr;  // flat over all tables
     uint64_t base[LTPG_TPCC_TABLES] = {};
+    // Customer last-name index: per district its 3,000 keys
+    // (min(C_LAST, 2^32 - 1) << 32 | C_ID) in ascending order.
+    uint64_t *name_idx = nullptr;
 };
 
 // One device batch slot.
@@ -153,6 +156,7 @@ cudaError_t ycsb_init_table(ltpg_ctx *c);
 cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase);      // 0 exec, 1 check, 2 write-back
 cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode);   // fused / persistent
 cudaError_t tpcc_init_tables(ltpg_ctx *c);
+cudaError_t tpcc_build_name_index(ltpg_ctx *c);
 cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase);
 cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode);
 }  // namespace ltpg

@@ -115,6 +115,10 @@ struct ltpg_gen {
     Zipf zipf;
     // TPC-C per-warehouse counters (TF/Query.h:54-88,157-166).
     std::vector<uint32_t> o_id, no_id, ol_id, h_id;
+    // By-name Payments: C_LAST of every customer of the loaded image and its
+    // rank among the customers of its district with that name, in C_ID order.
+    std::vector<uint16_t> cust_name;
+    std::vector<uint8_t> cust_rank;
     uint64_t next_batch = 0, txn_base = 0;
 };
 
@@ -141,7 +145,8 @@ int ltpg_gen_create_ycsb(const ltpg_ycsb_params *p, ltpg_gen **out) {
 int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out) {
     if (!p || !out) return LTPG_ERR_INVALID;
     if (p->warehouses == 0 || p->warehouses > 65535 || p->n_txn == 0) return LTPG_ERR_INVALID;
-    if (p->neworder_pct > 100 || p->remote_line_pct > 100 || p->remote_pay_pct > 100) return LTPG_ERR_INVALID;
+    if (p->neworder_pct > 100 || p->remote_line_pct > 100 || p->remote_pay_pct > 100 || p->by_name_pct > 100)
+        return LTPG_ERR_INVALID;
     ltpg_gen *g = new (std::nothrow) ltpg_gen();
     if (!g) return LTPG_ERR_NOMEM;
     g->kind = LTPG_WORKLOAD_TPCC;
@@ -150,6 +155,21 @@ int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out) {
     g->no_id.assign(p->warehouses, 0);
     g->ol_id.assign(p->warehouses, 0);
     g->h_id.assign(p->warehouses, 0);
+    if (p->by_name_pct) {
+        // names of the initial image (tpcc_init_value: C_LAST < 1000)
+        const uint64_t n = 30000ull * p->warehouses;
+        g->cust_name.resize(n);
+        g->cust_rank.resize(n);
+        std::vector<uint16_t> seen(1000);
+        for (uint64_t d0 = 0; d0 < n; d0 += 3000) {
+            std::fill(seen.begin(), seen.end(), 0);
+            for (uint64_t row = d0; row < d0 + 3000; ++row) {
+                const uint32_t name = (uint32_t)tpcc_init_value(p->table_seed, LTPG_T_CUSTOMER, row, C_LAST);
+                g->cust_name[row] = (uint16_t)name;
+                g->cust_rank[row] = (uint8_t)std::min<uint32_t>(seen[name]++, 255u);
+            }
+        }
+    }
     *out = g;
     return LTPG_OK;
 }
@@ -310,6 +330,15 @@ int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
             g->h_id[w] = (g->h_id[w] + 1) % 30000u;
             x.b = (uint32_t)amount;
             x.c = (uint32_t)(amount >> 32);
+            // by last name (TF/Query.h:174-181): the query names the customer
+            // drawn above by its C_LAST and its rank among that name's holders
+            if (p.by_name_pct && r.below(100) < p.by_name_pct) {
+                const uint64_t row = 30000ull * c_w + 3000ull * c_d + x.c_id;
+                if (g->cust_rank[row] < 255u) {
+                    x.kind_info |= LTPG_PAY_BY_NAME;
+                    x.c_id = ((uint32_t)g->cust_name[row] << 8) | g->cust_rank[row];
+                }
+            }
         }
     }
     out->n_txn = p.n_txn;

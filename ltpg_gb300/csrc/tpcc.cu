@@ -20,8 +20,10 @@ struct TpccDev {
     uint64_t *tab[LTPG_TPCC_TABLES];
     uint64_t rows[LTPG_TPCC_TABLES];
     uint64_t base[LTPG_TPCC_TABLES];
+    const uint64_t *name_idx;
     uint32_t W;
     uint32_t strict;
+    uint32_t ref_names;
 };
 
 static TpccDev make_dev(ltpg_ctx *c) {
@@ -31,8 +33,10 @@ static TpccDev make_dev(ltpg_ctx *c) {
         d.rows[t] = c->tpcc.rows[t];
         d.base[t] = c->tpcc.base[t];
     }
+    d.name_idx = c->tpcc.name_idx;
     d.W = c->tpcc.W;
     d.strict = (c->cfg.flags & LTPG_CFG_STRICT_INSERT) ? 1u : 0u;
+    d.ref_names = (c->cfg.flags & LTPG_CFG_REF_NAME_LOOKUP) ? 1u : 0u;
     return d;
 }
 
@@ -79,6 +83,129 @@ cudaError_t tpcc_init_tables(ltpg_ctx *c) {
     return cudaMemsetAsync(c->tpcc.reg, 0xFF, c->tpcc.n_slots * sizeof(RegSlot), c->stream);
 }
 
+// ---- customer last-name index (replaces INDEX.customer_name_index and its
+// 3,000-entry warp scan, TF/Datastructure.h:131-134, TF/Genericfunction.h:29-77)
+// One block per district sorts the district's keys (C_LAST << 32 | C_ID) in
+// shared memory (bitonic, 4,096 slots); a lookup is then a binary search in a
+// 24 KB run that stays in L2.
+constexpr uint32_t NAME_SORT = 4096;
+
+__global__ void __launch_bounds__(1024) tpcc_name_index_kernel(const uint64_t *__restrict__ cust,
+                                                               uint64_t *__restrict__ idx) {
+    __shared__ unsigned long long k[NAME_SORT];
+    const uint64_t r0 = (uint64_t)blockIdx.x * 3000u;
+    for (uint32_t i = threadIdx.x; i < NAME_SORT; i += blockDim.x) {
+        unsigned long long v = ~0ull;
+        if (i < 3000u) {
+            const uint64_t name = cust[(r0 + i) * tpcc_cols(LTPG_T_CUSTOMER) + C_LAST];
+            v = ((name < 0xFFFFFFFFull ? name : 0xFFFFFFFFull) << 32) | i;
+        }
+        k[i] = v;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= NAME_SORT; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = threadIdx.x; i < NAME_SORT; i += blockDim.x) {
+                const uint32_t j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0u;
+                    const unsigned long long a = k[i], b = k[j];
+                    if ((a > b) == up) {
+                        k[i] = b;
+                        k[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t i = threadIdx.x; i < 3000u; i += blockDim.x) idx[r0 + i] = k[i];
+}
+
+cudaError_t tpcc_build_name_index(ltpg_ctx *c) {
+    if (!c->tpcc.W || !c->tpcc.name_idx) return cudaSuccess;
+    tpcc_name_index_kernel<<<c->tpcc.W * 10u, 1024, 0, c->stream>>>(c->tpcc.tab[LTPG_T_CUSTOMER], c->tpcc.name_idx);
+    return cudaGetLastError();
+}
+
+// The nth (0-based) customer of district (w, d) whose C_LAST is name, in C_ID
+// order: the first index key >= name << 32, then nth further.
+__device__ __forceinline__ bool name_lookup(const TpccDev &db, uint32_t w, uint32_t d, uint32_t name, uint32_t nth,
+                                            uint32_t &cid) {
+    const uint64_t *k = db.name_idx + (10ull * w + d) * 3000u;
+    const uint64_t target = (uint64_t)name << 32;
+    uint32_t lo = 0, hi = 3000u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(k + mid) < target) lo = mid + 1u;
+        else hi = mid;
+    }
+    const uint32_t p = lo + nth;
+    if (p >= 3000u) return false;
+    const uint64_t v = __ldg(k + p);
+    if ((v >> 32) != name) return false;
+    cid = (uint32_t)v;
+    return true;
+}
+
+// The reference's __FIND_CID_INDEX (TF/Genericfunction.h:29-77) as its lane 0
+// computes it: the lane's shuffle reads its own match flag 32 times, so it
+// tests customers 0, 32, 64, ... and counts each match 32 times until the
+// count reaches nth; it then walks back from the end of its last block of 32
+// (down to position 1) over customers with that name, counting down to nth,
+// and returns the C_ID column of the row it stops at; otherwise C_ID 0.
+// Positions past the district read the next district's rows, as the
+// reference's index does; past the table they match nothing.
+__device__ __forceinline__ uint32_t ref_name_lookup(const TpccDev &db, uint32_t w, uint32_t d, uint32_t name,
+                                                    uint32_t nth) {
+    const uint64_t dist = 30000ull * w + 3000ull * d, rows = db.rows[LTPG_T_CUSTOMER];
+    auto name_at = [&](uint64_t row) {
+        return row < rows && ld_col(db, LTPG_T_CUSTOMER, row, C_LAST) == (uint64_t)name;
+    };
+    uint32_t cum = 0, flag = 0;
+    for (uint32_t i = 0; i < 3000u; i += 32u) {
+        cum += name_at(dist + i) ? 32u : 0u;
+        flag += 32u;
+        if (cum >= nth) break;
+    }
+    if (cum < nth) return 0u;
+    uint64_t result = 0;
+    for (uint32_t i = flag - 1u; i > 0u; --i) {
+        if (!name_at(dist + i)) continue;
+        if (cum == nth) {
+            result = dist + i;
+            break;
+        }
+        --cum;
+    }
+    return (uint32_t)ld_col(db, LTPG_T_CUSTOMER, result, C_ID);
+}
+
+// Marks a by-name Payment whose customer was not found (kept in the
+// shared-memory copy of the record only; a Payment's bits 8..15 are flags,
+// a NewOrder's its line count).
+constexpr uint32_t KI_NOT_FOUND = 0x200u;
+__device__ __forceinline__ bool txn_not_found(const ltpg_tpcc_txn &x) {
+    return tpcc_kind(x.kind_info) == LTPG_TPCC_PAYMENT && (x.kind_info & KI_NOT_FOUND);
+}
+
+// Resolves a by-name Payment in place: c_id becomes the customer's C_ID.
+// Returns false when the customer is not found; out-of-range fields are left
+// for txn_valid to reject.
+__device__ __forceinline__ bool resolve_by_name(const TpccDev &db, ltpg_tpcc_txn &x) {
+    if (tpcc_kind(x.kind_info) != LTPG_TPCC_PAYMENT || !(x.kind_info & LTPG_PAY_BY_NAME)) return true;
+    const uint32_t c_d = tpcc_c_d(x.kind_info);
+    if (x.c_w >= db.W || c_d >= 10u) return true;
+    const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
+    if (db.ref_names) {
+        x.c_id = ref_name_lookup(db, x.c_w, c_d, name, nth);
+        return true;
+    }
+    uint32_t cid;
+    if (!name_lookup(db, x.c_w, c_d, name, nth, cid)) return false;
+    x.c_id = cid;
+    return true;
+}
+
 constexpr uint32_t PT = 64;    // transactions per tile (plain path)
 constexpr uint32_t PBS = 256;  // threads per block (plain path)
 
@@ -99,9 +226,11 @@ __device__ __forceinline__ uint32_t load_tile(TileHdr &h, const ltpg_tpcc_txn *_
         ltpg_tpcc_txn x;
         x.kind_info = a.x; x.w = a.y; x.c_w = a.z; x.c_id = a.w;
         x.a = b.x; x.b = b.y; x.c = b.z; x.line_off = b.w;
+        const bool found = resolve_by_name(db, x);
+        if (!found) x.kind_info |= KI_NOT_FOUND;
         h.x[threadIdx.x] = x;
-        const bool ok = txn_valid(x, db.W, n_lines);
-        if (!ok) report_error(ctl, DERR_BOUNDS, t0 + threadIdx.x);
+        const bool ok = found && txn_valid(x, db.W, n_lines);
+        if (!ok && found) report_error(ctl, DERR_BOUNDS, t0 + threadIdx.x);
         h.ok[threadIdx.x] = ok;
     }
     __syncthreads();
@@ -231,6 +360,7 @@ __global__ void __launch_bounds__(PBS) tpcc_check_plain(const ltpg_tpcc_txn *__r
     if (threadIdx.x < nt) {
         uint32_t f = fl[threadIdx.x];
         if (h.ok[threadIdx.x] && commits(f)) f |= LTPG_FLAG_COMMIT;
+        if (txn_not_found(h.x[threadIdx.x])) f |= LTPG_FLAG_NOT_FOUND;
         flags[t0 + threadIdx.x] = (uint8_t)f;
     }
 }
@@ -508,6 +638,7 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
             uint32_t f = threadIdx.x < nt ? fl[threadIdx.x] : 0u;
             const bool com = threadIdx.x < nt && h.ok[threadIdx.x] && commits(f);
             if (com) f |= LTPG_FLAG_COMMIT;
+            if (threadIdx.x < nt && txn_not_found(h.x[threadIdx.x])) f |= LTPG_FLAG_NOT_FOUND;
             if (threadIdx.x < nt) {
                 a.flags[t0 + threadIdx.x] = (uint8_t)f;
                 fl[threadIdx.x] = f;

@@ -37,6 +37,7 @@ struct YcsbTunedArgs {
     uint32_t *bucket_counts;
     uint32_t ways, stage_entries;
     uint32_t filter;
+    uint32_t lpt;  // lanes per transaction of the one-op-per-lane kernels: stride rounded up to a power of two (0: > 32)
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
@@ -374,8 +375,9 @@ __global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t 
 }
 
 // ---- cooperative execute+register: one op per lane, rows read by 5 lanes ----
-// A warp takes 32 consecutive op words (whole transactions, the stride being a
-// power of two <= 32).  Each lane registers its own op; then the rows of the
+// A warp takes whole transactions, lpt lanes each (the stride rounded up to a
+// power of two <= 32; lanes past the stride hold padding ops).  Each lane
+// registers its own op; then the rows of the
 // warp's reads are fetched six at a time, five lanes per row, each lane one
 // contiguous 16-byte chunk, so a row costs one or two cache-line requests
 // instead of five.  The five chunks are xor-folded within their lane group and
@@ -385,17 +387,18 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
                                                const uint32_t *srank, uint64_t tag) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lanes_below = (1u << lane) - 1u;
-    const uint32_t lpt = a.stride;  // lanes per transaction
+    const uint32_t lpt = a.lpt;  // lanes per transaction, a power of two
+    const uint32_t lsh = (uint32_t)__ffs(lpt) - 1u;
     const uint32_t groups = a.ways ? a.stage_entries / a.ways : 0u;
-    const uint64_t nw = (uint64_t)a.B * a.stride;
+    const uint64_t nw = (uint64_t)a.B << lsh;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     const uint32_t grp = lane / 5, chunk = lane % 5;  // row-read lane groups (6 x 5 lanes)
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
         const uint64_t v = base + threadIdx.x;
         const bool act = v < nw;
-        const uint32_t w = act ? __ldg(a.ops + v) : LTPG_YCSB_OP_PAD;
-        const uint32_t t = (uint32_t)(v / lpt);
-        const uint32_t j = (uint32_t)(v % lpt);
+        const uint32_t t = (uint32_t)(v >> lsh);
+        const uint32_t j = (uint32_t)v & (lpt - 1u);
+        const uint32_t w = act && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
         bool valid = act && !ycsb_is_pad(w);
         const uint32_t key = ycsb_key(w);
         if (valid && key >= a.n) {
@@ -561,7 +564,7 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         stage_init(p.tab, a.stage_entries);
         __syncthreads();
     }
-    if (a.stride <= 32 && (a.stride & (a.stride - 1)) == 0) {
+    if (a.lpt) {
         if (a.filter) coop_exec_loop<kStage, true, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
         else coop_exec_loop<kStage, false, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
     } else {
@@ -632,19 +635,19 @@ static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
     if (per_sm < 1) per_sm = 1;
     if (L.blocks_per_sm && (int)L.blocks_per_sm < per_sm) per_sm = (int)L.blocks_per_sm;
-    const uint64_t nw = (uint64_t)a.B * a.stride;
+    const uint64_t nw = (uint64_t)a.B * a.lpt;
     const uint32_t grid = (uint32_t)std::min<uint64_t>((nw + 255) / 256, (uint64_t)per_sm * c->sm_count);
     k<<<grid, 256, smem, c->stream>>>(a);
 }
 
 // Launch shapes of the execute phase, by ops_per_thread: 1 = cooperative row
-// reads (ycsb_exec_coop), 2 / 4 = per-thread row reads (ycsb_exec_fast);
-// 8 = block tiles (ycsb_exec_tuned), which also serve strides that are not a
-// power of two.
+// reads (ycsb_exec_coop, any stride <= 32), 2 / 4 = per-thread row reads
+// (ycsb_exec_fast, stride / ops a power of two); 8 = block tiles
+// (ycsb_exec_tuned), which serve every stride.
 static bool launch_fast_exec(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
     const uint32_t opt = c->launch_y.per_thread ? c->launch_y.per_thread : 4u;
     if (opt >= 8) return false;
-    if (opt == 1 && a.stride <= 32 && (a.stride & (a.stride - 1)) == 0) {
+    if (opt == 1 && a.lpt) {
         launch_coop(c, a, stage);
         return true;
     }
@@ -670,6 +673,11 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.B = s.n_txn;
     a.k = s.k;
     a.stride = s.stride;
+    a.lpt = 0;
+    if (s.stride <= 32) {
+        a.lpt = 1;
+        while (a.lpt < s.stride) a.lpt <<= 1;
+    }
     a.tile = tuned_tile(s.stride, threads, per_thread);
     a.rows = c->ycsb.rows;
     a.n = c->ycsb.n;

@@ -52,6 +52,8 @@ def lib():
         _lib.oracle_tpcc_slots.restype = U64
         _lib.oracle_tpcc_slots.argtypes = [U32]
         _lib.oracle_tpcc_init_table.argtypes = [P, U32, U32, U64]
+        _lib.oracle_tpcc_resolve.restype = None
+        _lib.oracle_tpcc_resolve.argtypes = [C.POINTER(P), U32, C.POINTER(abi.TpccBatchC), C.c_int, P, P]
         _lib.oracle_tpcc_batch.restype = I64
         _lib.oracle_tpcc_batch.argtypes = [C.POINTER(P), U32, C.POINTER(abi.TpccBatchC), C.c_int, P, P, P, P, P]
     return _lib
@@ -102,9 +104,10 @@ class YcsbOracle:
 class TpccOracle:
     """Single-threaded replay over host copies of the nine TPC-C tables."""
 
-    def __init__(self, seed, warehouses, strict=False):
+    def __init__(self, seed, warehouses, strict=False, ref_name_lookup=False):
         self.W = int(warehouses)
-        self.strict = int(bool(strict))
+        # LTPG_CFG_* word: strict NEW-ORDER insert, reference by-name arithmetic
+        self.strict = (abi.CFG_STRICT_INSERT if strict else 0) | (abi.CFG_REF_NAME_LOOKUP if ref_name_lookup else 0)
         L = lib()
         self.tables = []
         for t in range(abi.TPCC_TABLES):
@@ -115,6 +118,14 @@ class TpccOracle:
         nslots = L.oracle_tpcc_slots(self.W)
         self.reg_r = np.empty(nslots, dtype=np.uint32)
         self.reg_w = np.empty(nslots, dtype=np.uint32)
+
+    def resolve(self, batch):
+        """(customer C_ID per transaction after by-name resolution, found flags)."""
+        cid = np.zeros(batch.n_txn, dtype=np.uint32)
+        found = np.zeros(batch.n_txn, dtype=np.uint8)
+        cb = batch.as_c()
+        lib().oracle_tpcc_resolve(self._ptrs, self.W, C.byref(cb), self.strict, _p(cid), _p(found))
+        return cid, found.astype(bool)
 
     def run(self, batch):
         B = batch.n_txn

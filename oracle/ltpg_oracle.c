@@ -380,6 +380,62 @@ static inline uint64_t *colp(uint64_t **tab, uint32_t table, uint64_t row, uint3
 }
 
 /*
+ * Payment by customer last name (LTPG_PAY_BY_NAME): c_id holds the query word
+ * (name << 8) | nth of the reference's PAYMENT_QUERY.C_LAST (TF/Query.h:176-181).
+ * Default rule: the nth (0-based) customer of the district whose C_LAST column
+ * equals name, in C_ID order — a linear scan here (the engine uses a sorted
+ * per-district index).  Returns 0 when there is no such customer.
+ */
+static int name_lookup(uint64_t **tab, uint32_t w, uint32_t d, uint32_t name, uint32_t nth, uint32_t *cid) {
+    const uint64_t dist = 30000ull * w + 3000ull * d;
+    uint32_t seen = 0;
+    for (uint32_t c = 0; c < 3000; ++c) {
+        if (*colp(tab, LTPG_T_CUSTOMER, dist + c, 13) != (uint64_t)name) continue;
+        if (seen++ == nth) {
+            *cid = c;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+/*
+ * LTPG_CFG_REF_NAME_LOOKUP: __FIND_CID_INDEX (TF/Genericfunction.h:29-77) as
+ * lane 0 of its warp computes it.  Its shuffle `__shfl_sync(.., tmp, i)` takes
+ * the loop index as source lane, i.e. the lane itself (i = lane + 32k), so
+ * count = 32 * tmp: lane 0 tests positions 0, 32, 64, ... (:42-52), adding 32
+ * per match, and stops once the sum reaches nth (:53-56, flag = 32 per
+ * iteration).  Only lane 0 finishes (:59): walking back from flag - 1 down to 1
+ * over positions holding name, it stops where the sum equals nth and
+ * decrements it otherwise (:61-71); C_ID is column 0 of that row (:72), or 0
+ * if the walk found nothing or the sum never reached nth (:37).  Positions past
+ * the district read the next district, as the reference's flat index does;
+ * past the table nothing matches (the reference reads past its array there).
+ */
+static uint32_t ref_name_lookup(uint64_t **tab, uint32_t W, uint32_t w, uint32_t d, uint32_t name, uint32_t nth) {
+    const uint64_t dist = 30000ull * w + 3000ull * d, rows = 30000ull * W;
+#define NAME_AT(row) ((row) < rows && *colp(tab, LTPG_T_CUSTOMER, (row), 13) == (uint64_t)name)
+    uint32_t cum = 0, flag = 0;
+    for (uint32_t i = 0; i < 3000; i += 32) {
+        cum += NAME_AT(dist + i) ? 32u : 0u;
+        flag += 32;
+        if (cum >= nth) break;
+    }
+    if (cum < nth) return 0;
+    uint64_t result = 0;
+    for (uint32_t i = flag - 1; i > 0; --i) {
+        if (!NAME_AT(dist + i)) continue;
+        if (cum == nth) {
+            result = dist + i;
+            break;
+        }
+        --cum;
+    }
+#undef NAME_AT
+    return (uint32_t)*colp(tab, LTPG_T_CUSTOMER, result, 0);
+}
+
+/*
  * One TPC-C batch, single-threaded.  tab[9]: the nine tables (updated in
  * place).  reg_r / reg_w: scratch indexed by (table, row), sized by
  * oracle_tpcc_slots(W).  Returns the commit count or -1 for an invalid batch.
@@ -390,8 +446,61 @@ uint64_t oracle_tpcc_slots(uint32_t W) {
     return s;
 }
 
-int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int strict, uint32_t *reg_r,
+static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, const uint8_t *nf,
+                                   int strict, uint32_t *reg_r, uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap,
+                                   int64_t *results);
+
+/* The customer of every transaction after by-name resolution: cid[t] (the
+ * record's c_id when it is not a by-name Payment) and found[t]. */
+void oracle_tpcc_resolve(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int cfg_flags, uint32_t *cid,
+                         uint8_t *found) {
+    for (uint32_t t = 0; t < b->n_txn; ++t) {
+        const ltpg_tpcc_txn *x = &b->txns[t];
+        const uint32_t c_d = k_cd(x->kind_info);
+        cid[t] = x->c_id;
+        found[t] = 1;
+        if (k_kind(x->kind_info) == LTPG_TPCC_PAYMENT && (x->kind_info & LTPG_PAY_BY_NAME) && x->c_w < W && c_d < 10) {
+            const uint32_t name = x->c_id >> 8, nth = x->c_id & 0xFFu;
+            if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) cid[t] = ref_name_lookup(tab, W, x->c_w, c_d, name, nth);
+            else found[t] = (uint8_t)name_lookup(tab, x->c_w, c_d, name, nth, &cid[t]);
+        }
+    }
+}
+
+int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int cfg_flags, uint32_t *reg_r,
                           uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap, int64_t *results) {
+    /* resolve by-name Payments first (the reference's KERNEL_CID pre-phase,
+       TF/tp.cu:11-23), into a copy of the records */
+    const uint32_t B = b->n_txn;
+    ltpg_tpcc_txn *rx = (ltpg_tpcc_txn *)malloc((size_t)(B ? B : 1) * sizeof *rx);
+    uint8_t *nf = (uint8_t *)calloc(B ? B : 1, 1);
+    if (!rx || !nf) {
+        free(rx);
+        free(nf);
+        return -1;
+    }
+    for (uint32_t t = 0; t < B; ++t) {
+        ltpg_tpcc_txn x = b->txns[t];
+        const uint32_t c_d = k_cd(x.kind_info);
+        if (k_kind(x.kind_info) == LTPG_TPCC_PAYMENT && (x.kind_info & LTPG_PAY_BY_NAME) && x.c_w < W && c_d < 10) {
+            const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
+            if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) x.c_id = ref_name_lookup(tab, W, x.c_w, c_d, name, nth);
+            else if (!name_lookup(tab, x.c_w, c_d, name, nth, &x.c_id)) nf[t] = 1;
+        }
+        rx[t] = x;
+    }
+    ltpg_tpcc_batch rb = *b;
+    rb.txns = rx;
+    const int64_t r = tpcc_batch_resolved(tab, W, &rb, nf, cfg_flags & LTPG_CFG_STRICT_INSERT, reg_r, reg_w, flags,
+                                          bitmap, results);
+    free(rx);
+    free(nf);
+    return r;
+}
+
+static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, const uint8_t *nf,
+                                   int strict, uint32_t *reg_r, uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap,
+                                   int64_t *results) {
     uint64_t base[LTPG_TPCC_TABLES], acc = 0;
     for (uint32_t t = 0; t < LTPG_TPCC_TABLES; ++t) {
         base[t] = acc;
@@ -401,6 +510,7 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
     const uint32_t B = b->n_txn;
     /* validate and clear the touched slots */
     for (uint32_t t = 0; t < B; ++t) {
+        if (nf[t]) continue;
         const int m = txn_ops(&b->txns[t], b->lines, b->n_lines, W, strict, ops);
         if (m < 0) return -1;
         for (int j = 0; j < m; ++j) reg_r[base[ops[j].table] + ops[j].row] = reg_w[base[ops[j].table] + ops[j].row] = NONE;
@@ -408,6 +518,10 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
     /* phase 1: register + reads of the execute phase */
     for (uint32_t t = 0; t < B; ++t) {
         const ltpg_tpcc_txn *x = &b->txns[t];
+        if (nf[t]) {
+            results[t] = 0;
+            continue;
+        }
         const int m = txn_ops(x, b->lines, b->n_lines, W, strict, ops);
         for (int j = 0; j < m; ++j) {
             const uint64_t s = base[ops[j].table] + ops[j].row;
@@ -434,6 +548,10 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
     int64_t commits = 0;
     memset(bitmap, 0, ((size_t)B + 31) / 32 * 4);
     for (uint32_t t = 0; t < B; ++t) {
+        if (nf[t]) {
+            flags[t] = LTPG_FLAG_NOT_FOUND;
+            continue;
+        }
         const int m = txn_ops(&b->txns[t], b->lines, b->n_lines, W, strict, ops);
         uint32_t f = 0;
         for (int j = 0; j < m; ++j) {

@@ -64,9 +64,13 @@ int main() {
          OFF(PAYMENT_QUERY, C_LAST), OFF(PAYMENT_QUERY, isName), OFF(PAYMENT_QUERY, C_D_ID),
          OFF(PAYMENT_QUERY, C_W_ID), OFF(PAYMENT_QUERY, H_AMOUNT), OFF(PAYMENT_QUERY, H_ID), OFF(PAYMENT_QUERY, TID));
   printf("\"log\": {\"size\": %zu, \"w_ytd\": %zu},", sizeof(LOG), OFF(LOG, W_YTD));
+  printf("\"customer_size\": %llu, \"cust_snapshot\": %zu, \"name_index\": %zu,", CUSTOMER_SIZE,
+         OFF(SNAPSHOT, customer_snapshot), OFF(INDEX, customer_name_index));
+  printf("\"cid_grid\": %u, \"cid_block\": %u,", GRID_SIZE, BLOCK_SIZE);
   printf("\"snapshot\": %zu, \"index\": %zu}\n", sizeof(SNAPSHOT), sizeof(INDEX));
 }
-''', kernels=["_Z14KERNEL_EXECUTEP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
+''', cid_kernel="_Z10KERNEL_CIDP11PAYMENT_SETP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
+        kernels=["_Z14KERNEL_EXECUTEP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
               "_Z12KERNEL_CHECKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
               "_Z16KERNEL_WRITEBACKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX"]),
 }
@@ -88,7 +92,8 @@ def build(force=False):
         if force or not os.path.exists(cubin):
             subprocess.run([NVCC, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
                             "-w", "-o", cubin, os.path.join(src_dir, p["main"])], check=True, capture_output=True)
-        if force or not os.path.exists(layout):
+        stale = os.path.exists(layout) and "cid_kernel" in p and "cid_grid" not in json.load(open(layout))
+        if force or stale or not os.path.exists(layout):
             cpp = os.path.join(OUT, f"{name}_layout.cpp")
             exe = os.path.join(OUT, f"{name}_layout")
             with open(cpp, "w") as f:
@@ -98,6 +103,8 @@ def build(force=False):
             out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
             data = json.loads(out)
             data["kernels"] = p["kernels"]
+            if "cid_kernel" in p:
+                data["cid_kernel"] = p["cid_kernel"]
             with open(layout, "w") as f:
                 json.dump(data, f, indent=1)
             os.remove(exe)

@@ -7,7 +7,8 @@ oracle/ref_build.py (oracle/_ref/) and runs them through ref_harness.cu:
          key 0 around registration (Y1/Genericfunction.h:163-187), so batches
          for it use keys 1 .. N-1.
   RefTF  LTPG/TPCC-allopt-final as shipped: 65,536 Payments (NEWORDER_PERCENT
-         = 0), 64 warehouses (TF/Predefine.h:8-10), customers by id.
+         = 0), 64 warehouses (TF/Predefine.h:8-10), customers by id; and its
+         KERNEL_CID by-name lookup (TF/tp.cu:11-23) on its own.
 Both return per-transaction flags rebuilt from the reference's conflict
 counters raw / war / waw (the commit flag from its own rule,
 TF/Execute_payment.h:607, Y1/Execute.h:187).
@@ -53,22 +54,48 @@ def _harness():
         _lib.ref_launch.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_uint),
                                     C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p),
                                     C.POINTER(C.c_int), C.c_char_p, C.c_int]
+        _lib.ref_time.restype = C.c_int
+        _lib.ref_time.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_uint),
+                                  C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p),
+                                  C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint64),
+                                  C.POINTER(C.c_uint64), C.POINTER(C.c_ubyte), C.c_int, C.POINTER(C.c_float),
+                                  C.c_char_p, C.c_int]
     return _lib
 
 
-def _launch(prog, layout, bufs, copy_back):
+def _launch(prog, layout, bufs, copy_back, resets=None, iters=0, kernels=None):
+    """Runs the three kernels (or `kernels` = (names, grids, blocks)) once
+    (iters = 0) or times `iters` repetitions, resetting the (buffer, offset,
+    length, byte) ranges before each one.  Returns the mean milliseconds of
+    each kernel when timing."""
     n = len(bufs)
-    names = (C.c_char_p * 3)(*[k.encode() for k in layout["kernels"]])
-    grids = (C.c_uint * 3)(*layout["grids"])
-    blocks = (C.c_uint * 3)(*layout["blocks"])
+    kn, kg, kb = kernels or (layout["kernels"], layout["grids"], layout["blocks"])
+    nk = len(kn)
+    names = (C.c_char_p * nk)(*[k.encode() for k in kn])
+    grids = (C.c_uint * nk)(*kg)
+    blocks = (C.c_uint * nk)(*kb)
     sizes = (C.c_uint64 * n)(*[b.nbytes for b in bufs])
     ptrs = (C.c_void_p * n)(*[b.ctypes.data for b in bufs])
     cb = (C.c_int * n)(*copy_back)
     err = C.create_string_buffer(256)
-    rc = _harness().ref_launch(os.path.join(REF, f"{prog}.cubin").encode(), 3, names, grids, blocks, n, sizes, ptrs,
-                               cb, err, 256)
+    cubin = os.path.join(REF, f"{prog}.cubin").encode()
+    if not iters:
+        rc = _harness().ref_launch(cubin, nk, names, grids, blocks, n, sizes, ptrs, cb, err, 256)
+        ms = None
+    else:
+        resets = resets or []
+        m = len(resets)
+        rb = (C.c_int * max(1, m))(*[r[0] for r in resets])
+        ro = (C.c_uint64 * max(1, m))(*[r[1] for r in resets])
+        rl = (C.c_uint64 * max(1, m))(*[r[2] for r in resets])
+        rv = (C.c_ubyte * max(1, m))(*[r[3] for r in resets])
+        out = (C.c_float * nk)()
+        rc = _harness().ref_time(cubin, nk, names, grids, blocks, n, sizes, ptrs, cb, m, rb, ro, rl, rv, iters, out,
+                                 err, 256)
+        ms = [float(x) for x in out]
     if rc:
         raise RuntimeError(f"reference kernels failed: {err.value.decode()}")
+    return ms
 
 
 def _flags(raw, war, waw):
@@ -97,9 +124,11 @@ class RefY1:
         # write, write-back 1 + writes (Y1/Predefine.h:31-35, Y1/Execute.h:79-252)
         self.covered = covered_txns(self.L, [2 * self.L["ops"], self.reads + 2 * writes, 1 + writes], self.B)
 
-    def run(self, read_keys, write_keys):
+    def run(self, read_keys, write_keys, iters=0):
         """read_keys: (B, reads) uint32, write_keys: (B,) uint32, TID = row index.
-        Returns the reference's flags and its COMMIT_AND_ABORT marks."""
+        Returns the reference's flags and its COMMIT_AND_ABORT marks (and, with
+        iters > 0, the mean milliseconds of its three kernels over `iters`
+        batches, each after the reference's per-batch clears)."""
         L, B = self.L, self.B
         s, q, lg = L["set"], L["query"], L["log"]
         set_b = np.zeros(s["size"], dtype=np.uint8)
@@ -113,12 +142,17 @@ class RefY1:
         log[:lg["ytd"]] = 0xFF  # registration tables cleared as clear_LOG does (Y1/Database.h:321-326)
         snap = np.zeros(L["snapshot"], dtype=np.uint8)
         index = np.zeros(max(1, L["index"]), dtype=np.uint8)
-        _launch("y1", L, [set_b, query, log, snap, index], [1, 0, 0, 0, 0])
+        # per batch the reference refills its registration tables with 0xFF
+        # (clear_LOG) and starts from fresh conflict counters and marks
+        resets = [(2, 0, lg["ytd"], 0xFF), (0, s["war"], s["size"] - s["war"], 0)]
+        ms = _launch("y1", L, [set_b, query, log, snap, index], [1, 0, 0, 0, 0], resets, iters)
         sv = set_b.view(np.uint32)
         raw = sv[s["raw"] // 4:s["raw"] // 4 + B]
         war = sv[s["war"] // 4:s["war"] // 4 + B]
         waw = sv[s["waw"] // 4:s["waw"] // 4 + B]
         mark = sv[s["commit"] // 4:s["commit"] // 4 + B]
+        if iters:
+            return _flags(raw, war, waw), mark, ms
         return _flags(raw, war, waw), mark
 
 
@@ -130,8 +164,10 @@ class RefTF:
         # 147 / 93 / 67 warp roles per 32 transactions (TF/Predefine.h:38-40)
         self.covered = covered_txns(self.L, [147, 93, 67], self.B)
 
-    def run(self, txns):
-        """txns: Payment records (TpccBatch.TXN_DTYPE) of one batch, TID = index."""
+    def run(self, txns, iters=0):
+        """txns: Payment records (TpccBatch.TXN_DTYPE) of one batch, TID = index.
+        Returns the flags (and, with iters > 0, the mean milliseconds of the
+        three kernels over `iters` batches, each after the per-batch clears)."""
         L, B = self.L, self.B
         ps, pq, lg = L["payment_set"], L["payment_query"], L["log"]
         assert len(txns) == B
@@ -160,9 +196,60 @@ class RefTF:
         snap = np.zeros(L["snapshot"], dtype=np.uint8)
         index = np.zeros(max(16, L["index"]), dtype=np.uint8)
         # argument order of KERNEL_EXECUTE / CHECK / WRITEBACK (TF/tp.cu:24-30)
-        _launch("tf", L, [nset, pset, nquery, query, log, snap, index], [0, 1, 0, 0, 0, 0, 0])
+        resets = [(4, 0, lg["w_ytd"], 0xFF), (1, ps["war"], ps["size"] - ps["war"], 0)]
+        ms = _launch("tf", L, [nset, pset, nquery, query, log, snap, index], [0, 1, 0, 0, 0, 0, 0], resets, iters)
         sv = pset.view(np.uint32)
         raw = sv[ps["raw"] // 4:ps["raw"] // 4 + B]
         war = sv[ps["war"] // 4:ps["war"] // 4 + B]
         waw = sv[ps["waw"] // 4:ps["waw"] // 4 + B]
+        if iters:
+            return _flags(raw, war, waw), ms
         return _flags(raw, war, waw)
+
+    def cid(self, txns, c_last, c_id):
+        """The reference's KERNEL_CID on one batch of Payments: the C_ID it
+        writes for each by-name query (LTPG_PAY_BY_NAME; c_id field =
+        (name << 8) | nth).  c_last / c_id: the customer table's C_LAST and C_ID
+        columns, loaded into its INDEX and SNAPSHOT as Database.h does
+        (TF/Database.h:188-211).
+
+        Only nth = 0 is accepted.  The lookup's lanes leave its shuffle loop at
+        different iterations for nth > 0 (a full-mask __shfl_sync after a
+        per-lane break, TF/Genericfunction.h:42-57), which is undefined; at
+        nth = 0 every lane leaves after the first iteration, together."""
+        L, B = self.L, self.B
+        assert len(txns) == B
+        by_name = ((txns["kind_info"] & 0xFF) == 1) & ((txns["kind_info"] & 0x100) != 0)
+        if (txns["c_id"][by_name] & 0xFF).any():
+            raise ValueError("KERNEL_CID is run on nth = 0 queries only")
+        pq = L["payment_query"]
+        query = np.zeros(pq["size"], dtype=np.uint8)
+        qv = query.view(np.uint32)
+
+        def put(field, values):
+            qv[pq[field] // 4:pq[field] // 4 + B] = np.asarray(values, dtype=np.uint32)
+
+        ki = txns["kind_info"]
+        put("W_ID", txns["w"])
+        put("D_ID", (ki >> 16) & 0xFF)
+        put("C_ID", np.where(by_name, 0, txns["c_id"]))
+        put("C_LAST", np.where(by_name, txns["c_id"], 20))
+        put("isName", by_name.astype(np.uint32))
+        put("C_D_ID", ki >> 24)
+        put("C_W_ID", txns["c_w"])
+        put("TID", np.arange(B))
+        CS = L["customer_size"]
+        assert len(c_last) == CS
+        snap = np.zeros(L["snapshot"], dtype=np.uint8)
+        sv = snap.view(np.uint32)
+        o = L["cust_snapshot"] // 4
+        sv[o:o + CS] = np.asarray(c_id, dtype=np.uint32)  # customer_snapshot[0 * CUSTOMER_SIZE + row]
+        index = np.zeros(L["index"], dtype=np.uint8)
+        iv = index.view(np.uint32)
+        iv[L["name_index"] // 4:L["name_index"] // 4 + CS] = np.asarray(c_last, dtype=np.uint32)
+        pset = np.zeros(L["payment_set"]["size"], dtype=np.uint8)
+        log = np.zeros(L["log"]["size"], dtype=np.uint8)
+        # KERNEL_CID(PAYMENT_SET*, PAYMENT_QUERY*, LOG*, SNAPSHOT*, INDEX*), <<<GRID_SIZE, BLOCK_SIZE>>> (TF/tp.cu:154)
+        _launch("tf", L, [pset, query, log, snap, index], [0, 1, 0, 0, 0],
+                kernels=([L["cid_kernel"]], [L["cid_grid"]], [L["cid_block"]]))
+        return qv[pq["C_ID"] // 4:pq["C_ID"] // 4 + B].copy()

@@ -189,8 +189,11 @@ def test_tpcc_invalid_record_reports_error(eng):
 # ---- tuning never changes outcomes ------------------------------------------------------
 @pytest.mark.parametrize("opt,filt,dd,bps", [(1, 0, 0, 0), (1, 1, 1, 2), (2, 0, 1, 1), (4, 1, 0, 0), (8, 1, 1, 0),
                                              (4, 0, 0, 3)])
-@pytest.mark.parametrize("k", [4, 7, 10, 16, 32])
+@pytest.mark.parametrize("k", [3, 4, 7, 10, 16, 20, 32])
 def test_launch_shapes_do_not_change_outcomes(eng, opt, filt, dd, bps, k):
+    """Every launch shape gives the oracle's results; strides that are not a
+    power of two (k = 10 -> 12, 20) run the one-op-per-lane kernel with padded
+    lanes."""
     n = 40000
     eng.load_ycsb(31, n)
     o = oracle.YcsbOracle(31, n)
@@ -206,8 +209,8 @@ def test_launch_shapes_do_not_change_outcomes(eng, opt, filt, dd, bps, k):
         eng.set_launch("ycsb", **saved)
 
 
-@pytest.mark.parametrize("ways", [1, 2, 4])
-def test_staging_does_not_change_outcomes(eng, ways):
+@pytest.mark.parametrize("ways,k,opt", [(1, 16, None), (2, 16, None), (4, 16, None), (4, 10, 1), (2, 20, 1)])
+def test_staging_does_not_change_outcomes(eng, ways, k, opt):
     """Stage the hottest buckets (and, in a second round, every bucket, so that
     most keys collide and fall back to the global path): results stay bit-exact
     and the staged registrations are counted."""
@@ -215,13 +218,13 @@ def test_staging_does_not_change_outcomes(eng, ways):
     n = 100000
     eng.load_ycsb(41, n)
     o = oracle.YcsbOracle(41, n)
-    g = YcsbGenerator(41, n, 30000, 16, 5, 0.99, rotate_every=2)
+    g = YcsbGenerator(41, n, 30000, k, 5, 0.99, rotate_every=2)
     saved = eng.get_launch("ycsb")
     try:
-        eng.set_launch("ycsb", stage_ways=ways)
+        eng.set_launch("ycsb", stage_ways=ways, **({} if opt is None else {"ops_per_thread": opt}))
         for bid in range(6):
             b = g.batch(bid)
-            keys = (b.ops.reshape(b.n_txn, -1)[:, :16] & ((1 << 27) - 1)).ravel()
+            keys = (b.ops.reshape(b.n_txn, -1)[:, :k] & ((1 << 27) - 1)).ravel()
             cnt = np.bincount(key_bucket(keys), minlength=abi.STAGE_BUCKETS)
             staged = np.argsort(-cnt, kind="stable")[:abi.STAGE_ENTRIES // ways] if bid < 3 else \
                 np.arange(abi.STAGE_BUCKETS)

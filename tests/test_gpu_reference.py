@@ -11,7 +11,7 @@ import pytest
 
 import oracle
 from oracle import reference
-from ltpg_gb300 import Engine, TpccGenerator, YcsbBatch, YcsbGenerator, abi
+from ltpg_gb300 import Engine, TpccBatch, TpccGenerator, YcsbBatch, YcsbGenerator, abi
 
 pytestmark = pytest.mark.gpu
 KEY_MASK = (1 << abi.YCSB_KEY_BITS) - 1
@@ -90,5 +90,44 @@ def test_reference_payment_flags_match(ref):
             eng.sync()
             assert np.array_equal(eng.txn_flags(0, B), want)
             assert (want & abi.FLAG_WAW).any() and (want & abi.FLAG_COMMIT).any()
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("data", ["generated", "reference"])
+def test_reference_name_lookup_matches(ref, data):
+    """The reference's KERNEL_CID (TF/tp.cu:11-23) on our Payments by last name
+    (nth = 0, where its warp stays converged) writes the C_IDs that the
+    oracle's LTPG_CFG_REF_NAME_LOOKUP rule computes, and the engine in that
+    mode gives the oracle's flags — on the generated names and on the
+    reference's own (C_LAST = row % 20, TF/Database.h:180)."""
+    r = reference.RefTF()
+    B, W = r.B, r.W
+    o = oracle.TpccOracle(9, W, ref_name_lookup=True)
+    cust = o.tables[abi.T_CUSTOMER].reshape(-1, abi.TPCC_COLS[abi.T_CUSTOMER])
+    if data == "reference":
+        cust[:, 13] = np.arange(len(cust)) % 20
+    b = TpccGenerator(9, W, B, neworder_pct=0, by_name_pct=60).next()
+    txns = b.txns.copy()
+    by_name = ((txns["kind_info"] & 0xFF) == abi.TPCC_PAYMENT) & ((txns["kind_info"] & abi.PAY_BY_NAME) != 0)
+    names = txns["c_id"] >> 8
+    if data == "reference":
+        names = names % 20
+    txns["c_id"] = np.where(by_name, names << 8, txns["c_id"])  # nth = 0
+    mb = TpccBatch(txns, b.lines, b.txn_base)
+    ref_cid = r.cid(txns, cust[:, 13], cust[:, 0])
+    want, found = o.resolve(mb)
+    assert found.all()
+    assert np.array_equal(ref_cid[by_name], want[by_name]), np.nonzero(ref_cid[by_name] != want[by_name])[0][:10]
+    assert np.array_equal(ref_cid[~by_name], txns["c_id"][~by_name])
+    eng = Engine(device=0, n_slots=1, max_txn=B, max_ops_per_txn=16, max_lines=16, ref_name_lookup=True)
+    try:
+        eng.load_tpcc(9, W)
+        if data == "reference":
+            eng.upload_table(abi.T_CUSTOMER, o.tables[abi.T_CUSTOMER])
+        eng.upload(0, mb)
+        eng.run_batch(0, "graph")
+        eng.sync()
+        assert np.array_equal(eng.txn_flags(0, B), o.run(mb)[0])
     finally:
         eng.close()
