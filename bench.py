@@ -43,6 +43,8 @@ WORKLOADS = {
                        name="YCSB small: 1M x 10 uint64, 65,536 txn x 10 ops, 50/50, Zipf theta=0.6"),
     "tpcc": dict(kind="tpcc", warehouses=64, n_txn=1 << 20, n_batches=8,
                  name="TPC-C NewOrder+Payment 50/50, W=64, 1,048,576 txn per batch"),
+    "tpcc_prof": dict(kind="tpcc", warehouses=16, n_txn=1 << 18, n_batches=4,
+                      name="TPC-C NewOrder+Payment 50/50, profiling size: W=16, 262,144 txn per batch"),
 }
 SEED = 20261203
 
@@ -687,12 +689,17 @@ def predictor_section(w, batches):
 
 def tpcc_bytes_per_txn():
     """Algorithmic bytes per TPC-C transaction (50/50 NewOrder/Payment, 10 lines
-    on average).  Execute: 32 B record + 8 B per line, 16 B registration per op,
-    reads W/D tax, C discount, item price (8 B each).  Check+write-back: record
-    and lines again, 16 B slot load per op, committed writes (NewOrder: ORDER 64,
-    NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE 80 + price and dist
-    reads 16; Payment: 2 hot adds 16, customer 3x8 read+write, HISTORY 64)."""
-    no_ops, pay_ops = 5 + 3 * 10, 5
+    on average).  Only ops that can conflict register and check: no NewOrder or
+    Payment writes a WAREHOUSE, DISTRICT or ITEM row through registration, so
+    NewOrder has 3 + 2 per line (customer read, NEW-ORDER and ORDER inserts,
+    stock write, ORDER-LINE insert) and Payment 3 (customer read and write,
+    HISTORY insert).  Execute: 32 B record + 8 B per line, 16 B registration per
+    op, reads W/D tax, C discount, item price (8 B each).  Check+write-back:
+    record and lines again, 16 B slot load per op, committed writes (NewOrder:
+    ORDER 64, NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE 80 + price
+    and dist reads 16; Payment: 2 hot adds 16, customer 3x8 read+write,
+    HISTORY 64)."""
+    no_ops, pay_ops = 3 + 2 * 10, 3
     ex_no = 32 + 80 + 16 * no_ops + 24 + 8 * 10 + 8
     ex_pay = 32 + 16 * pay_ops + 8 + 8
     cw_no = 32 + 80 + 16 * no_ops + 64 + 24 + 10 * (64 + 80 + 16) + 2

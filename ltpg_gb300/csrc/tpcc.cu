@@ -534,59 +534,107 @@ __device__ __forceinline__ uint64_t ld_ca_u64t(const unsigned long long *p) {
     return v;
 }
 
+// Tables that no NewOrder or Payment registers a write on: WAREHOUSE and
+// DISTRICT (their YTD updates are unregistered hot adds, D_NEXT_O_ID is
+// host-assigned, TF/Query.h:54-88) and ITEM (read-only).  A read of such a row
+// never sees RAW, and its registration can never give a writer WAR, so the
+// tuned kernels neither register nor check those reads; the outcome is the
+// plain path's, which keeps the reference's full op list.
+//
+// What remains is uniform: every transaction has three header ops (tpcc_op
+// j = 2, 3, 4 — NewOrder: customer read, NEW-ORDER insert, ORDER insert;
+// Payment: customer read, customer write, HISTORY insert) and every order line
+// two (stock write, ORDER-LINE insert: j = 5 + 3i + 1, + 2).  A block walks its
+// tile's header ops, three lanes per transaction, then its lines, one lane per
+// line, so the lanes of a warp run the same code.  Lanes are in TID order in
+// both passes, so the lowest lane of a warp's same-slot group holds the
+// smallest TID.
+
+// One registration; `dedupe`: one atomic per distinct slot of the warp,
+// `filter`: skipped when the slot already holds a smaller tag.  Warp-uniform.
+__device__ __forceinline__ void tuned_register(const TpccTunedArgs &a, bool valid, uint64_t slot_idx, bool is_w,
+                                               unsigned long long mine, bool dedupe, bool filter) {
+    bool leader = valid;
+    if (dedupe) {
+        const unsigned long long mkey = valid ? (slot_idx << 1) | (is_w ? 1ull : 0ull) : ~0ull;
+        const unsigned peers = __match_any_sync(FULL, mkey);
+        leader = valid && (__ffs(peers) - 1) == (int)(threadIdx.x & 31);
+    }
+    if (!leader) return;
+    RegSlot *s = a.reg + slot_idx;
+    unsigned long long *p = is_w ? &s->w : &s->r;
+    if (!filter || ld_ca_u64t(p) > mine) red_min(p, mine);
+}
+
+// Order line e of a tile whose line prefix is h.off: owner transaction and
+// the line's index within it.
+__device__ __forceinline__ void tile_line(const TileHdr &h, uint32_t nt, uint32_t e, uint32_t &i, uint32_t &li) {
+    i = tile_owner(h, nt, e);
+    li = e - h.off[i];
+}
+
+__device__ __forceinline__ uint32_t load_tile_lines(TileHdr &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
+                                                    uint32_t n_lines) {
+    return load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl, [&](uint32_t i) {
+        return (h.ok[i] && tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER) ? tpcc_ol_cnt(h.x[i].kind_info) : 0u;
+    });
+}
+
 __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr &h, uint64_t tag) {
     const uint32_t n_lines = (uint32_t)a.hdr[0];
     __shared__ unsigned long long sum[PT];
     __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
     __shared__ long long res[PT];
-    const uint32_t lane = threadIdx.x & 31;
+    const bool filt = a.filter != 0u;
     const uint32_t n_tiles = (a.B + PT - 1) / PT;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
         if (threadIdx.x < PT) sum[threadIdx.x] = 0ull;
-        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl,
-                                         [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
-        for (uint32_t base = 0; base < total; base += blockDim.x) {
+        const uint32_t total = load_tile_lines(h, a, t0, nt, n_lines);
+        // header ops: three lanes per transaction
+        for (uint32_t base = 0; base < 3u * nt; base += blockDim.x) {
             const uint32_t e = base + threadIdx.x;
-            const bool act = e < total;
-            uint32_t i = 0, j = 0;
-            bool valid = act;
-            ltpg_tpcc_line ln{0, 0, 0};
+            const uint32_t i = e / 3u, k = e - 3u * i;
+            const bool valid = e < 3u * nt && h.ok[i];
+            const ltpg_tpcc_line no_line{0, 0, 0};
             TpccOp op{0, 0, 0};
-            if (act) {
-                i = tile_owner(h, nt, e);
-                j = e - h.off[i];
-                if (tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER && j >= 5) {
-                    ln = load_line(a.lines, (uint64_t)h.x[i].line_off + (j - 5) / 3);
-                    if (!line_valid(ln, a.db.W)) {
-                        report_error(a.ctl, DERR_BOUNDS, t0 + i);
-                        valid = false;
-                    }
-                }
-                if (valid) op = tpcc_op(h.x[i], j, ln, a.db.strict);
-            }
-            const uint64_t slot_idx = a.db.base[op.table] + op.row;
-            const unsigned long long mkey =
-                valid ? (slot_idx << 2) | ((op.flags & OPF_REG_W) ? 2ull : 1ull) : ~0ull;
-            const unsigned peers = __match_any_sync(FULL, mkey);
-            if (valid && (__ffs(peers) - 1) == (int)lane) {
-                RegSlot *s = a.reg + slot_idx;
-                unsigned long long *p = (op.flags & OPF_REG_W) ? &s->w : &s->r;
-                const unsigned long long mine = tag | (t0 + i);
-                if (!a.filter || ld_ca_u64t(p) > mine) red_min(p, mine);
-            }
-            if (valid) {
+            if (valid) op = tpcc_op(h.x[i], k + 2u, no_line, a.db.strict);
+            const bool w = (op.flags & OPF_REG_W) != 0u;
+            // customer rows repeat (NURand); the inserts are unique per batch
+            tuned_register(a, valid, a.db.base[op.table] + op.row, w, tag | (t0 + i), true,
+                           filt && op.table == LTPG_T_CUSTOMER);
+            if (valid && k == 0u) {
                 const ltpg_tpcc_txn &x = h.x[i];
                 if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
-                    if (j == 0) wtax[i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, op.row, W_TAX);
-                    else if (j == 1) dtax[i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, op.row, D_TAX);
-                    else if (j == 2) disc[i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
-                    else if (op.table == LTPG_T_ITEM)
-                        atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(a.db, LTPG_T_ITEM, op.row, I_PRICE));
-                } else if (j == 2) {
+                    wtax[i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, x.w, W_TAX);
+                    dtax[i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, 10ull * x.w + tpcc_d(x.kind_info), D_TAX);
+                    disc[i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
+                } else {
                     res[i] = (long long)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
                 }
             }
+        }
+        // order lines: one lane per line (stock write, ORDER-LINE insert, item price)
+        for (uint32_t base = 0; base < total; base += blockDim.x) {
+            const uint32_t e = base + threadIdx.x;
+            bool valid = e < total;
+            uint32_t i = 0, li = 0;
+            ltpg_tpcc_line ln{0, 0, 0};
+            if (valid) {
+                tile_line(h, nt, e, i, li);
+                ln = load_line(a.lines, (uint64_t)h.x[i].line_off + li);
+                if (!line_valid(ln, a.db.W)) {
+                    report_error(a.ctl, DERR_BOUNDS, t0 + i);
+                    valid = false;
+                }
+            }
+            const unsigned long long mine = tag | (t0 + i);
+            const ltpg_tpcc_txn &x = h.x[i];
+            const uint64_t srow = 100000ull * ln.supply_w + ln.i_id;
+            tuned_register(a, valid, a.db.base[LTPG_T_STOCK] + srow, true, mine, true, filt);
+            tuned_register(a, valid, a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, li), true, mine, false,
+                           false);
+            if (valid) atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(a.db, LTPG_T_ITEM, ln.i_id, I_PRICE));
         }
         __syncthreads();
         if (threadIdx.x < nt) {
@@ -614,23 +662,35 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
         if (threadIdx.x < PT) fl[threadIdx.x] = 0u;
-        const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl,
-                                         [&](uint32_t i) { return h.ok[i] ? tpcc_n_ops(h.x[i].kind_info) : 0u; });
-        for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-            const uint32_t i = tile_owner(h, nt, e), j = e - h.off[i];
-            const ltpg_tpcc_txn &x = h.x[i];
-            ltpg_tpcc_line ln{0, 0, 0};
-            if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER && j >= 5) {
-                ln = load_line(a.lines, (uint64_t)x.line_off + (j - 5) / 3);
-                if (!line_valid(ln, a.db.W)) continue;
-            }
-            const TpccOp op = tpcc_op(x, j, ln, a.db.strict);
+        const uint32_t total = load_tile_lines(h, a, t0, nt, n_lines);
+        // header ops, three lanes per transaction (reads of WAREHOUSE, DISTRICT
+        // and ITEM rows cannot conflict; see tpcc_exec_tiles)
+        for (uint32_t e = threadIdx.x; e < 3u * nt; e += blockDim.x) {
+            const uint32_t i = e / 3u, k = e - 3u * i;
+            if (!h.ok[i]) continue;
+            const ltpg_tpcc_line no_line{0, 0, 0};
+            const TpccOp op = tpcc_op(h.x[i], k + 2u, no_line, a.db.strict);
             const ulonglong2 s = ld_slot(a.reg + a.db.base[op.table] + op.row);
             const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch), t = t0 + i;
             uint32_t f = 0;
             if ((op.flags & OPF_CHK_RAW) && wmin < t) f |= LTPG_FLAG_RAW;
             if ((op.flags & OPF_CHK_WAR) && rmin < t) f |= LTPG_FLAG_WAR;
             if ((op.flags & OPF_CHK_WAW) && wmin < t) f |= LTPG_FLAG_WAW;
+            if (f) atomicOr(&fl[i], f);
+        }
+        // order lines: stock write and ORDER-LINE insert, WAR and WAW each
+        for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+            uint32_t i, li;
+            tile_line(h, nt, e, i, li);
+            const ltpg_tpcc_txn &x = h.x[i];
+            const ltpg_tpcc_line ln = load_line(a.lines, (uint64_t)x.line_off + li);
+            if (!line_valid(ln, a.db.W)) continue;
+            const ulonglong2 s1 = ld_slot(a.reg + a.db.base[LTPG_T_STOCK] + 100000ull * ln.supply_w + ln.i_id);
+            const ulonglong2 s2 = ld_slot(a.reg + a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, li));
+            const uint32_t t = t0 + i;
+            uint32_t f = 0;
+            if (slot_min(s1.x, epoch) < t || slot_min(s2.x, epoch) < t) f |= LTPG_FLAG_WAR;
+            if (slot_min(s1.y, epoch) < t || slot_min(s2.y, epoch) < t) f |= LTPG_FLAG_WAW;
             if (f) atomicOr(&fl[i], f);
         }
         __syncthreads();
