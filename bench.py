@@ -176,8 +176,7 @@ def profile_traffic(workload, kernel):
 def ycsb_exec_kernel_name(launch, stride):
     """Name of the execute kernel the tuned path launches for this shape."""
     opt = (launch or {}).get("ops_per_thread", 1)
-    pow2 = stride <= 32 and (stride & (stride - 1)) == 0
-    if opt == 1 and pow2:
+    if opt == 1 and stride <= 32:
         return "ycsb_exec_coop"
     if opt in (2, 4) and stride % opt == 0 and ((stride // opt) & (stride // opt - 1)) == 0:
         return "ycsb_exec_fast"

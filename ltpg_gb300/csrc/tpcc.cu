@@ -207,17 +207,21 @@ __device__ __forceinline__ bool resolve_by_name(const TpccDev &db, ltpg_tpcc_txn
 }
 
 constexpr uint32_t PT = 64;    // transactions per tile (plain path)
-constexpr uint32_t PBS = 256;  // threads per block (plain path)
+constexpr uint32_t PTT = 128;  // transactions per tile (tuned path)
+constexpr uint32_t PBS = 256;  // threads per block
 
-struct TileHdr {
-    ltpg_tpcc_txn x[PT];
-    uint32_t off[PT + 1];
-    uint32_t ok[PT];
+template <uint32_t N>
+struct TileHdrN {
+    ltpg_tpcc_txn x[N];
+    uint32_t off[N + 1];
+    uint32_t ok[N];
 };
+using TileHdr = TileHdrN<PT>;
+using TileHdrT = TileHdrN<PTT>;
 
 // Loads a tile and lays out its ops (n_ops_of = ops per transaction).
-template <class F>
-__device__ __forceinline__ uint32_t load_tile(TileHdr &h, const ltpg_tpcc_txn *__restrict__ txns, uint32_t t0,
+template <class H, class F>
+__device__ __forceinline__ uint32_t load_tile(H &h, const ltpg_tpcc_txn *__restrict__ txns, uint32_t t0,
                                               uint32_t nt, const TpccDev &db, uint32_t n_lines, DevCtl *ctl,
                                               F n_ops_of) {
     if (threadIdx.x < nt) {
@@ -250,7 +254,8 @@ __device__ __forceinline__ uint32_t load_tile(TileHdr &h, const ltpg_tpcc_txn *_
 }
 
 // Transaction of flat op e: the last i with off[i] <= e.
-__device__ __forceinline__ uint32_t tile_owner(const TileHdr &h, uint32_t nt, uint32_t e) {
+template <class H>
+__device__ __forceinline__ uint32_t tile_owner(const H &h, uint32_t nt, uint32_t e) {
     uint32_t lo = 0, hi = nt;  // off[lo] <= e < off[hi]
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
@@ -568,73 +573,84 @@ __device__ __forceinline__ void tuned_register(const TpccTunedArgs &a, bool vali
 
 // Order line e of a tile whose line prefix is h.off: owner transaction and
 // the line's index within it.
-__device__ __forceinline__ void tile_line(const TileHdr &h, uint32_t nt, uint32_t e, uint32_t &i, uint32_t &li) {
+__device__ __forceinline__ void tile_line(const TileHdrT &h, uint32_t nt, uint32_t e, uint32_t &i, uint32_t &li) {
     i = tile_owner(h, nt, e);
     li = e - h.off[i];
 }
 
-__device__ __forceinline__ uint32_t load_tile_lines(TileHdr &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
+__device__ __forceinline__ uint32_t load_tile_lines(TileHdrT &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
                                                     uint32_t n_lines) {
     return load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl, [&](uint32_t i) {
         return (h.ok[i] && tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER) ? tpcc_ol_cnt(h.x[i].kind_info) : 0u;
     });
 }
 
-__device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr &h, uint64_t tag) {
+// Work item e of a tile: e < 3 nt is header op k = e % 3 of transaction e / 3,
+// the rest are order lines.  Each item has up to two registrations: the header
+// op, or the line's stock write and ORDER-LINE insert.
+struct TileItem {
+    uint32_t i, k, li;
+    bool head, valid, two;
+    ltpg_tpcc_line ln;
+    TpccOp op;
+};
+__device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const TileHdrT &h, uint32_t nt, uint32_t e,
+                                              uint32_t n_items, uint32_t t0, bool report) {
+    TileItem it{0, 0, 0, false, false, false, {0, 0, 0}, {0, 0, 0}};
+    if (e >= n_items) return it;
+    const uint32_t n_head = 3u * nt;
+    if (e < n_head) {
+        it.head = true;
+        it.i = e / 3u;
+        it.k = e - 3u * it.i;
+        it.valid = h.ok[it.i] != 0u;
+        if (it.valid) it.op = tpcc_op(h.x[it.i], it.k + 2u, it.ln, a.db.strict);
+        return it;
+    }
+    tile_line(h, nt, e - n_head, it.i, it.li);
+    it.ln = load_line(a.lines, (uint64_t)h.x[it.i].line_off + it.li);
+    it.valid = line_valid(it.ln, a.db.W);
+    if (!it.valid && report) report_error(a.ctl, DERR_BOUNDS, t0 + it.i);
+    it.two = it.valid;
+    return it;
+}
+
+__device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT &h, uint64_t tag) {
     const uint32_t n_lines = (uint32_t)a.hdr[0];
-    __shared__ unsigned long long sum[PT];
-    __shared__ uint32_t wtax[PT], dtax[PT], disc[PT];
-    __shared__ long long res[PT];
+    __shared__ unsigned long long sum[PTT];
+    __shared__ uint32_t wtax[PTT], dtax[PTT], disc[PTT];
+    __shared__ long long res[PTT];
     const bool filt = a.filter != 0u;
-    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
-        if (threadIdx.x < PT) sum[threadIdx.x] = 0ull;
-        const uint32_t total = load_tile_lines(h, a, t0, nt, n_lines);
-        // header ops: three lanes per transaction
-        for (uint32_t base = 0; base < 3u * nt; base += blockDim.x) {
-            const uint32_t e = base + threadIdx.x;
-            const uint32_t i = e / 3u, k = e - 3u * i;
-            const bool valid = e < 3u * nt && h.ok[i];
-            const ltpg_tpcc_line no_line{0, 0, 0};
-            TpccOp op{0, 0, 0};
-            if (valid) op = tpcc_op(h.x[i], k + 2u, no_line, a.db.strict);
-            const bool w = (op.flags & OPF_REG_W) != 0u;
-            // customer rows repeat (NURand); the inserts are unique per batch
-            tuned_register(a, valid, a.db.base[op.table] + op.row, w, tag | (t0 + i), true,
-                           filt && op.table == LTPG_T_CUSTOMER);
-            if (valid && k == 0u) {
-                const ltpg_tpcc_txn &x = h.x[i];
-                if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
-                    wtax[i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, x.w, W_TAX);
-                    dtax[i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, 10ull * x.w + tpcc_d(x.kind_info), D_TAX);
-                    disc[i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
-                } else {
-                    res[i] = (long long)ld_col(a.db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
-                }
-            }
-        }
-        // order lines: one lane per line (stock write, ORDER-LINE insert, item price)
-        for (uint32_t base = 0; base < total; base += blockDim.x) {
-            const uint32_t e = base + threadIdx.x;
-            bool valid = e < total;
-            uint32_t i = 0, li = 0;
-            ltpg_tpcc_line ln{0, 0, 0};
-            if (valid) {
-                tile_line(h, nt, e, i, li);
-                ln = load_line(a.lines, (uint64_t)h.x[i].line_off + li);
-                if (!line_valid(ln, a.db.W)) {
-                    report_error(a.ctl, DERR_BOUNDS, t0 + i);
-                    valid = false;
-                }
-            }
-            const unsigned long long mine = tag | (t0 + i);
-            const ltpg_tpcc_txn &x = h.x[i];
-            const uint64_t srow = 100000ull * ln.supply_w + ln.i_id;
-            tuned_register(a, valid, a.db.base[LTPG_T_STOCK] + srow, true, mine, true, filt);
-            tuned_register(a, valid, a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, li), true, mine, false,
+        const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
+        if (threadIdx.x < PTT) sum[threadIdx.x] = 0ull;
+        const uint32_t n_items = 3u * nt + load_tile_lines(h, a, t0, nt, n_lines);
+        for (uint32_t base = 0; base < n_items; base += blockDim.x) {
+            const TileItem it = tile_item(a, h, nt, base + threadIdx.x, n_items, t0, true);
+            const ltpg_tpcc_txn &x = h.x[it.i];
+            const unsigned long long mine = tag | (t0 + it.i);
+            // header: the op (customer rows repeat under NURand, the inserts are
+            // unique per batch); line: the stock write, then the ORDER-LINE insert
+            const uint64_t srow = 100000ull * it.ln.supply_w + it.ln.i_id;
+            const uint64_t s1 = it.head ? a.db.base[it.op.table] + it.op.row : a.db.base[LTPG_T_STOCK] + srow;
+            const bool w1 = it.head ? (it.op.flags & OPF_REG_W) != 0u : true;
+            const bool f1 = filt && (it.head ? it.op.table == LTPG_T_CUSTOMER : true);
+            tuned_register(a, it.valid, s1, w1, mine, true, f1);
+            tuned_register(a, it.two, a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, it.li), true, mine, false,
                            false);
-            if (valid) atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(a.db, LTPG_T_ITEM, ln.i_id, I_PRICE));
+            if (!it.valid) continue;
+            if (!it.head) {
+                atomicAdd(&sum[it.i], (unsigned long long)it.ln.qty * ld_col(a.db, LTPG_T_ITEM, it.ln.i_id, I_PRICE));
+            } else if (it.k == 0u) {
+                if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
+                    wtax[it.i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, x.w, W_TAX);
+                    dtax[it.i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, 10ull * x.w + tpcc_d(x.kind_info), D_TAX);
+                    disc[it.i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, it.op.row, C_DISCOUNT);
+                } else {
+                    res[it.i] = (long long)ld_col(a.db, LTPG_T_CUSTOMER, it.op.row, C_BALANCE) - tpcc_amount(x);
+                }
+            }
         }
         __syncthreads();
         if (threadIdx.x < nt) {
@@ -651,50 +667,43 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdr 
 }
 
 // hot: 11 W int64 sums in shared memory (W <= HOT_SMEM_MAX_W), or null.
-__device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdr &h, uint32_t epoch,
+__device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdrT &h, uint32_t epoch,
                                                    long long *hot) {
     const uint32_t n_lines = (uint32_t)a.hdr[0];
     const uint64_t txn_base = a.hdr[1];
-    __shared__ uint32_t fl[PT];
+    __shared__ uint32_t fl[PTT];
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
     unsigned long long c_com = 0, c_raw = 0, c_war = 0, c_waw = 0;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const uint32_t t0 = tile * PT, nt = min(PT, a.B - t0);
-        if (threadIdx.x < PT) fl[threadIdx.x] = 0u;
-        const uint32_t total = load_tile_lines(h, a, t0, nt, n_lines);
-        // header ops, three lanes per transaction (reads of WAREHOUSE, DISTRICT
+        const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
+        if (threadIdx.x < PTT) fl[threadIdx.x] = 0u;
+        const uint32_t n_items = 3u * nt + load_tile_lines(h, a, t0, nt, n_lines);
+        // header ops and order lines in one pass (reads of WAREHOUSE, DISTRICT
         // and ITEM rows cannot conflict; see tpcc_exec_tiles)
-        for (uint32_t e = threadIdx.x; e < 3u * nt; e += blockDim.x) {
-            const uint32_t i = e / 3u, k = e - 3u * i;
-            if (!h.ok[i]) continue;
-            const ltpg_tpcc_line no_line{0, 0, 0};
-            const TpccOp op = tpcc_op(h.x[i], k + 2u, no_line, a.db.strict);
-            const ulonglong2 s = ld_slot(a.reg + a.db.base[op.table] + op.row);
-            const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch), t = t0 + i;
+        for (uint32_t e = threadIdx.x; e < n_items; e += blockDim.x) {
+            const TileItem it = tile_item(a, h, nt, e, n_items, t0, false);
+            if (!it.valid) continue;
+            const uint32_t t = t0 + it.i;
             uint32_t f = 0;
-            if ((op.flags & OPF_CHK_RAW) && wmin < t) f |= LTPG_FLAG_RAW;
-            if ((op.flags & OPF_CHK_WAR) && rmin < t) f |= LTPG_FLAG_WAR;
-            if ((op.flags & OPF_CHK_WAW) && wmin < t) f |= LTPG_FLAG_WAW;
-            if (f) atomicOr(&fl[i], f);
-        }
-        // order lines: stock write and ORDER-LINE insert, WAR and WAW each
-        for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-            uint32_t i, li;
-            tile_line(h, nt, e, i, li);
-            const ltpg_tpcc_txn &x = h.x[i];
-            const ltpg_tpcc_line ln = load_line(a.lines, (uint64_t)x.line_off + li);
-            if (!line_valid(ln, a.db.W)) continue;
-            const ulonglong2 s1 = ld_slot(a.reg + a.db.base[LTPG_T_STOCK] + 100000ull * ln.supply_w + ln.i_id);
-            const ulonglong2 s2 = ld_slot(a.reg + a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, li));
-            const uint32_t t = t0 + i;
-            uint32_t f = 0;
-            if (slot_min(s1.x, epoch) < t || slot_min(s2.x, epoch) < t) f |= LTPG_FLAG_WAR;
-            if (slot_min(s1.y, epoch) < t || slot_min(s2.y, epoch) < t) f |= LTPG_FLAG_WAW;
-            if (f) atomicOr(&fl[i], f);
+            if (it.head) {
+                const ulonglong2 s = ld_slot(a.reg + a.db.base[it.op.table] + it.op.row);
+                const uint32_t rmin = slot_min(s.x, epoch), wmin = slot_min(s.y, epoch);
+                if ((it.op.flags & OPF_CHK_RAW) && wmin < t) f |= LTPG_FLAG_RAW;
+                if ((it.op.flags & OPF_CHK_WAR) && rmin < t) f |= LTPG_FLAG_WAR;
+                if ((it.op.flags & OPF_CHK_WAW) && wmin < t) f |= LTPG_FLAG_WAW;
+            } else {
+                // stock write and ORDER-LINE insert: WAR and WAW each
+                const ltpg_tpcc_txn &x = h.x[it.i];
+                const ulonglong2 s1 = ld_slot(a.reg + a.db.base[LTPG_T_STOCK] + 100000ull * it.ln.supply_w + it.ln.i_id);
+                const ulonglong2 s2 = ld_slot(a.reg + a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, it.li));
+                if (slot_min(s1.x, epoch) < t || slot_min(s2.x, epoch) < t) f |= LTPG_FLAG_WAR;
+                if (slot_min(s1.y, epoch) < t || slot_min(s2.y, epoch) < t) f |= LTPG_FLAG_WAW;
+            }
+            if (f) atomicOr(&fl[it.i], f);
         }
         __syncthreads();
-        if (threadIdx.x < PT) {
+        if (threadIdx.x < PTT) {
             uint32_t f = threadIdx.x < nt ? fl[threadIdx.x] : 0u;
             const bool com = threadIdx.x < nt && h.ok[threadIdx.x] && commits(f);
             if (com) f |= LTPG_FLAG_COMMIT;
@@ -765,12 +774,12 @@ __device__ __forceinline__ void hot_flush(const TpccDev &db, const long long *ho
 }
 
 __global__ void __launch_bounds__(PBS) tpcc_exec_tuned(TpccTunedArgs a) {
-    __shared__ TileHdr h;
+    __shared__ TileHdrT h;
     tpcc_exec_tiles(a, h, slot_tag(a.ctl->epoch));
 }
 
 __global__ void __launch_bounds__(PBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
-    __shared__ TileHdr h;
+    __shared__ TileHdrT h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
     if (hot) hot_init(hot, 11u * a.db.W);
@@ -780,7 +789,7 @@ __global__ void __launch_bounds__(PBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
 }
 
 __global__ void __launch_bounds__(PBS) tpcc_persistent(TpccTunedArgs a) {
-    __shared__ TileHdr h;
+    __shared__ TileHdrT h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
     const uint32_t epoch = a.ctl->epoch;
@@ -817,7 +826,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     if (c->launch_c.blocks_per_sm && (int)c->launch_c.blocks_per_sm < per_sm) per_sm = (int)c->launch_c.blocks_per_sm;
-    const uint32_t n_tiles = (a.B + PT - 1) / PT;
+    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
     const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm * c->sm_count));
     if (mode == LTPG_MODE_PERSISTENT) {
         prof_mark(c, 0);
