@@ -229,6 +229,37 @@ def timed(eng, torch, n_slots, steps, mode, start, dist):
     return ev0.elapsed_time(ev1) / 1e3, c1 - c0, l1 - l0, nxt
 
 
+def e2e_run(eng, pinned, mode, steps, n_slots, n_txn, dist, depth=3):
+    """End to end through the pipelined host-buffer calls (ltpg_submit_*_host /
+    ltpg_host_wait): every step copies its pinned host batch to the device,
+    runs it and copies its commit bitmap back to pinned host memory; up to
+    `depth` steps are in flight, so one batch's copy overlaps the previous
+    one's kernels.  Host wall time from the first submit to the last bitmap."""
+    import ltpg_gb300 as L
+    depth = max(1, min(depth, n_slots))
+    words = (n_txn + 31) // 32
+    bits = [L.pinned_empty(words) for _ in range(depth)]
+
+    def go(count):
+        for i in range(count):
+            s = i % depth
+            if i >= depth:
+                eng.host_wait(s)
+            eng.submit_host(s, pinned[i % len(pinned)], mode, bits[s])
+        for i in range(max(0, count - depth), count):
+            eng.host_wait(i % depth)
+
+    go(depth + 2)
+    c0, _ = eng.counters()
+    barrier(dist)
+    t0 = time.perf_counter()
+    go(steps)
+    t1 = time.perf_counter()
+    c1, _ = eng.counters()
+    return dict(secs=t1 - t0, commits=c1 - c0, steps=steps, depth=depth,
+                h2d=int(np.mean([p.nbytes() for p in pinned])), d2h=words * 4)
+
+
 def ycsb_bench(args, w, theta, dist, want_extras=True):
     import torch
     import ltpg_gb300 as L
@@ -290,18 +321,7 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
         if want_extras:
             eng.load_ycsb(SEED, w["n_records"])
             pinned = [L.pinned_copy(b) for b in batches[:min(len(batches), 8)]]
-            bits = np.empty((w["n_txn"] + 31) // 32, dtype=np.uint32)
-            for i in range(3):
-                eng.run_host(0, pinned[i % len(pinned)], args.mode, bits)
-            c0, _ = eng.counters()
-            barrier(dist)
-            t0 = time.perf_counter()
-            for i in range(args.e2e_steps):
-                eng.run_host(i % n_slots, pinned[i % len(pinned)], args.mode, bits)
-            t1 = time.perf_counter()
-            c1, _ = eng.counters()
-            e2e = dict(secs=t1 - t0, commits=c1 - c0, steps=args.e2e_steps,
-                       h2d=int(np.mean([p.nbytes() for p in pinned])), d2h=int(bits.nbytes))
+            e2e = e2e_run(eng, pinned, args.mode, args.e2e_steps, n_slots, w["n_txn"], dist)
     finally:
         eng.close()
     return res, exact, e2e, batches
@@ -365,17 +385,7 @@ def tpcc_bench(args, w, dist, want_extras=True):
         exact = all(np.array_equal(x, y) for x, y in zip(a[0], b[0])) and a[1] == b[1]
         eng.load_tpcc(SEED, w["warehouses"])
         pinned = [L.pinned_copy(b) for b in batches[:4]]
-        bits = np.empty((w["n_txn"] + 31) // 32, dtype=np.uint32)
-        for i in range(2):
-            eng.run_host(0, pinned[i], args.mode, bits)
-        c0, _ = eng.counters()
-        t0 = time.perf_counter()
-        for i in range(args.e2e_steps):
-            eng.run_host(i % n_slots, pinned[i % len(pinned)], args.mode, bits)
-        t1 = time.perf_counter()
-        c1, _ = eng.counters()
-        e2e = dict(secs=t1 - t0, commits=c1 - c0, steps=args.e2e_steps,
-                   h2d=int(np.mean([p.nbytes() for p in pinned])), d2h=int(bits.nbytes))
+        e2e = e2e_run(eng, pinned, args.mode, args.e2e_steps, n_slots, w["n_txn"], dist)
     finally:
         eng.close()
     return res, exact, e2e, batches
@@ -594,7 +604,8 @@ def main():
                      "kernel_ms": {"execute": exec_ms, "check_writeback": cwb_ms},
                      "pattern_ceilings": ceilings},
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
-                "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"]},
+                "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],
+                "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)"},
         "gpu_launches": int(tuned["launches"]),
         "launch": launch,
         "clocks": tuned["clocks"],

@@ -279,6 +279,20 @@ int ltpg_run_ycsb_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b, i
                        uint32_t *host_bitmap);
 int ltpg_run_tpcc_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, int mode,
                        uint32_t *host_bitmap);
+/* Pipelined form of the two calls above (no reference counterpart: the
+ * reference's epoch loop copies, runs and synchronises each batch in turn,
+ * TF/tp.cu:136-261).  Returns once the slot's copy (on a copy stream, after
+ * the slot's previous batch is finished), run and bitmap download are
+ * enqueued; ltpg_host_wait(slot) returns when that bitmap is on the host, with
+ * any device-side error of the batch.  The copy of one batch overlaps the
+ * kernels of the previous ones.  The host buffers, pinned
+ * (ltpg_host_alloc) for the copies to overlap, must stay unchanged until the
+ * wait. */
+int ltpg_submit_ycsb_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b, int mode,
+                          uint32_t *host_bitmap);
+int ltpg_submit_tpcc_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, int mode,
+                          uint32_t *host_bitmap);
+int ltpg_host_wait(ltpg_ctx *ctx, uint32_t slot);
 
 /* ---- results (statistic_query / copy_to_host surface) ------------------- */
 /* Replaces: Query::copy_to_host (TF/Query.h:606-631), which reads back only

@@ -138,6 +138,19 @@ def pinned_copy(batch):
 _PINNED = {}
 
 
+def pinned_empty(n, dtype=np.uint32):
+    """Uninitialised array of n elements in pinned host memory (for bitmaps of
+    pipelined host calls); keep it alive while the engine writes it."""
+    dtype = np.dtype(dtype)
+    nbytes = max(int(n) * dtype.itemsize, 16)
+    ptr = lib().ltpg_host_alloc(nbytes)
+    if not ptr:
+        raise MemoryError("ltpg_host_alloc failed")
+    out = np.frombuffer((C.c_char * nbytes).from_address(ptr), dtype=dtype, count=int(n))
+    _PINNED[id(out)] = ptr
+    return out
+
+
 def _check(code, ctx=None):
     if code != abi.OK:
         msg = lib().ltpg_last_error(ctx).decode() if ctx else "invalid argument"
@@ -298,6 +311,21 @@ class Engine:
         else:
             self._ck(lib().ltpg_run_tpcc_host(self._h, slot, C.byref(cb), m, _p(out)))
         return out
+
+    def submit_host(self, slot, batch, mode, bitmap):
+        """Pipelined host-buffer call (ltpg_submit_*_host): returns once the copy,
+        run and bitmap download are enqueued; `bitmap` (pinned_empty) holds the
+        result after host_wait(slot).  Keep `batch` and `bitmap` alive and
+        unchanged until then."""
+        cb = batch.as_c()
+        m = MODES[mode] if isinstance(mode, str) else mode
+        if isinstance(batch, YcsbBatch):
+            self._ck(lib().ltpg_submit_ycsb_host(self._h, slot, C.byref(cb), m, _p(bitmap)))
+        else:
+            self._ck(lib().ltpg_submit_tpcc_host(self._h, slot, C.byref(cb), m, _p(bitmap)))
+
+    def host_wait(self, slot):
+        self._ck(lib().ltpg_host_wait(self._h, slot))
 
     # results
     def commit_bitmap(self, slot, n_txn):

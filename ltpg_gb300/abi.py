@@ -115,6 +115,9 @@ SIGNATURES = {
     "ltpg_run_batches": (C.c_int, [P, U32, U32, C.c_int]),
     "ltpg_run_ycsb_host": (C.c_int, [P, U32, C.POINTER(YcsbBatchC), C.c_int, P]),
     "ltpg_run_tpcc_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), C.c_int, P]),
+    "ltpg_submit_ycsb_host": (C.c_int, [P, U32, C.POINTER(YcsbBatchC), C.c_int, P]),
+    "ltpg_submit_tpcc_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), C.c_int, P]),
+    "ltpg_host_wait": (C.c_int, [P, U32]),
     "ltpg_commit_bitmap": (C.c_int, [P, U32, P, SZ]),
     "ltpg_txn_flags": (C.c_int, [P, U32, P, SZ]),
     "ltpg_txn_results": (C.c_int, [P, U32, P, SZ]),

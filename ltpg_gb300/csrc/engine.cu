@@ -46,6 +46,8 @@ void free_slot(Slot &s) {
     dev_free(s.bitmap);
     dev_free(s.results);
     dev_free(s.stats);
+    if (s.copied) cudaEventDestroy(s.copied);
+    if (s.done) cudaEventDestroy(s.done);
     s = Slot{};
 }
 
@@ -173,6 +175,7 @@ int ltpg_destroy(ltpg_ctx *c) {
     dev_free(c->stage_rank);
     dev_free(c->bucket_counts);
     dev_free(c->ctl);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return LTPG_OK;
@@ -306,7 +309,8 @@ int ltpg_db_download(ltpg_ctx *c, uint32_t table, void *host, size_t bytes) {
 }
 
 // ---- batches ---------------------------------------------------------------------
-int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b) {
+namespace {
+int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream_t st) {
     Slot *s = get_slot(c, slot);
     if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
     if (!c->ycsb.rows) return fail(c, LTPG_ERR_STATE, "no YCSB table loaded");
@@ -328,12 +332,11 @@ int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b)
     }
     int r = ensure_outputs(c, *s, b->n_txn);
     if (r) return r;
-    CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, c->stream), "upload ops");
-    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, c->stream),
+    CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, st), "upload ops");
+    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, st),
        "upload val_off");
     if (b->n_updates)
-        CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, c->stream),
-           "upload vals");
+        CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, st), "upload vals");
     if (s->workload != LTPG_WORKLOAD_YCSB || s->n_txn != b->n_txn || s->k != b->ops_per_txn) drop_graphs(c);
     s->workload = LTPG_WORKLOAD_YCSB;
     s->n_txn = b->n_txn;
@@ -343,7 +346,7 @@ int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b)
     return LTPG_OK;
 }
 
-int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b) {
+int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream_t st) {
     Slot *s = get_slot(c, slot);
     if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
     if (!c->tpcc.W) return fail(c, LTPG_ERR_STATE, "no TPC-C tables loaded");
@@ -359,16 +362,17 @@ int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b)
     }
     int r = ensure_outputs(c, *s, b->n_txn);
     if (r) return r;
-    CK(cudaMemcpyAsync(s->txns, b->txns, (uint64_t)b->n_txn * sizeof(ltpg_tpcc_txn), cudaMemcpyHostToDevice,
-                       c->stream),
+    CK(cudaMemcpyAsync(s->txns, b->txns, (uint64_t)b->n_txn * sizeof(ltpg_tpcc_txn), cudaMemcpyHostToDevice, st),
        "upload txns");
     if (b->n_lines)
         CK(cudaMemcpyAsync(s->lines, b->lines, (uint64_t)b->n_lines * sizeof(ltpg_tpcc_line),
-                           cudaMemcpyHostToDevice, c->stream),
+                           cudaMemcpyHostToDevice, st),
            "upload lines");
     s->host_hdr[0] = b->n_lines;
     s->host_hdr[1] = b->txn_base;
-    CK(cudaMemcpyAsync(s->dev_hdr, s->host_hdr, sizeof s->host_hdr, cudaMemcpyHostToDevice, c->stream),
+    // pageable source: the runtime stages it before returning, so the next
+    // upload may overwrite host_hdr at once
+    CK(cudaMemcpyAsync(s->dev_hdr, s->host_hdr, sizeof s->host_hdr, cudaMemcpyHostToDevice, st),
        "upload slot header");
     if (s->workload != LTPG_WORKLOAD_TPCC || s->n_txn != b->n_txn) drop_graphs(c);
     s->workload = LTPG_WORKLOAD_TPCC;
@@ -376,6 +380,14 @@ int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b)
     s->n_lines = b->n_lines;
     s->txn_base = b->txn_base;
     return LTPG_OK;
+}
+}  // namespace
+
+int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b) {
+    return c ? upload_ycsb(c, slot, b, c->stream) : LTPG_ERR_INVALID;
+}
+int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b) {
+    return c ? upload_tpcc(c, slot, b, c->stream) : LTPG_ERR_INVALID;
 }
 
 }  // extern "C"
@@ -504,6 +516,56 @@ int ltpg_run_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int
            "bitmap download");
     }
     return ltpg_sync(c);
+}
+
+// Pipelined host calls: the batch is copied on the copy stream once the slot's
+// previous use is over, the run waits for the copy on the compute stream, and
+// the bitmap download follows the run; nothing blocks the caller, so the copy
+// of the next batch overlaps this one's kernels.
+extern "C++" {
+namespace {
+template <class Up>
+int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up upload) {
+    Slot *s = get_slot(c, slot);
+    if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "create copy stream");
+    if (!s->copied) CK(cudaEventCreateWithFlags(&s->copied, cudaEventDisableTiming), "create event");
+    if (!s->done) {
+        CK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming), "create event");
+        CK(cudaEventRecord(s->done, c->stream), "record event");
+    }
+    CK(cudaStreamWaitEvent(c->copy_stream, s->done, 0), "wait for the slot");
+    int r = upload(c->copy_stream);
+    if (r) return r;
+    CK(cudaEventRecord(s->copied, c->copy_stream), "record copy");
+    CK(cudaStreamWaitEvent(c->stream, s->copied, 0), "wait for the copy");
+    r = ltpg_run_batch(c, slot, mode);
+    if (r) return r;
+    if (host_bitmap)
+        CK(cudaMemcpyAsync(host_bitmap, s->bitmap, ((uint64_t)s->n_txn + 31) / 32 * 4, cudaMemcpyDeviceToHost,
+                           c->stream),
+           "bitmap download");
+    CK(cudaEventRecord(s->done, c->stream), "record done");
+    return LTPG_OK;
+}
+}  // namespace
+}  // extern "C++"
+
+int ltpg_submit_ycsb_host(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, int mode, uint32_t *host_bitmap) {
+    if (!c) return LTPG_ERR_INVALID;
+    return submit_host(c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_ycsb(c, slot, b, st); });
+}
+
+int ltpg_submit_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int mode, uint32_t *host_bitmap) {
+    if (!c) return LTPG_ERR_INVALID;
+    return submit_host(c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_tpcc(c, slot, b, st); });
+}
+
+int ltpg_host_wait(ltpg_ctx *c, uint32_t slot) {
+    Slot *s = get_slot(c, slot);
+    if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (s->done) CK(cudaEventSynchronize(s->done), "wait for the slot");
+    return check_device_error(c);
 }
 
 // ---- results -----------------------------------------------------------------

@@ -86,6 +86,9 @@ struct Slot {
     int64_t *results = nullptr;
     DevStats *stats = nullptr;
     uint64_t cap_out = 0;
+    // pipelined host calls: the batch's copy is done / the slot's last use
+    // (kernels and bitmap download) is done
+    cudaEvent_t copied = nullptr, done = nullptr;
 };
 
 struct LaunchCfg {
@@ -105,6 +108,7 @@ struct ltpg_ctx {
     int device = 0;
     ltpg_config cfg{};
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host-to-device copies of pipelined host calls
     cudaStream_t stream = nullptr;
     std::string err;
     ltpg::DevCtl *ctl = nullptr;

@@ -122,6 +122,58 @@ def test_ycsb_host_call_end_to_end(eng):
         assert np.array_equal(bits, o.run(b)[1])
 
 
+@pytest.mark.parametrize("mode", ["plain", "fused", "graph"])
+def test_pipelined_host_calls(eng, mode):
+    """ltpg_submit_*_host / ltpg_host_wait with three batches in flight: every
+    bitmap equals the oracle's, for YCSB and TPC-C, and a bad batch's error
+    comes back from its wait."""
+    from ltpg_gb300 import pinned_copy, pinned_empty
+    n, B, depth = 30000, 8000, 3
+    eng.load_ycsb(12, n)
+    o = oracle.YcsbOracle(12, n)
+    g = YcsbGenerator(12, n, B, 16, 5, 0.99, rotate_every=2)
+    batches = [pinned_copy(g.batch(i)) for i in range(7)]
+    bits = [pinned_empty((B + 31) // 32) for _ in range(depth)]
+    want = [o.run(b) for b in batches]
+    for i, b in enumerate(batches):
+        if i >= depth:
+            eng.host_wait(i % depth)
+            assert np.array_equal(bits[i % depth], want[i - depth][1]), i - depth
+        eng.submit_host(i % depth, b, mode, bits[i % depth])
+    for i in range(len(batches) - depth, len(batches)):
+        eng.host_wait(i % depth)
+        assert np.array_equal(bits[i % depth], want[i][1]), i
+        assert np.array_equal(eng.txn_flags(i % depth, B), want[i][0])
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+    # an out-of-range key: the error is reported by the wait
+    bad = g.batch(9)
+    ops = bad.ops.copy()
+    ops[0] = (ops[0] & ~np.uint32((1 << abi.YCSB_KEY_BITS) - 1)) | np.uint32(n + 5)
+    badb = pinned_copy(YcsbBatch(ops, bad.val_off, bad.vals, bad.n_txn, bad.ops_per_txn))
+    eng.submit_host(0, badb, mode, bits[0])
+    with pytest.raises(LtpgError) as ei:
+        eng.host_wait(0)
+    assert ei.value.code == abi.ERR_BOUNDS
+    eng.load_ycsb(12, n)  # the failed batch may have left partial state
+
+    W = 2
+    eng.load_tpcc(14, W)
+    to = oracle.TpccOracle(14, W)
+    tg = TpccGenerator(14, W, B, by_name_pct=60)
+    tb = [pinned_copy(tg.next()) for _ in range(5)]
+    twant = [to.run(b) for b in tb]
+    for i, b in enumerate(tb):
+        if i >= depth:
+            eng.host_wait(i % depth)
+            assert np.array_equal(bits[i % depth], twant[i - depth][1]), i - depth
+        eng.submit_host(i % depth, b, mode, bits[i % depth])
+    for i in range(len(tb) - depth, len(tb)):
+        eng.host_wait(i % depth)
+        assert np.array_equal(bits[i % depth], twant[i][1]), i
+    for t in range(abi.TPCC_TABLES):
+        assert np.array_equal(eng.download_table(t), to.tables[t]), t
+
+
 # ---- TPC-C --------------------------------------------------------------------------
 @pytest.fixture(scope="module")
 def eng_strict(gpu):
