@@ -654,6 +654,8 @@ def serving_section(args):
                              slots=4)
                 out[f"{rate / 1e6:g}M/s {'tuned' if mode != 'plain' else 'plain'}"] = {
                     "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "p999_ms": st["p999_ms"],
+                    "close_wait_ms": st["wait_ms"], "launch_ms_per_batch": st["launch_ms"],
+                    "device_ms_per_batch": st["device_ms"],
                     "committed_per_s": st["throughput"], "submitted": st["submitted"],
                     "commit_rate": st["committed"] / max(1, st["submitted"]), "batches": st["batches"],
                     "mean_batch": st["mean_batch"], "slot_waits": st["waited_for_slot"]}

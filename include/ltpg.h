@@ -392,6 +392,10 @@ typedef struct {
 typedef struct {
     uint64_t submitted, committed, batches, slots, waited_for_slot;
     double wall_s, throughput, mean_batch, mean_ms, p50_ms, p99_ms, p999_ms;
+    /* where latency goes: mean wait of a request until its batch closes,
+     * host time to pack and enqueue a batch, device time of a batch (copies,
+     * kernels, bitmap download; the longer of its TPC-C and YCSB parts) */
+    double wait_ms, launch_ms, device_ms;
 } ltpg_serve_stats;
 typedef struct ltpg_serve_record ltpg_serve_record;
 int ltpg_serve_run(ltpg_ctx *tpcc_ctx, ltpg_ctx *ycsb_ctx, const ltpg_serve_cfg *cfg, const ltpg_tpcc_params *tp,

@@ -73,7 +73,8 @@ class ServeStatsC(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("committed", C.c_uint64), ("batches", C.c_uint64),
                 ("slots", C.c_uint64), ("waited_for_slot", C.c_uint64), ("wall_s", C.c_double),
                 ("throughput", C.c_double), ("mean_batch", C.c_double), ("mean_ms", C.c_double),
-                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double)]
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double),
+                ("wait_ms", C.c_double), ("launch_ms", C.c_double), ("device_ms", C.c_double)]
 
 
 class StatsC(C.Structure):

@@ -49,7 +49,10 @@ struct Pinned {
 struct SlotState {
     bool busy = false;
     cudaEvent_t done_c = nullptr, done_y = nullptr;
+    cudaEvent_t start = nullptr;  // recorded when the batch is handed to the engines
+    double t_close = 0;           // host time the batch closed
     uint64_t c_start = 0, c_count = 0, y_start = 0, y_count = 0;
+    uint64_t c_packed = 0, y_packed = 0;  // requests of the forming batch already in the staging buffers
     double arrival_first = 0;
     Pinned c_txns, c_lines, y_ops, y_voff, y_vals;   // host staging of the batch
     Pinned c_bits, y_bits, c_flags, y_flags, c_res, y_res;
@@ -173,8 +176,9 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     cudaStreamCreateWithFlags(&cs_y, cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&cp_y, cudaStreamNonBlocking);
     for (auto &s : slots) {
-        cudaEventCreateWithFlags(&s.done_c, cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&s.done_y, cudaEventDisableTiming);
+        cudaEventCreate(&s.done_c);
+        cudaEventCreate(&s.done_y);
+        cudaEventCreate(&s.start);
     }
     // pinned staging for the largest batch, reserved before the clock starts
     for (auto &s : slots) {
@@ -199,6 +203,7 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     }
     std::vector<double> lat;  // committed requests' latencies (ms)
     lat.reserve(N);
+    double wait_sum = 0, pack_sum = 0, dev_sum = 0;  // latency parts (s): close wait per request, per batch
     std::vector<double> arr_c(n_c), arr_y(n_y);
     {
         uint64_t ic = 0, iy = 0;
@@ -215,6 +220,11 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     auto now_s = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
 
     auto complete = [&](SlotState &s, double t_done) {
+        float ms_c = 0.f, ms_y = 0.f;
+        cudaEventElapsedTime(&ms_c, s.start, s.done_c);
+        cudaEventElapsedTime(&ms_y, s.start, s.done_y);
+        dev_sum += std::max(ms_c, ms_y) * 1e-3;
+        (void)t_done;
         // latency of every committed request of the batch
         const uint32_t *bc = static_cast<const uint32_t *>(s.c_bits.p);
         const uint32_t *by = static_cast<const uint32_t *>(s.y_bits.p);
@@ -237,21 +247,44 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         s.busy = false;
     };
 
+    // Packs pool requests [c_start + c_packed, c_end) and [y_start + y_packed,
+    // y_end) into the slot's pinned staging: called as requests are admitted,
+    // so a batch is mostly packed when it closes.
+    auto pack_upto = [&](SlotState &s, uint64_t c_end, uint64_t y_end) {
+        const uint64_t c_from = s.c_start + s.c_packed;
+        if (c_end > c_from) {
+            const uint64_t l0 = c_line_off[s.c_start];
+            ltpg_tpcc_txn *tx = static_cast<ltpg_tpcc_txn *>(s.c_txns.p);
+            for (uint64_t i = c_from; i < c_end; ++i) {
+                tx[i - s.c_start] = c_pool[i];
+                tx[i - s.c_start].line_off = (uint32_t)(c_line_off[i] - l0);
+            }
+            memcpy(static_cast<ltpg_tpcc_line *>(s.c_lines.p) + (c_line_off[c_from] - l0), c_lines.data() + c_line_off[c_from],
+                   (c_line_off[c_end] - c_line_off[c_from]) * 8);
+            s.c_packed = c_end - s.c_start;
+        }
+        const uint64_t y_from = s.y_start + s.y_packed;
+        if (y_end > y_from) {
+            const uint64_t v0 = y_voff[s.y_start];
+            memcpy(static_cast<uint32_t *>(s.y_ops.p) + (y_from - s.y_start) * sy, y_ops.data() + y_from * sy,
+                   (y_end - y_from) * sy * 4);
+            uint32_t *vo = static_cast<uint32_t *>(s.y_voff.p);
+            for (uint64_t i = y_from; i < y_end; ++i) vo[i - s.y_start] = (uint32_t)(y_voff[i] - v0);
+            memcpy(static_cast<uint64_t *>(s.y_vals.p) + (y_voff[y_from] - v0), y_vals.data() + y_voff[y_from],
+                   (y_voff[y_end] - y_voff[y_from]) * 8);
+            s.y_packed = y_end - s.y_start;
+        }
+    };
+
+    // Hands a closed, packed batch to the two engines.
     auto launch = [&](SlotState &s, uint32_t slot_idx) -> int {
-        // ---- TPC-C sub-batch: records and lines from the pool, line offsets rebased
         const uint64_t nc = s.c_count, ny = s.y_count;
+        pack_upto(s, s.c_start + nc, s.y_start + ny);
+        cudaEventRecord(s.start, cp_c);
+        // ---- TPC-C sub-batch
         if (nc) {
             const uint64_t l0 = c_line_off[s.c_start], l1 = c_line_off[s.c_start + nc];
-            if (!s.c_txns.reserve(nc * sizeof(ltpg_tpcc_txn)) || !s.c_lines.reserve((l1 - l0 + 1) * 8) ||
-                !s.c_bits.reserve((nc + 31) / 32 * 4) || !s.c_flags.reserve(nc) || !s.c_res.reserve(nc * 8))
-                return LTPG_ERR_NOMEM;
-            ltpg_tpcc_txn *tx = static_cast<ltpg_tpcc_txn *>(s.c_txns.p);
-            for (uint64_t i = 0; i < nc; ++i) {
-                tx[i] = c_pool[s.c_start + i];
-                tx[i].line_off = (uint32_t)(c_line_off[s.c_start + i] - l0);
-            }
-            memcpy(s.c_lines.p, c_lines.data() + l0, (l1 - l0) * 8);
-            ltpg_tpcc_batch b{(uint32_t)nc, (uint32_t)(l1 - l0), s.c_start, tx,
+            ltpg_tpcc_batch b{(uint32_t)nc, (uint32_t)(l1 - l0), s.c_start, static_cast<ltpg_tpcc_txn *>(s.c_txns.p),
                               static_cast<ltpg_tpcc_line *>(s.c_lines.p)};
             ltpg_set_stream(tc, cp_c);
             int r = ltpg_batch_upload_tpcc(tc, slot_idx, &b);
@@ -272,13 +305,8 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         // ---- YCSB sub-batch
         if (ny) {
             const uint64_t v0 = y_voff[s.y_start], v1 = y_voff[s.y_start + ny];
-            if (!s.y_ops.reserve(ny * sy * 4) || !s.y_voff.reserve((ny + 1) * 4) || !s.y_vals.reserve((v1 - v0 + 1) * 8) ||
-                !s.y_bits.reserve((ny + 31) / 32 * 4) || !s.y_flags.reserve(ny) || !s.y_res.reserve(ny * 8))
-                return LTPG_ERR_NOMEM;
-            memcpy(s.y_ops.p, y_ops.data() + s.y_start * sy, ny * sy * 4);
             uint32_t *vo = static_cast<uint32_t *>(s.y_voff.p);
-            for (uint64_t i = 0; i <= ny; ++i) vo[i] = (uint32_t)(y_voff[s.y_start + i] - v0);
-            memcpy(s.y_vals.p, y_vals.data() + v0, (v1 - v0) * 8);
+            vo[ny] = (uint32_t)(v1 - v0);
             ltpg_ycsb_batch b{(uint32_t)ny, ky, sy, (uint32_t)(v1 - v0), static_cast<uint32_t *>(s.y_ops.p), vo,
                               static_cast<uint64_t *>(s.y_vals.p)};
             ltpg_set_stream(yc, cp_y);
@@ -298,6 +326,7 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         }
         cudaEventRecord(s.done_y, cs_y);
         s.busy = true;
+        s.c_packed = s.y_packed = 0;
         if (rec) {
             rec->batches.push_back(s.c_start);
             rec->batches.push_back(nc);
@@ -307,7 +336,9 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         return LTPG_OK;
     };
 
-    uint32_t rr = 0;  // next slot in round-robin order (batches complete in order)
+    uint32_t rr = 0;           // next slot in round-robin order (batches complete in order)
+    uint64_t form_c = 0;       // TPC-C requests in the forming batch (the rest are YCSB)
+    bool form_packing = false; // the forming batch is being packed into slots[rr]
     while (rc == LTPG_OK) {
         const double t = now_s();
         // completions
@@ -319,9 +350,23 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         }
         // admission: requests that have arrived join the forming batch
         uint64_t form_end = next;
-        while (form_end < N && arrival[form_end] <= t && form_end - form_start < cfg->max_batch) ++form_end;
+        while (form_end < N && arrival[form_end] <= t && form_end - form_start < cfg->max_batch) {
+            form_c += is_tpcc[form_end];
+            ++form_end;
+        }
         next = form_end;
         const uint64_t size = next - form_start;
+        // pack the admitted requests now if the forming batch's slot is free
+        SlotState &fs = slots[rr];
+        if (!fs.busy && size > 0) {
+            if (!form_packing) {
+                fs.c_start = pos_c;
+                fs.y_start = pos_y;
+                fs.c_packed = fs.y_packed = 0;
+                form_packing = true;
+            }
+            pack_upto(fs, pos_c + form_c, pos_y + (size - form_c));
+        }
         const bool full = size >= cfg->max_batch;
         const bool due = size > 0 && t - arrival[form_start] >= deadline;
         const bool drain = next >= N && size > 0;
@@ -330,19 +375,26 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
             if (s.busy) {
                 ++waited_for_slot;  // all slots in flight: the batch keeps forming
             } else {
-                uint64_t nc = 0;
-                for (uint64_t i = form_start; i < next; ++i) nc += is_tpcc[i];
+                const uint64_t nc = form_c;
+                if (!form_packing) {
+                    s.c_packed = s.y_packed = 0;
+                }
                 s.c_start = pos_c;
                 s.c_count = nc;
                 s.y_start = pos_y;
                 s.y_count = size - nc;
                 s.arrival_first = arrival[form_start];
+                s.t_close = t;
+                for (uint64_t i = form_start; i < next; ++i) wait_sum += t - arrival[i];
                 pos_c += nc;
                 pos_y += size - nc;
                 rc = launch(s, rr);
+                pack_sum += now_s() - t;
                 batches++;
                 batch_sizes += (double)size;
                 form_start = next;
+                form_c = 0;
+                form_packing = false;
                 rr = (rr + 1) % allowed;
             }
         }
@@ -360,6 +412,7 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     for (auto &s : slots) {
         cudaEventDestroy(s.done_c);
         cudaEventDestroy(s.done_y);
+        cudaEventDestroy(s.start);
     }
     cudaEventDestroy(up_c);
     cudaEventDestroy(up_y);
@@ -386,6 +439,9 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     out->p50_ms = percentile(lat, 0.50);
     out->p99_ms = percentile(lat, 0.99);
     out->p999_ms = percentile(lat, 0.999);
+    out->wait_ms = N ? wait_sum * 1e3 / N : 0;
+    out->launch_ms = batches ? pack_sum * 1e3 / batches : 0;
+    out->device_ms = batches ? dev_sum * 1e3 / batches : 0;
     if (record) *record = rec;
     return rc;
 }
