@@ -43,6 +43,10 @@ WORKLOADS = {
                        name="YCSB small: 1M x 10 uint64, 65,536 txn x 10 ops, 50/50, Zipf theta=0.6"),
     "tpcc": dict(kind="tpcc", warehouses=64, n_txn=1 << 20, n_batches=8,
                  name="TPC-C NewOrder+Payment 50/50, W=64, 1,048,576 txn per batch"),
+    "tpcc_mix": dict(kind="tpcc", warehouses=64, n_txn=1 << 20, n_batches=8,
+                     mix=dict(neworder_pct=45, orderstatus_pct=4, delivery_pct=4, stocklevel_pct=4, by_name_pct=60),
+                     name="TPC-C five-transaction mix 45/43/4/4/4 (customers by last name 60 %), W=64, "
+                          "1,048,576 txn per batch"),
     "tpcc_prof": dict(kind="tpcc", warehouses=16, n_txn=1 << 18, n_batches=4,
                       name="TPC-C NewOrder+Payment 50/50, profiling size: W=16, 262,144 txn per batch"),
 }
@@ -343,7 +347,7 @@ def cpu_baseline_ycsb(w, batches, n_batches, threads=1):
 def tpcc_bench(args, w, dist, want_extras=True):
     import torch
     import ltpg_gb300 as L
-    g = L.TpccGenerator(SEED, w["warehouses"], w["n_txn"])
+    g = L.TpccGenerator(SEED, w["warehouses"], w["n_txn"], **w.get("mix", {}))
     batches = [g.next() for _ in range(w["n_batches"])]
     n_slots = len(batches)
     max_lines = max(b.n_lines for b in batches)
@@ -508,7 +512,7 @@ def reference_arm(args, w, rank):
     else:
         import oracle
         from ltpg_gb300 import TpccGenerator
-        g = TpccGenerator(SEED, w["warehouses"], w["n_txn"])
+        g = TpccGenerator(SEED, w["warehouses"], w["n_txn"], **w.get("mix", {}))
         nb = 2
         batches = [g.next() for _ in range(nb)]
         o = oracle.TpccOracle(SEED, w["warehouses"])
@@ -578,7 +582,7 @@ def main():
         kernel, kbytes, kms = (ek, eb, exec_ms) if exec_ms >= cwb_ms else ("ycsb_checkwb_tuned", cb, cwb_ms)
     else:
         # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
-        eb, cb = tpcc_bytes_per_txn()
+        eb, cb = tpcc_bytes_per_txn(w.get("mix"))
         kernel, kbytes, kms = ("tpcc_exec_tuned", eb, exec_ms) if exec_ms >= cwb_ms else \
             ("tpcc_checkwb_tuned", cb, cwb_ms)
     achieved = kbytes * B / (kms / 1e3) / 1e9 if kms > 0 else None
@@ -699,24 +703,31 @@ def predictor_section(w, batches):
     return out
 
 
-def tpcc_bytes_per_txn():
-    """Algorithmic bytes per TPC-C transaction (50/50 NewOrder/Payment, 10 lines
-    on average).  Only ops that can conflict register and check: no NewOrder or
-    Payment writes a WAREHOUSE, DISTRICT or ITEM row through registration, so
-    NewOrder has 3 + 2 per line (customer read, NEW-ORDER and ORDER inserts,
-    stock write, ORDER-LINE insert) and Payment 3 (customer read and write,
-    HISTORY insert).  Execute: 32 B record + 8 B per line, 16 B registration per
-    op, reads W/D tax, C discount, item price (8 B each).  Check+write-back:
-    record and lines again, 16 B slot load per op, committed writes (NewOrder:
-    ORDER 64, NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE 80 + price
-    and dist reads 16; Payment: 2 hot adds 16, customer 3x8 read+write,
-    HISTORY 64)."""
-    no_ops, pay_ops = 3 + 2 * 10, 3
-    ex_no = 32 + 80 + 16 * no_ops + 24 + 8 * 10 + 8
-    ex_pay = 32 + 16 * pay_ops + 8 + 8
-    cw_no = 32 + 80 + 16 * no_ops + 64 + 24 + 10 * (64 + 80 + 16) + 2
-    cw_pay = 32 + 16 * pay_ops + 16 + 48 + 64 + 2
-    return (ex_no + ex_pay) / 2, (cw_no + cw_pay) / 2
+def tpcc_bytes_per_txn(mix=None):
+    """Algorithmic bytes per TPC-C transaction (10 lines per NewOrder on
+    average), weighted by the workload's mix (default 50/50 NewOrder/Payment).
+    Only ops that can conflict register and check: no transaction writes a
+    WAREHOUSE, DISTRICT or ITEM row through registration, so NewOrder has 3 + 2
+    per line (customer read, NEW-ORDER and ORDER inserts, stock write,
+    ORDER-LINE insert), Payment 3 (customer read and write, HISTORY insert),
+    OrderStatus 3 reads, Delivery 4 (two of them read and write their row),
+    StockLevel 1.  Execute: 32 B record + 8 B per line, 16 B registration per
+    op (Delivery's read-and-write rows: 32), reads W/D tax, C discount, item
+    price, balance, OL_AMOUNT, S_QUANTITY (8 B each).  Check+write-back: record
+    and lines again, 16 B slot load per op, committed writes (NewOrder: ORDER
+    64, NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE 80 + price and
+    dist reads 16; Payment: 2 hot adds 16, customer 3x8 read+write, HISTORY 64;
+    Delivery: NEW-ORDER 24, carrier 8, delivery date 8, customer 2x8 read+write)."""
+    mix = mix or {}
+    no = mix.get("neworder_pct", 50)
+    os_, dl, sl = mix.get("orderstatus_pct", 0), mix.get("delivery_pct", 0), mix.get("stocklevel_pct", 0)
+    pay = 100 - no - os_ - dl - sl
+    ex = {"no": 32 + 80 + 16 * 23 + 24 + 8 * 10 + 8, "pay": 32 + 16 * 3 + 8 + 8, "os": 32 + 16 * 3 + 8,
+          "dl": 32 + 16 * 6 + 8, "sl": 32 + 16 + 8}
+    cw = {"no": 32 + 80 + 16 * 23 + 64 + 24 + 10 * (64 + 80 + 16) + 2, "pay": 32 + 16 * 3 + 16 + 48 + 64 + 2,
+          "os": 32 + 16 * 3 + 2, "dl": 32 + 16 * 4 + 24 + 8 + 8 + 32 + 2, "sl": 32 + 16 + 2}
+    share = {"no": no, "pay": pay, "os": os_, "dl": dl, "sl": sl}
+    return (sum(ex[k] * share[k] for k in ex) / 100.0, sum(cw[k] * share[k] for k in cw) / 100.0)
 
 
 if __name__ == "__main__":

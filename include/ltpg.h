@@ -118,6 +118,9 @@ typedef struct {
 
 #define LTPG_TPCC_NEWORDER 0
 #define LTPG_TPCC_PAYMENT 1
+#define LTPG_TPCC_ORDERSTATUS 2
+#define LTPG_TPCC_DELIVERY 3
+#define LTPG_TPCC_STOCKLEVEL 4
 #define LTPG_TPCC_MAX_LINES 15
 
 /* 32-byte transaction record.  kind_info: bits 0..7 kind, 8..15 order-line
@@ -130,7 +133,20 @@ typedef struct {
  * nth (0-based) one of district (c_w, customer district) whose C_LAST column
  * equals name, in C_ID order; it replaces the reference's KERNEL_CID /
  * __FIND_CID_INDEX pre-phase (TF/tp.cu:11-23, TF/Genericfunction.h:29-77).
- * line_off = number of order lines of all earlier transactions of the batch. */
+ * line_off = number of order lines of all earlier transactions of the batch.
+ *
+ * The other three TPC-C transactions follow the reference's all-transaction
+ * variant (TA/Execute.h:1592-2231: one customer / order / order line, one
+ * stock row), with the row keys computed from the record:
+ *   OrderStatus: reads customer (c_w, customer district, c_id — by name with
+ *     LTPG_PAY_BY_NAME as for Payment), ORDER row a and ORDER-LINE row b of
+ *     warehouse w; result = C_BALANCE.
+ *   Delivery: deletes NEW-ORDER row b of warehouse w (every column set to all
+ *     ones), sets O_CARRIER_ID of ORDER row a (carrier in bits 8..15, 1..10)
+ *     and OL_DELIVERY_D of ORDER-LINE row c, and credits customer (w,
+ *     district, c_id) with that line's OL_AMOUNT (C_BALANCE +=, C_DELIVERY_CNT
+ *     += 1); result = the amount.
+ *   StockLevel: reads STOCK row a of warehouse w; result = S_QUANTITY. */
 #define LTPG_PAY_BY_NAME 0x100u
 typedef struct {
     uint32_t kind_info;
@@ -164,9 +180,12 @@ typedef struct {
     uint32_t neworder_pct; /* share of NewOrder, rest Payment         */
     uint32_t remote_line_pct; /* NewOrder remote supply, per line (1)  */
     uint32_t remote_pay_pct;  /* Payment remote customer (15)          */
-    uint32_t by_name_pct;     /* Payment by last name (0; TPC-C: 60)  */
+    uint32_t by_name_pct;     /* Payment / OrderStatus by last name (0; TPC-C: 60) */
     uint64_t table_seed;      /* seed of the loaded tables: by-name queries
                                  name the customer a by-id Payment would pick */
+    /* shares of OrderStatus, Delivery, StockLevel, taken from the non-NewOrder
+     * share (0 each: NewOrder + Payment only; TPC-C mix: 45/43/4/4/4) */
+    uint32_t orderstatus_pct, delivery_pct, stocklevel_pct, pad;
 } ltpg_tpcc_params;
 
 /* ---- engine context ---------------------------------------------------- */

@@ -188,11 +188,14 @@ class TpccGenerator:
     """Deterministic, stateful TPC-C NewOrder/Payment batches (draw in order)."""
 
     def __init__(self, seed, warehouses, n_txn, neworder_pct=50, remote_line_pct=1, remote_pay_pct=15,
-                 by_name_pct=0, table_seed=None):
-        """by_name_pct: share of Payments that name their customer by last name;
-        table_seed: seed the tables were loaded with (default: seed)."""
+                 by_name_pct=0, table_seed=None, orderstatus_pct=0, delivery_pct=0, stocklevel_pct=0):
+        """by_name_pct: share of Payments / OrderStatus that name their customer
+        by last name; table_seed: seed the tables were loaded with (default:
+        seed); orderstatus / delivery / stocklevel_pct: shares of the other three
+        TPC-C transactions, taken from Payment's."""
         self.params = abi.TpccParamsC(seed, warehouses, n_txn, neworder_pct, remote_line_pct, remote_pay_pct,
-                                      by_name_pct, seed if table_seed is None else table_seed)
+                                      by_name_pct, seed if table_seed is None else table_seed, orderstatus_pct,
+                                      delivery_pct, stocklevel_pct, 0)
         h = C.c_void_p()
         _check(lib().ltpg_gen_create_tpcc(C.byref(self.params), C.byref(h)))
         self._h = h
@@ -441,7 +444,8 @@ def serve(tpcc_engine, ycsb_engine, rate, duration_s, tpcc_params, ycsb_params, 
     tp = abi.TpccParamsC(tpcc_params["seed"], tpcc_params["warehouses"], tpcc_params.get("n_txn", 262144),
                          tpcc_params.get("neworder_pct", 50), tpcc_params.get("remote_line_pct", 1),
                          tpcc_params.get("remote_pay_pct", 15), tpcc_params.get("by_name_pct", 0),
-                         tpcc_params.get("table_seed", tpcc_params["seed"]))
+                         tpcc_params.get("table_seed", tpcc_params["seed"]), tpcc_params.get("orderstatus_pct", 0),
+                         tpcc_params.get("delivery_pct", 0), tpcc_params.get("stocklevel_pct", 0), 0)
     yp = abi.YcsbParamsC(ycsb_params["seed"], ycsb_params["n_records"], ycsb_params.get("n_txn", 262144),
                          ycsb_params.get("ops_per_txn", 10), ycsb_params.get("update_pct", 50),
                          ycsb_params.get("rotate_every", 0), ycsb_params.get("theta", 0.9))

@@ -16,7 +16,7 @@ TABLE_YCSB = 100
 T_WAREHOUSE, T_DISTRICT, T_CUSTOMER, T_HISTORY, T_NEWORDER, T_ORDER, T_ORDERLINE, T_STOCK, T_ITEM = range(9)
 TPCC_TABLES = 9
 TPCC_COLS = (9, 11, 21, 8, 3, 8, 10, 17, 5)
-TPCC_NEWORDER, TPCC_PAYMENT = 0, 1
+TPCC_NEWORDER, TPCC_PAYMENT, TPCC_ORDERSTATUS, TPCC_DELIVERY, TPCC_STOCKLEVEL = 0, 1, 2, 3, 4
 TPCC_MAX_LINES = 15
 CFG_STRICT_INSERT = 1
 CFG_REF_NAME_LOOKUP = 2
@@ -45,7 +45,8 @@ class TpccBatchC(C.Structure):
 class TpccParamsC(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("warehouses", C.c_uint32), ("n_txn", C.c_uint32),
                 ("neworder_pct", C.c_uint32), ("remote_line_pct", C.c_uint32), ("remote_pay_pct", C.c_uint32),
-                ("by_name_pct", C.c_uint32), ("table_seed", C.c_uint64)]
+                ("by_name_pct", C.c_uint32), ("table_seed", C.c_uint64), ("orderstatus_pct", C.c_uint32),
+                ("delivery_pct", C.c_uint32), ("stocklevel_pct", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class ConfigC(C.Structure):

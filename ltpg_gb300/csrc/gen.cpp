@@ -119,6 +119,13 @@ struct ltpg_gen {
     // rank among the customers of its district with that name, in C_ID order.
     std::vector<uint16_t> cust_name;
     std::vector<uint8_t> cust_rank;
+    // OrderStatus / Delivery: the orders this generator made, per warehouse
+    // (indexed by O_ID): customer, district, first OL_ID, line count; how many
+    // were made and delivered.
+    std::vector<uint16_t> o_cust;
+    std::vector<uint8_t> o_dist, o_cnt;
+    std::vector<uint32_t> o_ol;
+    std::vector<uint64_t> made, delivered;
     uint64_t next_batch = 0, txn_base = 0;
 };
 
@@ -147,6 +154,8 @@ int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out) {
     if (p->warehouses == 0 || p->warehouses > 65535 || p->n_txn == 0) return LTPG_ERR_INVALID;
     if (p->neworder_pct > 100 || p->remote_line_pct > 100 || p->remote_pay_pct > 100 || p->by_name_pct > 100)
         return LTPG_ERR_INVALID;
+    if ((uint64_t)p->neworder_pct + p->orderstatus_pct + p->delivery_pct + p->stocklevel_pct > 100)
+        return LTPG_ERR_INVALID;
     ltpg_gen *g = new (std::nothrow) ltpg_gen();
     if (!g) return LTPG_ERR_NOMEM;
     g->kind = LTPG_WORKLOAD_TPCC;
@@ -155,6 +164,15 @@ int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out) {
     g->no_id.assign(p->warehouses, 0);
     g->ol_id.assign(p->warehouses, 0);
     g->h_id.assign(p->warehouses, 0);
+    if (p->orderstatus_pct || p->delivery_pct) {
+        const size_t n = 30000ull * p->warehouses;
+        g->o_cust.assign(n, 0);
+        g->o_dist.assign(n, 0);
+        g->o_cnt.assign(n, 0);
+        g->o_ol.assign(n, 0);
+        g->made.assign(p->warehouses, 0);
+        g->delivered.assign(p->warehouses, 0);
+    }
     if (p->by_name_pct) {
         // names of the initial image (tpcc_init_value: C_LAST < 1000)
         const uint64_t n = 30000ull * p->warehouses;
@@ -286,9 +304,79 @@ int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
         ltpg_tpcc_txn &x = txns[t];
         memset(&x, 0, sizeof x);
         x.line_off = nl;
-        const bool is_no = r.below(100) < p.neworder_pct;
+        // kind: NewOrder, then OrderStatus, Delivery, StockLevel, else Payment
+        const uint32_t u = (uint32_t)r.below(100);
+        const bool is_no = u < p.neworder_pct;
+        const uint32_t c_os = p.neworder_pct + p.orderstatus_pct, c_dl = c_os + p.delivery_pct,
+                       c_sl = c_dl + p.stocklevel_pct;
         const uint32_t w = (uint32_t)r.below(W), d = (uint32_t)r.below(10);
         x.w = w;
+        const bool tracking = !g->made.empty();
+        // by last name (TF/Query.h:174-181): the query names customer (cw, cd,
+        // c) by its C_LAST and its rank among that name's holders
+        auto by_name = [&](uint32_t cw, uint32_t cd) {
+            if (p.by_name_pct && r.below(100) < p.by_name_pct) {
+                const uint64_t row = 30000ull * cw + 3000ull * cd + x.c_id;
+                if (g->cust_rank[row] < 255u) {
+                    x.kind_info |= LTPG_PAY_BY_NAME;
+                    x.c_id = ((uint32_t)g->cust_name[row] << 8) | g->cust_rank[row];
+                }
+            }
+        };
+        if (!is_no && u < c_os) {
+            // OrderStatus (TA/Query.h:214-246): a recent order of warehouse w
+            // and one of its lines, read with its customer
+            uint32_t cd = d, o, ol;
+            if (tracking && g->made[w]) {
+                const uint64_t back = r.below(std::min<uint64_t>(g->made[w], 1000));
+                o = (uint32_t)((g->o_id[w] + 30000u - 1u - (uint32_t)back) % 30000u);
+                const size_t k = 30000ull * w + o;
+                cd = g->o_dist[k];
+                x.c_id = g->o_cust[k];
+                ol = (uint32_t)((g->o_ol[k] + r.below(std::max<uint32_t>(1u, g->o_cnt[k]))) % 450000u);
+            } else {
+                x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
+                o = (uint32_t)r.below(30000);
+                ol = (uint32_t)r.below(450000);
+            }
+            x.kind_info = LTPG_TPCC_ORDERSTATUS | (cd << 16) | (cd << 24);
+            x.c_w = w;
+            x.a = o;
+            x.b = ol;
+            by_name(w, cd);
+            continue;
+        }
+        if (!is_no && u < c_dl) {
+            // Delivery (TA/Query.h:247-269): the oldest undelivered order of w
+            uint32_t cd = d, o, ol;
+            if (tracking && g->delivered[w] < g->made[w]) {
+                if (g->made[w] - g->delivered[w] > 30000u) g->delivered[w] = g->made[w] - 30000u;
+                o = (uint32_t)(g->delivered[w]++ % 30000u);
+                const size_t k = 30000ull * w + o;
+                cd = g->o_dist[k];
+                x.c_id = g->o_cust[k];
+                ol = g->o_ol[k];
+            } else {
+                x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
+                o = (uint32_t)r.below(30000);
+                ol = (uint32_t)r.below(450000);
+            }
+            const uint32_t carrier = (uint32_t)r.range(1, 10);
+            x.kind_info = LTPG_TPCC_DELIVERY | (carrier << 8) | (cd << 16);
+            x.c_w = w;
+            x.a = o;
+            x.b = o;  // NO_ID and O_ID advance together (TF/Query.h:54-88)
+            x.c = ol;
+            continue;
+        }
+        if (!is_no && u < c_sl) {
+            // StockLevel (TA/Query.h:270-296): one stock row of w
+            const uint32_t threshold = (uint32_t)r.range(10, 20);
+            x.kind_info = LTPG_TPCC_STOCKLEVEL | (threshold << 8) | (d << 16);
+            x.c_w = w;
+            x.a = (uint32_t)nurand(r, 8191, 1, 100000) - 1;
+            continue;
+        }
         if (is_no) {
             const uint32_t cnt = (uint32_t)r.range(5, LTPG_TPCC_MAX_LINES);
             x.kind_info = LTPG_TPCC_NEWORDER | (cnt << 8) | (d << 16);
@@ -300,6 +388,14 @@ int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
             g->no_id[w] = (g->no_id[w] + 1) % 30000u;
             x.c = g->ol_id[w];
             g->ol_id[w] = (g->ol_id[w] + cnt) % 450000u;
+            if (tracking) {
+                const size_t k = 30000ull * w + x.a;
+                g->o_cust[k] = (uint16_t)x.c_id;
+                g->o_dist[k] = (uint8_t)d;
+                g->o_ol[k] = x.c;
+                g->o_cnt[k] = (uint8_t)cnt;
+                g->made[w]++;
+            }
             for (uint32_t i = 0; i < cnt; ++i) {
                 ltpg_tpcc_line &ln = lines[nl + i];
                 uint32_t item;
@@ -330,15 +426,7 @@ int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
             g->h_id[w] = (g->h_id[w] + 1) % 30000u;
             x.b = (uint32_t)amount;
             x.c = (uint32_t)(amount >> 32);
-            // by last name (TF/Query.h:174-181): the query names the customer
-            // drawn above by its C_LAST and its rank among that name's holders
-            if (p.by_name_pct && r.below(100) < p.by_name_pct) {
-                const uint64_t row = 30000ull * c_w + 3000ull * c_d + x.c_id;
-                if (g->cust_rank[row] < 255u) {
-                    x.kind_info |= LTPG_PAY_BY_NAME;
-                    x.c_id = ((uint32_t)g->cust_name[row] << 8) | g->cust_rank[row];
-                }
-            }
+            by_name(c_w, c_d);
         }
     }
     out->n_txn = p.n_txn;

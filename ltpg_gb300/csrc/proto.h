@@ -118,13 +118,41 @@ constexpr uint32_t OPF_WRITE = OPF_REG_W | OPF_CHK_WAR | OPF_CHK_WAW;
 // (TF/Execute_neworder.h:115) and, because check_3_0 is never dispatched
 // (TF/Execute_neworder.h:639-646), checked only for WAW (check_3_1, :478-490).
 constexpr uint32_t OPF_NO_INSERT_COMPAT = OPF_REG_R | OPF_CHK_WAW;
+// A row read and then updated by one transaction (the reference registers and
+// checks it as a read op and a write op of the same row, TA/Execute.h:1772-2153).
+constexpr uint32_t OPF_RW = OPF_READ | OPF_WRITE;
 
 LTPG_HD uint32_t tpcc_kind(uint32_t kind_info) { return kind_info & 0xFFu; }
 LTPG_HD uint32_t tpcc_ol_cnt(uint32_t kind_info) { return (kind_info >> 8) & 0xFFu; }
 LTPG_HD uint32_t tpcc_d(uint32_t kind_info) { return (kind_info >> 16) & 0xFFu; }
 LTPG_HD uint32_t tpcc_c_d(uint32_t kind_info) { return (kind_info >> 24) & 0xFFu; }
 LTPG_HD uint32_t tpcc_n_ops(uint32_t kind_info) {
-    return tpcc_kind(kind_info) == LTPG_TPCC_NEWORDER ? 5u + 3u * tpcc_ol_cnt(kind_info) : 5u;
+    switch (tpcc_kind(kind_info)) {
+    case LTPG_TPCC_NEWORDER: return 5u + 3u * tpcc_ol_cnt(kind_info);
+    case LTPG_TPCC_PAYMENT: return 5u;
+    case LTPG_TPCC_ORDERSTATUS: return 3u;
+    case LTPG_TPCC_DELIVERY: return 4u;
+    default: return 1u;
+    }
+}
+// Ops that can conflict, apart from order lines (the tuned kernels' header
+// ops): reads of WAREHOUSE, DISTRICT and ITEM rows never can (no transaction
+// registers a write there), so NewOrder and Payment keep ops j = 2, 3, 4 and
+// the other kinds all of theirs.
+LTPG_HD uint32_t tpcc_n_head(uint32_t kind_info) {
+    switch (tpcc_kind(kind_info)) {
+    case LTPG_TPCC_DELIVERY: return 4u;
+    case LTPG_TPCC_STOCKLEVEL: return 1u;
+    default: return 3u;
+    }
+}
+LTPG_HD uint32_t tpcc_head_j(uint32_t kind_info, uint32_t k) {
+    const uint32_t kind = tpcc_kind(kind_info);
+    return (kind == LTPG_TPCC_NEWORDER || kind == LTPG_TPCC_PAYMENT) ? k + 2u : k;
+}
+LTPG_HD bool tpcc_customer_by_name(uint32_t kind_info) {
+    const uint32_t kind = tpcc_kind(kind_info);
+    return (kind == LTPG_TPCC_PAYMENT || kind == LTPG_TPCC_ORDERSTATUS) && (kind_info & LTPG_PAY_BY_NAME);
 }
 // First concurrency-control op of transaction t: NewOrder has 5 + 3 per line,
 // Payment 5, so the offset follows from t and the line prefix alone.
@@ -167,6 +195,24 @@ LTPG_HD TpccOp tpcc_op(const ltpg_tpcc_txn &x, uint32_t j, const ltpg_tpcc_line 
         return op;
     }
     const uint32_t c_d = tpcc_c_d(x.kind_info);
+    switch (tpcc_kind(x.kind_info)) {
+    case LTPG_TPCC_ORDERSTATUS:  // TA/Execute.h:1592-1770
+        if (j == 0) { op.table = LTPG_T_CUSTOMER; op.row = tpcc_cust_row(x.c_w, c_d, x.c_id); }
+        else if (j == 1) { op.table = LTPG_T_ORDER; op.row = 30000ull * x.w + x.a; }
+        else { op.table = LTPG_T_ORDERLINE; op.row = 450000ull * x.w + x.b; }
+        op.flags = OPF_READ;
+        return op;
+    case LTPG_TPCC_DELIVERY:  // TA/Execute.h:1772-2153
+        if (j == 0) { op.table = LTPG_T_NEWORDER; op.row = 30000ull * x.w + x.b; op.flags = OPF_WRITE; }
+        else if (j == 1) { op.table = LTPG_T_ORDER; op.row = 30000ull * x.w + x.a; op.flags = OPF_RW; }
+        else if (j == 2) { op.table = LTPG_T_ORDERLINE; op.row = 450000ull * x.w + x.c; op.flags = OPF_RW; }
+        else { op.table = LTPG_T_CUSTOMER; op.row = tpcc_cust_row(x.w, d, x.c_id); op.flags = OPF_WRITE; }
+        return op;
+    case LTPG_TPCC_STOCKLEVEL:  // TA/Execute.h:2155-2231
+        op.table = LTPG_T_STOCK; op.row = 100000ull * x.w + x.a; op.flags = OPF_READ;
+        return op;
+    default: break;
+    }
     switch (j) {
     case 0: op.table = LTPG_T_WAREHOUSE; op.row = x.w; op.flags = OPF_READ; return op;
     case 1: op.table = LTPG_T_DISTRICT; op.row = 10ull * x.w + d; op.flags = OPF_READ; return op;

@@ -52,13 +52,22 @@ __device__ __forceinline__ uint64_t ld_col(const TpccDev &db, uint32_t table, ui
 __device__ __forceinline__ bool txn_valid(const ltpg_tpcc_txn &x, uint32_t W, uint32_t n_lines) {
     const uint32_t kind = tpcc_kind(x.kind_info);
     if (x.w >= W || tpcc_d(x.kind_info) >= 10u || x.c_id >= 3000u) return false;
-    if (kind == LTPG_TPCC_NEWORDER) {
+    switch (kind) {
+    case LTPG_TPCC_NEWORDER: {
         const uint32_t cnt = tpcc_ol_cnt(x.kind_info);
         return cnt <= LTPG_TPCC_MAX_LINES && x.a < 30000u && x.b < 30000u && x.c < 450000u &&
                (uint64_t)x.line_off + cnt <= n_lines;
     }
-    if (kind == LTPG_TPCC_PAYMENT) return x.c_w < W && tpcc_c_d(x.kind_info) < 10u && x.a < 30000u;
-    return false;
+    case LTPG_TPCC_PAYMENT: return x.c_w < W && tpcc_c_d(x.kind_info) < 10u && x.a < 30000u;
+    case LTPG_TPCC_ORDERSTATUS:
+        return x.c_w < W && tpcc_c_d(x.kind_info) < 10u && x.a < 30000u && x.b < 450000u;
+    case LTPG_TPCC_DELIVERY: {
+        const uint32_t carrier = tpcc_ol_cnt(x.kind_info);
+        return x.a < 30000u && x.b < 30000u && x.c < 450000u && carrier >= 1u && carrier <= 10u;
+    }
+    case LTPG_TPCC_STOCKLEVEL: return x.a < 100000u;
+    default: return false;
+    }
 }
 __device__ __forceinline__ bool line_valid(const ltpg_tpcc_line &ln, uint32_t W) {
     return ln.i_id < 100000u && ln.supply_w < W;
@@ -185,14 +194,15 @@ __device__ __forceinline__ uint32_t ref_name_lookup(const TpccDev &db, uint32_t 
 // a NewOrder's its line count).
 constexpr uint32_t KI_NOT_FOUND = 0x200u;
 __device__ __forceinline__ bool txn_not_found(const ltpg_tpcc_txn &x) {
-    return tpcc_kind(x.kind_info) == LTPG_TPCC_PAYMENT && (x.kind_info & KI_NOT_FOUND);
+    const uint32_t kind = tpcc_kind(x.kind_info);
+    return (kind == LTPG_TPCC_PAYMENT || kind == LTPG_TPCC_ORDERSTATUS) && (x.kind_info & KI_NOT_FOUND);
 }
 
-// Resolves a by-name Payment in place: c_id becomes the customer's C_ID.
-// Returns false when the customer is not found; out-of-range fields are left
-// for txn_valid to reject.
+// Resolves a by-name Payment or OrderStatus in place: c_id becomes the
+// customer's C_ID.  Returns false when the customer is not found;
+// out-of-range fields are left for txn_valid to reject.
 __device__ __forceinline__ bool resolve_by_name(const TpccDev &db, ltpg_tpcc_txn &x) {
-    if (tpcc_kind(x.kind_info) != LTPG_TPCC_PAYMENT || !(x.kind_info & LTPG_PAY_BY_NAME)) return true;
+    if (!tpcc_customer_by_name(x.kind_info)) return true;
     const uint32_t c_d = tpcc_c_d(x.kind_info);
     if (x.c_w >= db.W || c_d >= 10u) return true;
     const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
@@ -274,6 +284,32 @@ __device__ __forceinline__ ltpg_tpcc_line load_line(const ltpg_tpcc_line *__rest
     return ln;
 }
 
+// The execute-phase read that gives a non-NewOrder transaction its result, if
+// op j is the op holding it: Payment j = 2 (C_BALANCE - amount), OrderStatus
+// j = 0 (C_BALANCE), Delivery j = 2 (the line's OL_AMOUNT), StockLevel j = 0
+// (S_QUANTITY).  Batch-start image.
+__device__ __forceinline__ bool result_read(const TpccDev &db, const ltpg_tpcc_txn &x, uint32_t j, const TpccOp &op,
+                                            long long &out) {
+    switch (tpcc_kind(x.kind_info)) {
+    case LTPG_TPCC_PAYMENT:
+        if (j != 2u) return false;
+        out = (long long)ld_col(db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
+        return true;
+    case LTPG_TPCC_ORDERSTATUS:
+        if (j != 0u) return false;
+        out = (long long)ld_col(db, LTPG_T_CUSTOMER, op.row, C_BALANCE);
+        return true;
+    case LTPG_TPCC_DELIVERY:
+        if (j != 2u) return false;
+        out = (long long)ld_col(db, LTPG_T_ORDERLINE, op.row, OL_AMOUNT);
+        return true;
+    case LTPG_TPCC_STOCKLEVEL:
+        out = (long long)ld_col(db, LTPG_T_STOCK, op.row, S_QUANTITY);
+        return true;
+    default: return false;
+    }
+}
+
 // ---- plain phase 1: execute + register (KERNEL_EXECUTE, TF/tp.cu:24-54) ----
 __global__ void __launch_bounds__(PBS) tpcc_exec_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
                                                        const ltpg_tpcc_line *__restrict__ lines,
@@ -314,8 +350,9 @@ __global__ void __launch_bounds__(PBS) tpcc_exec_plain(const ltpg_tpcc_txn *__re
             else if (j == 2) disc[i] = (uint32_t)ld_col(db, LTPG_T_CUSTOMER, op.row, C_DISCOUNT);
             else if (op.table == LTPG_T_ITEM)
                 atomicAdd(&sum[i], (unsigned long long)ln.qty * ld_col(db, LTPG_T_ITEM, op.row, I_PRICE));
-        } else if (j == 2) {
-            res[i] = (long long)ld_col(db, LTPG_T_CUSTOMER, op.row, C_BALANCE) - tpcc_amount(x);
+        } else {
+            long long r;
+            if (result_read(db, x, j, op, r)) res[i] = r;
         }
     }
     __syncthreads();
@@ -373,18 +410,40 @@ __global__ void __launch_bounds__(PBS) tpcc_check_plain(const ltpg_tpcc_txn *__r
 // Write op q of a committed transaction.  NewOrder: 0 ORDER insert, 1
 // NEW-ORDER insert, 2+2i stock update of line i, 3+2i ORDER-LINE insert of
 // line i.  Payment: 0 W_YTD add, 1 D_YTD add, 2 customer update, 3 HISTORY
-// insert.  Rows written here have exactly one committed writer in the batch
+// insert.  Delivery: 0 NEW-ORDER delete, 1 ORDER carrier, 2 ORDER-LINE delivery
+// date, 3 customer credit (`result` = the line's OL_AMOUNT read by the execute
+// phase).  Rows written here have exactly one committed writer in the batch
 // (a second one would have seen WAW), so plain read-modify-writes are safe;
 // the YTD adds are commutative and use atomics.
 __device__ __forceinline__ uint32_t tpcc_n_writes(uint32_t kind_info) {
-    return tpcc_kind(kind_info) == LTPG_TPCC_NEWORDER ? 2u + 2u * tpcc_ol_cnt(kind_info) : 4u;
+    switch (tpcc_kind(kind_info)) {
+    case LTPG_TPCC_NEWORDER: return 2u + 2u * tpcc_ol_cnt(kind_info);
+    case LTPG_TPCC_PAYMENT: return 4u;
+    case LTPG_TPCC_DELIVERY: return 4u;
+    default: return 0u;  // OrderStatus, StockLevel: read-only
+    }
 }
 
 template <bool kHotDirect>
 __device__ __forceinline__ void tpcc_apply_write(const TpccDev &db, const ltpg_tpcc_txn &x, uint32_t q,
                                                  const ltpg_tpcc_line *__restrict__ lines, uint64_t date,
-                                                 long long *hot_w, long long *hot_d) {
+                                                 long long *hot_w, long long *hot_d, int64_t result) {
     const uint32_t d = tpcc_d(x.kind_info);
+    if (tpcc_kind(x.kind_info) == LTPG_TPCC_DELIVERY) {
+        if (q == 0) {
+            uint64_t *o = col_ptr(db, LTPG_T_NEWORDER, 30000ull * x.w + x.b, 0);
+            o[NO_O_ID] = o[NO_D_ID] = o[NO_W_ID] = ~0ull;  // deleted
+        } else if (q == 1) {
+            *col_ptr(db, LTPG_T_ORDER, 30000ull * x.w + x.a, O_CARRIER_ID) = tpcc_ol_cnt(x.kind_info);
+        } else if (q == 2) {
+            *col_ptr(db, LTPG_T_ORDERLINE, 450000ull * x.w + x.c, OL_DELIVERY_D) = date;
+        } else {
+            uint64_t *cst = col_ptr(db, LTPG_T_CUSTOMER, tpcc_cust_row(x.w, d, x.c_id), 0);
+            cst[C_BALANCE] = (uint64_t)((int64_t)cst[C_BALANCE] + result);
+            cst[C_DELIVERY_CNT] += 1u;
+        }
+        return;
+    }
     if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
         const uint32_t cnt = tpcc_ol_cnt(x.kind_info);
         if (q == 0) {
@@ -446,6 +505,7 @@ __device__ __forceinline__ void tpcc_apply_write(const TpccDev &db, const ltpg_t
 __global__ void __launch_bounds__(PBS) tpcc_writeback_plain(const ltpg_tpcc_txn *__restrict__ txns, uint32_t B,
                                                             const ltpg_tpcc_line *__restrict__ lines,
                                                             const uint64_t *__restrict__ hdr, TpccDev db,
+                                                            const int64_t *__restrict__ results,
                                                             const uint8_t *__restrict__ flags,
                                                             uint32_t *__restrict__ bitmap, DevStats *st,
                                                             DevCtl *ctl) {
@@ -478,7 +538,7 @@ __global__ void __launch_bounds__(PBS) tpcc_writeback_plain(const ltpg_tpcc_txn 
     });
     for (uint32_t e = threadIdx.x; e < total; e += PBS) {
         const uint32_t i = tile_owner(h, nt, e), q = e - h.off[i];
-        tpcc_apply_write<true>(db, h.x[i], q, lines, txn_base + t0 + i, nullptr, nullptr);
+        tpcc_apply_write<true>(db, h.x[i], q, lines, txn_base + t0 + i, nullptr, nullptr, results[t0 + i]);
     }
     finish_batch(ctl);
 }
@@ -497,8 +557,8 @@ cudaError_t tpcc_phase(ltpg_ctx *c, Slot &s, int phase) {
         tpcc_check_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, c->tpcc.reg, s.flags,
                                                       c->ctl);
     } else {
-        tpcc_writeback_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, s.flags, s.bitmap,
-                                                          s.stats, c->ctl);
+        tpcc_writeback_plain<<<grid, PBS, 0, c->stream>>>(s.txns, B, s.lines, s.dev_hdr, db, s.results, s.flags,
+                                                          s.bitmap, s.stats, c->ctl);
     }
     return cudaGetLastError();
 }
@@ -578,33 +638,40 @@ __device__ __forceinline__ void tile_line(const TileHdrT &h, uint32_t nt, uint32
     li = e - h.off[i];
 }
 
+// Loads a tile, lays out its order lines and returns their number; hk = header
+// lanes per transaction (4 if the tile holds a Delivery, else 3).
 __device__ __forceinline__ uint32_t load_tile_lines(TileHdrT &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
-                                                    uint32_t n_lines) {
-    return load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl, [&](uint32_t i) {
+                                                    uint32_t n_lines, uint32_t &hk) {
+    const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl, [&](uint32_t i) {
         return (h.ok[i] && tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER) ? tpcc_ol_cnt(h.x[i].kind_info) : 0u;
     });
+    const bool dl = threadIdx.x < nt && tpcc_kind(h.x[threadIdx.x].kind_info) == LTPG_TPCC_DELIVERY;
+    hk = __syncthreads_or(dl) ? 4u : 3u;
+    return total;
 }
 
-// Work item e of a tile: e < 3 nt is header op k = e % 3 of transaction e / 3,
-// the rest are order lines.  Each item has up to two registrations: the header
-// op, or the line's stock write and ORDER-LINE insert.
+// Work item e of a tile: e < hk nt is header op k = e % hk of transaction
+// e / hk (valid when k < tpcc_n_head), the rest are order lines.  Each item
+// has up to two registrations: the header op, or the line's stock write and
+// ORDER-LINE insert.
 struct TileItem {
     uint32_t i, k, li;
     bool head, valid, two;
     ltpg_tpcc_line ln;
     TpccOp op;
 };
-__device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const TileHdrT &h, uint32_t nt, uint32_t e,
-                                              uint32_t n_items, uint32_t t0, bool report) {
+__device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const TileHdrT &h, uint32_t nt, uint32_t hk,
+                                              uint32_t e, uint32_t n_items, uint32_t t0, bool report) {
     TileItem it{0, 0, 0, false, false, false, {0, 0, 0}, {0, 0, 0}};
     if (e >= n_items) return it;
-    const uint32_t n_head = 3u * nt;
+    const uint32_t n_head = hk * nt;
     if (e < n_head) {
         it.head = true;
-        it.i = e / 3u;
-        it.k = e - 3u * it.i;
-        it.valid = h.ok[it.i] != 0u;
-        if (it.valid) it.op = tpcc_op(h.x[it.i], it.k + 2u, it.ln, a.db.strict);
+        it.i = e / hk;
+        it.k = e - hk * it.i;
+        const uint32_t ki = h.x[it.i].kind_info;
+        it.valid = h.ok[it.i] != 0u && it.k < tpcc_n_head(ki);
+        if (it.valid) it.op = tpcc_op(h.x[it.i], tpcc_head_j(ki, it.k), it.ln, a.db.strict);
         return it;
     }
     tile_line(h, nt, e - n_head, it.i, it.li);
@@ -625,9 +692,11 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
         if (threadIdx.x < PTT) sum[threadIdx.x] = 0ull;
-        const uint32_t n_items = 3u * nt + load_tile_lines(h, a, t0, nt, n_lines);
+        uint32_t hk;
+        const uint32_t lines_n = load_tile_lines(h, a, t0, nt, n_lines, hk);
+        const uint32_t n_items = hk * nt + lines_n;
         for (uint32_t base = 0; base < n_items; base += blockDim.x) {
-            const TileItem it = tile_item(a, h, nt, base + threadIdx.x, n_items, t0, true);
+            const TileItem it = tile_item(a, h, nt, hk, base + threadIdx.x, n_items, t0, true);
             const ltpg_tpcc_txn &x = h.x[it.i];
             const unsigned long long mine = tag | (t0 + it.i);
             // header: the op (customer rows repeat under NURand, the inserts are
@@ -637,19 +706,23 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT
             const bool w1 = it.head ? (it.op.flags & OPF_REG_W) != 0u : true;
             const bool f1 = filt && (it.head ? it.op.table == LTPG_T_CUSTOMER : true);
             tuned_register(a, it.valid, s1, w1, mine, true, f1);
-            tuned_register(a, it.two, a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, it.li), true, mine, false,
-                           false);
+            // second registration: a line's ORDER-LINE insert, or the read half
+            // of a header op that reads and writes its row (Delivery)
+            const bool rw = it.head && (it.op.flags & OPF_REG_R) && (it.op.flags & OPF_REG_W);
+            const uint64_t s2 = it.head ? s1 : a.db.base[LTPG_T_ORDERLINE] + tpcc_ol_row(x.w, x.c, it.li);
+            tuned_register(a, it.two || (it.valid && rw), s2, !it.head, mine, false, false);
             if (!it.valid) continue;
             if (!it.head) {
                 atomicAdd(&sum[it.i], (unsigned long long)it.ln.qty * ld_col(a.db, LTPG_T_ITEM, it.ln.i_id, I_PRICE));
-            } else if (it.k == 0u) {
-                if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
+            } else if (tpcc_kind(x.kind_info) == LTPG_TPCC_NEWORDER) {
+                if (it.k == 0u) {
                     wtax[it.i] = (uint32_t)ld_col(a.db, LTPG_T_WAREHOUSE, x.w, W_TAX);
                     dtax[it.i] = (uint32_t)ld_col(a.db, LTPG_T_DISTRICT, 10ull * x.w + tpcc_d(x.kind_info), D_TAX);
                     disc[it.i] = (uint32_t)ld_col(a.db, LTPG_T_CUSTOMER, it.op.row, C_DISCOUNT);
-                } else {
-                    res[it.i] = (long long)ld_col(a.db, LTPG_T_CUSTOMER, it.op.row, C_BALANCE) - tpcc_amount(x);
                 }
+            } else {
+                long long r;
+                if (result_read(a.db, x, tpcc_head_j(x.kind_info, it.k), it.op, r)) res[it.i] = r;
             }
         }
         __syncthreads();
@@ -678,11 +751,13 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
         if (threadIdx.x < PTT) fl[threadIdx.x] = 0u;
-        const uint32_t n_items = 3u * nt + load_tile_lines(h, a, t0, nt, n_lines);
+        uint32_t hk;
+        const uint32_t lines_n = load_tile_lines(h, a, t0, nt, n_lines, hk);
+        const uint32_t n_items = hk * nt + lines_n;
         // header ops and order lines in one pass (reads of WAREHOUSE, DISTRICT
         // and ITEM rows cannot conflict; see tpcc_exec_tiles)
         for (uint32_t e = threadIdx.x; e < n_items; e += blockDim.x) {
-            const TileItem it = tile_item(a, h, nt, e, n_items, t0, false);
+            const TileItem it = tile_item(a, h, nt, hk, e, n_items, t0, false);
             if (!it.valid) continue;
             const uint32_t t = t0 + it.i;
             uint32_t f = 0;
@@ -742,9 +817,9 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
         for (uint32_t e = threadIdx.x; e < wtotal; e += blockDim.x) {
             const uint32_t i = tile_owner(h, nt, e);
             if (hot) tpcc_apply_write<false>(a.db, h.x[i], e - h.off[i], a.lines, txn_base + t0 + i, hot,
-                                             hot + a.db.W);
+                                             hot + a.db.W, a.results[t0 + i]);
             else tpcc_apply_write<true>(a.db, h.x[i], e - h.off[i], a.lines, txn_base + t0 + i, nullptr,
-                                        nullptr);
+                                        nullptr, a.results[t0 + i]);
         }
         __syncthreads();
     }

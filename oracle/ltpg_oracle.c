@@ -355,6 +355,33 @@ static int txn_ops(const ltpg_tpcc_txn *x, const ltpg_tpcc_line *lines, uint32_t
         }
         return m;
     }
+    if (k_kind(x->kind_info) == LTPG_TPCC_ORDERSTATUS) {
+        /* TA/Execute.h:1592-1770: select customer, order, order line */
+        const uint32_t c_d = k_cd(x->kind_info);
+        if (x->c_w >= W || c_d >= 10 || x->a >= 30000 || x->b >= 450000) return -1;
+        ops[0] = (cc_op){LTPG_T_CUSTOMER, 30000ull * x->c_w + 3000ull * c_d + x->c_id, OP_READ};
+        ops[1] = (cc_op){LTPG_T_ORDER, 30000ull * x->w + x->a, OP_READ};
+        ops[2] = (cc_op){LTPG_T_ORDERLINE, 450000ull * x->w + x->b, OP_READ};
+        return 3;
+    }
+    if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {
+        /* TA/Execute.h:1772-2153: delete NEW-ORDER, select + update ORDER,
+           update + select ORDER-LINE, update customer (a row read and updated
+           registers and checks as both) */
+        const uint32_t carrier = k_cnt(x->kind_info);
+        if (x->a >= 30000 || x->b >= 30000 || x->c >= 450000 || carrier < 1 || carrier > 10) return -1;
+        ops[0] = (cc_op){LTPG_T_NEWORDER, 30000ull * x->w + x->b, OP_WRITE};
+        ops[1] = (cc_op){LTPG_T_ORDER, 30000ull * x->w + x->a, OP_READ | OP_WRITE};
+        ops[2] = (cc_op){LTPG_T_ORDERLINE, 450000ull * x->w + x->c, OP_READ | OP_WRITE};
+        ops[3] = (cc_op){LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, OP_WRITE};
+        return 4;
+    }
+    if (k_kind(x->kind_info) == LTPG_TPCC_STOCKLEVEL) {
+        /* TA/Execute.h:2155-2231: select stock */
+        if (x->a >= 100000) return -1;
+        ops[0] = (cc_op){LTPG_T_STOCK, 100000ull * x->w + x->a, OP_READ};
+        return 1;
+    }
     if (k_kind(x->kind_info) != LTPG_TPCC_PAYMENT) return -1;
     const uint32_t c_d = k_cd(x->kind_info);
     if (x->c_w >= W || c_d >= 10 || x->a >= 30000) return -1;
@@ -459,7 +486,8 @@ void oracle_tpcc_resolve(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, i
         const uint32_t c_d = k_cd(x->kind_info);
         cid[t] = x->c_id;
         found[t] = 1;
-        if (k_kind(x->kind_info) == LTPG_TPCC_PAYMENT && (x->kind_info & LTPG_PAY_BY_NAME) && x->c_w < W && c_d < 10) {
+        if ((k_kind(x->kind_info) == LTPG_TPCC_PAYMENT || k_kind(x->kind_info) == LTPG_TPCC_ORDERSTATUS) &&
+            (x->kind_info & LTPG_PAY_BY_NAME) && x->c_w < W && c_d < 10) {
             const uint32_t name = x->c_id >> 8, nth = x->c_id & 0xFFu;
             if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) cid[t] = ref_name_lookup(tab, W, x->c_w, c_d, name, nth);
             else found[t] = (uint8_t)name_lookup(tab, x->c_w, c_d, name, nth, &cid[t]);
@@ -482,7 +510,8 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
     for (uint32_t t = 0; t < B; ++t) {
         ltpg_tpcc_txn x = b->txns[t];
         const uint32_t c_d = k_cd(x.kind_info);
-        if (k_kind(x.kind_info) == LTPG_TPCC_PAYMENT && (x.kind_info & LTPG_PAY_BY_NAME) && x.c_w < W && c_d < 10) {
+        if ((k_kind(x.kind_info) == LTPG_TPCC_PAYMENT || k_kind(x.kind_info) == LTPG_TPCC_ORDERSTATUS) &&
+            (x.kind_info & LTPG_PAY_BY_NAME) && x.c_w < W && c_d < 10) {
             const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
             if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) x.c_id = ref_name_lookup(tab, W, x.c_w, c_d, name, nth);
             else if (!name_lookup(tab, x.c_w, c_d, name, nth, &x.c_id)) nf[t] = 1;
@@ -539,9 +568,16 @@ static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_b
             const int64_t wtax = (int64_t)*colp(tab, LTPG_T_WAREHOUSE, x->w, 1);
             const int64_t dtax = (int64_t)*colp(tab, LTPG_T_DISTRICT, 10ull * x->w + d, 2);
             results[t] = sum * (10000 - disc) * (10000 + wtax + dtax) / 100000000;
-        } else {
+        } else if (k_kind(x->kind_info) == LTPG_TPCC_PAYMENT) {
             const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
             results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5) - amount_of(x);
+        } else if (k_kind(x->kind_info) == LTPG_TPCC_ORDERSTATUS) {  /* C_BALANCE */
+            const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
+            results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5);
+        } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {  /* the line's OL_AMOUNT */
+            results[t] = (int64_t)*colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 8);
+        } else {  /* StockLevel: S_QUANTITY */
+            results[t] = (int64_t)*colp(tab, LTPG_T_STOCK, 100000ull * x->w + x->a, 2);
         }
     }
     /* phase 2: check */
@@ -596,6 +632,16 @@ static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_b
             o[7] = (uint64_t)all_local;
             uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
             no[0] = x->a; no[1] = d; no[2] = x->w;
+        } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {
+            uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
+            no[0] = no[1] = no[2] = ~0ull; /* deleted */
+            *colp(tab, LTPG_T_ORDER, 30000ull * x->w + x->a, 5) = k_cnt(x->kind_info);   /* O_CARRIER_ID */
+            *colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 6) = date;              /* OL_DELIVERY_D */
+            uint64_t *c = colp(tab, LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, 0);
+            c[5] = (uint64_t)((int64_t)c[5] + results[t]);                                 /* C_BALANCE */
+            c[8] += 1;                                                                     /* C_DELIVERY_CNT */
+        } else if (k_kind(x->kind_info) != LTPG_TPCC_PAYMENT) {
+            /* OrderStatus, StockLevel: read-only */
         } else {
             const int64_t amt = amount_of(x);
             const uint32_t c_d = k_cd(x->kind_info);
