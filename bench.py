@@ -38,6 +38,10 @@ WORKLOADS = {
                          rotate_every=8, n_batches=4,
                          name="YCSB high contention, profiling size: 10M x 10 uint64, 262,144 txn x 16 ops, "
                               "95/5, Zipf theta=0.99, 4 batches"),
+    "ycsb_scan": dict(kind="ycsb", n_records=10_000_000, n_txn=1 << 18, ops=10, update_pct=5, theta=0.99,
+                      rotate_every=8, n_batches=16, scan_len=10,
+                      name="YCSB range scans: 10M x 10 uint64, 262,144 txn x 10 ops, 95/5, every read scans "
+                           "10 keys, Zipf theta=0.99"),
     "ycsb_small": dict(kind="ycsb", n_records=1_000_000, n_txn=65536, ops=10, update_pct=50, theta=0.6,
                        rotate_every=0, n_batches=32,
                        name="YCSB small: 1M x 10 uint64, 65,536 txn x 10 ops, 50/50, Zipf theta=0.6"),
@@ -154,13 +158,16 @@ class Clocks:
 
 
 # ---- byte model (algorithmic bytes, logical, no sector rounding) --------------------
-def ycsb_bytes_per_txn(k, u, commit_rate):
+def ycsb_bytes_per_txn(k, u, commit_rate, scan=1):
     """Per transaction: op words 4k, value offset 4, update values 8uk, registration
-    (8-byte slot word read+written) 16k, check loads 8 per read / 16 per update,
-    row reads 80 per read, committed update stores 8 per update of a committed
-    transaction, result 8, flags 1+1, bitmap 1/8."""
-    exec_b = 4 * k + 16 * k + 80 * (1 - u) * k + 8
-    check_b = 4 * k + 4 + 8 * (1 - u) * k + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1 + 1 / 8
+    (8-byte slot word read+written) 16 per update and 16 per key a read covers,
+    check loads 8 per key a read covers / 16 per update, row reads 80 per key a
+    read covers, committed update stores 8 per update of a committed
+    transaction, result 8, flags 1+1, bitmap 1/8.  A read covers `scan` keys
+    (1: point reads)."""
+    exec_b = 4 * k + 16 * u * k + (16 + 80) * (1 - u) * k * scan + 8
+    check_b = (4 * k + 4 + 8 * (1 - u) * k * scan + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1
+               + 1 / 8)
     return exec_b, check_b
 
 
@@ -197,7 +204,8 @@ def measured_peaks():
 # ---- YCSB ---------------------------------------------------------------------------
 def make_ycsb(w, theta):
     from ltpg_gb300 import YcsbGenerator
-    g = YcsbGenerator(SEED, w["n_records"], w["n_txn"], w["ops"], w["update_pct"], theta, w["rotate_every"])
+    g = YcsbGenerator(SEED, w["n_records"], w["n_txn"], w["ops"], w["update_pct"], theta, w["rotate_every"],
+                      w.get("scan_len", 0))
     return [g.batch(i) for i in range(w["n_batches"])]
 
 
@@ -496,7 +504,8 @@ def reference_arm(args, w, rank):
         import oracle
         from ltpg_gb300 import YcsbGenerator
         theta = args.theta if args.theta is not None else w["theta"]
-        g = YcsbGenerator(SEED, w["n_records"], w["n_txn"], w["ops"], w["update_pct"], theta, w["rotate_every"])
+        g = YcsbGenerator(SEED, w["n_records"], w["n_txn"], w["ops"], w["update_pct"], theta, w["rotate_every"],
+                          w.get("scan_len", 0))
         nb = min(w["n_batches"], 8)
         batches = [g.batch(i) for i in range(nb)]
         o = oracle.YcsbOracle(SEED, w["n_records"])
@@ -577,7 +586,7 @@ def main():
     kt = tuned["kt"]
     exec_ms, cwb_ms = float(np.mean(kt[:, 0])), float(np.mean(kt[:, 1]))
     if w["kind"] == "ycsb":
-        eb, cb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate)
+        eb, cb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate, max(1, w.get("scan_len", 0)))
         ek = ycsb_exec_kernel_name(launch, (w["ops"] + 3) & ~3)
         kernel, kbytes, kms = (ek, eb, exec_ms) if exec_ms >= cwb_ms else ("ycsb_checkwb_tuned", cb, cwb_ms)
     else:

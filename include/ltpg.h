@@ -69,13 +69,17 @@ extern "C" {
  * rounded up to 4, so every transaction starts on a 16-byte boundary); unused
  * words hold LTPG_YCSB_OP_PAD.  Op word layout:
  *   bit 31      1 = update, 0 = read
- *   bits 27..30 field written by an update (0..9)
+ *   bits 27..30 update: field written (0..9); read: scan span s — the read
+ *               covers keys key .. key + s (s = 0: a point read; keys past
+ *               the table's end are left out, as the reference's scans do,
+ *               Y2/Execute.h:24-32)
  *   bits 0..26  key
  * Updates carry their new values in vals[], in transaction/op order;
  * val_off[t] is the index of transaction t's first value (val_off[n_txn] =
- * number of updates).  Per-transaction result: sum over the reads j of
- * (xor of the 10 fields of the row) * (2j + 1), mod 2^64, read from the
- * batch-start image.
+ * number of updates).  A read registers and checks every key it covers.
+ * Per-transaction result: sum over the reads j of (xor of the 10 fields of
+ * every row the read covers) * (2j + 1), mod 2^64, read from the batch-start
+ * image.
  */
 #define LTPG_YCSB_FIELDS 10
 #define LTPG_YCSB_OP_PAD 0xFFFFFFFFu
@@ -100,6 +104,9 @@ typedef struct {
     uint32_t update_pct;   /* share of update operations, 0..100         */
     uint32_t rotate_every; /* new hot-set permutation every R batches; 0 = key rank order */
     double theta;          /* Zipf exponent, 0 = uniform                 */
+    uint32_t scan_len;     /* 0 or 1: point reads; 2..16: every read scans
+                              scan_len keys (the reference's YCSB/2: 10)  */
+    uint32_t pad;
 } ltpg_ycsb_params;
 
 /* ---- TPC-C ---------------------------------------------------------------

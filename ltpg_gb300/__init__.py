@@ -160,8 +160,11 @@ def _check(code, ctx=None):
 class YcsbGenerator:
     """Deterministic YCSB batches (Zipf by Gray et al., splitmix64 streams)."""
 
-    def __init__(self, seed, n_records, n_txn, ops_per_txn=10, update_pct=50, theta=0.6, rotate_every=0):
-        self.params = abi.YcsbParamsC(seed, n_records, n_txn, ops_per_txn, update_pct, rotate_every, theta)
+    def __init__(self, seed, n_records, n_txn, ops_per_txn=10, update_pct=50, theta=0.6, rotate_every=0,
+                 scan_len=0):
+        """scan_len >= 2: every read is a range scan of scan_len keys."""
+        self.params = abi.YcsbParamsC(seed, n_records, n_txn, ops_per_txn, update_pct, rotate_every, theta, scan_len,
+                                      0)
         h = C.c_void_p()
         _check(lib().ltpg_gen_create_ycsb(C.byref(self.params), C.byref(h)))
         self._h = h

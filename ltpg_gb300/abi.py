@@ -34,7 +34,7 @@ class YcsbBatchC(C.Structure):
 class YcsbParamsC(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("n_records", C.c_uint64), ("n_txn", C.c_uint32),
                 ("ops_per_txn", C.c_uint32), ("update_pct", C.c_uint32), ("rotate_every", C.c_uint32),
-                ("theta", C.c_double)]
+                ("theta", C.c_double), ("scan_len", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class TpccBatchC(C.Structure):

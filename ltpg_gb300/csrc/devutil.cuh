@@ -45,6 +45,47 @@ __device__ __forceinline__ void red_add_u64(unsigned long long *p, unsigned long
     asm volatile("red.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Xor of the 10 fields of a YCSB row (five 16-byte loads).
+__device__ __forceinline__ unsigned long long row_xor(const uint64_t *__restrict__ rows, uint64_t key) {
+    const char *p = reinterpret_cast<const char *>(rows + key * LTPG_YCSB_FIELDS);
+    const ulonglong2 a = ld_nc16(p), b = ld_nc16(p + 16), c = ld_nc16(p + 32), d = ld_nc16(p + 48), e = ld_nc16(p + 64);
+    return a.x ^ a.y ^ b.x ^ b.y ^ c.x ^ c.y ^ d.x ^ d.y ^ e.x ^ e.y;
+}
+// Last key a YCSB read covers (key + scan span, within the table).
+__device__ __forceinline__ uint64_t scan_last(uint32_t w, uint64_t n) {
+    const uint64_t last = (uint64_t)ycsb_key(w) + ycsb_span(w);
+    return last < n ? last : n - 1;
+}
+// The keys of a range-scan read after its first (key + 1 .. last): each
+// registered in its read slot (with `filter`, skipped when the slot already
+// holds a smaller tag) and their rows xor-ed.  Point reads return 0.
+__device__ __forceinline__ unsigned long long scan_rest(RegSlot *reg, const uint64_t *__restrict__ rows, uint64_t n,
+                                                        uint32_t w, unsigned long long mine, bool filter) {
+    unsigned long long x = 0;
+    if (!ycsb_span(w)) return x;
+    const uint64_t last = scan_last(w, n);
+    for (uint64_t q = (uint64_t)ycsb_key(w) + 1; q <= last; ++q) {
+        unsigned long long *p = &reg[q].r;
+        bool go = true;
+        if (filter) {
+            unsigned long long cur;
+            asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(cur) : "l"(p));
+            go = cur > mine;
+        }
+        if (go) red_min(p, mine);
+        x ^= row_xor(rows, q);
+    }
+    return x;
+}
+// RAW on the keys of a range-scan read after its first.
+__device__ __forceinline__ bool scan_rest_raw(const RegSlot *reg, uint64_t n, uint32_t w, uint32_t t, uint32_t epoch) {
+    if (!ycsb_span(w)) return false;
+    const uint64_t last = scan_last(w, n);
+    bool raw = false;
+    for (uint64_t q = (uint64_t)ycsb_key(w) + 1; q <= last; ++q) raw |= slot_min(ld_slot(reg + q).y, epoch) < t;
+    return raw;
+}
+
 __device__ __forceinline__ void report_error(DevCtl *ctl, uint32_t code, uint32_t index) {
     if (atomicOr(&ctl->error, code) == 0u) ctl->err_index = index;
 }

@@ -140,6 +140,7 @@ int ltpg_gen_create_ycsb(const ltpg_ycsb_params *p, ltpg_gen **out) {
     if (p->ops_per_txn == 0 || p->ops_per_txn > LTPG_YCSB_MAX_OPS) return LTPG_ERR_INVALID;
     if (p->ops_per_txn > p->n_records || p->update_pct > 100 || p->n_txn == 0) return LTPG_ERR_INVALID;
     if (!(p->theta >= 0.0 && p->theta < 1.0)) return LTPG_ERR_INVALID;
+    if (p->scan_len > 16) return LTPG_ERR_INVALID;
     ltpg_gen *g = new (std::nothrow) ltpg_gen();
     if (!g) return LTPG_ERR_NOMEM;
     g->kind = LTPG_WORKLOAD_YCSB;
@@ -247,7 +248,9 @@ int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t 
                 keys[j] = (uint32_t)key;
                 const bool upd = r.below(100) < p.update_pct;
                 const uint32_t field = (uint32_t)r.below(LTPG_YCSB_FIELDS);
-                w[j] = ycsb_word((uint32_t)key, upd, upd ? field : 0u);
+                // a read scans scan_len keys when scan_len >= 2 (span in the field bits)
+                const uint32_t span = p.scan_len >= 2u ? p.scan_len - 1u : 0u;
+                w[j] = ycsb_word((uint32_t)key, upd, upd ? field : span);
                 nupd += upd;
             }
             for (uint32_t j = k; j < stride; ++j) w[j] = LTPG_YCSB_OP_PAD;

@@ -44,6 +44,9 @@ LTPG_HD bool ycsb_is_pad(uint32_t w) { return w == LTPG_YCSB_OP_PAD; }
 LTPG_HD bool ycsb_is_update(uint32_t w) { return (w >> 31) != 0; }
 LTPG_HD uint32_t ycsb_field(uint32_t w) { return (w >> 27) & 0xFu; }
 LTPG_HD uint32_t ycsb_key(uint32_t w) { return w & YCSB_KEY_MASK; }
+// A read's field bits name a range scan of span + 1 consecutive keys (0: a
+// point read); keys past the table's end are left out (Y2/Execute.h:24-32).
+LTPG_HD uint32_t ycsb_span(uint32_t w) { return ycsb_is_update(w) ? 0u : ((w >> 27) & 0xFu); }
 LTPG_HD uint32_t ycsb_word(uint32_t key, bool update, uint32_t field) {
     return (update ? 0x80000000u : 0u) | ((field & 0xFu) << 27) | (key & YCSB_KEY_MASK);
 }

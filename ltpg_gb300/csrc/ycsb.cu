@@ -26,16 +26,6 @@ cudaError_t ycsb_init_table(ltpg_ctx *c) {
     return cudaMemsetAsync(c->ycsb.reg, 0xFF, c->ycsb.n * sizeof(RegSlot), c->stream);
 }
 
-// Checksum contribution of read j of a transaction: xor of the row's fields
-// times (2j + 1).
-__device__ __forceinline__ unsigned long long row_digest(const uint64_t *__restrict__ rows, uint32_t key,
-                                                         uint32_t j) {
-    const char *p = reinterpret_cast<const char *>(rows + (uint64_t)key * LTPG_YCSB_FIELDS);
-    ulonglong2 a = ld_nc16(p), b = ld_nc16(p + 16), c = ld_nc16(p + 32), d = ld_nc16(p + 48),
-               e = ld_nc16(p + 64);
-    const unsigned long long x = a.x ^ a.y ^ b.x ^ b.y ^ c.x ^ c.y ^ d.x ^ d.y ^ e.x ^ e.y;
-    return x * (2ull * j + 1ull);
-}
 
 // ---- plain phase 1: execute + register (KERNEL_EXECUTE, Y1/ycsb.cu:9-24) -----
 // One thread per operation; a block holds `tile` whole transactions.
@@ -59,8 +49,10 @@ __global__ void __launch_bounds__(256) ycsb_exec_plain(const uint32_t *__restric
             } else if (ycsb_is_update(w)) {
                 red_min(&reg[key].w, tag | t);
             } else {
+                // a point read, or a range scan of keys key .. key + span
                 red_min(&reg[key].r, tag | t);
-                atomicAdd(&dig[lt], row_digest(rows, key, j));
+                const unsigned long long x = row_xor(rows, key) ^ scan_rest(reg, rows, n, w, tag | t, false);
+                atomicAdd(&dig[lt], x * (2ull * j + 1ull));
             }
         }
     }
@@ -91,7 +83,7 @@ __global__ void __launch_bounds__(256) ycsb_check_plain(const uint32_t *__restri
             if (ycsb_is_update(w)) {
                 if (rmin < t) f |= LTPG_FLAG_WAR;
                 if (wmin < t) f |= LTPG_FLAG_WAW;
-            } else if (wmin < t) {
+            } else if (wmin < t || scan_rest_raw(reg, n, w, t, epoch)) {
                 f |= LTPG_FLAG_RAW;
             }
             if (f) atomicOr(&fl[lt], f);

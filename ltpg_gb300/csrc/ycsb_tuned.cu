@@ -111,8 +111,8 @@ __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long
                     const char *p = reinterpret_cast<const char *>(a.rows + (uint64_t)key * LTPG_YCSB_FIELDS);
                     const ulonglong2 r0 = ld_nc16(p), r1 = ld_nc16(p + 16), r2 = ld_nc16(p + 32),
                                      r3 = ld_nc16(p + 48), r4 = ld_nc16(p + 64);
-                    const unsigned long long x =
-                        r0.x ^ r0.y ^ r1.x ^ r1.y ^ r2.x ^ r2.y ^ r3.x ^ r3.y ^ r4.x ^ r4.y;
+                    const unsigned long long x = r0.x ^ r0.y ^ r1.x ^ r1.y ^ r2.x ^ r2.y ^ r3.x ^ r3.y ^ r4.x ^ r4.y ^
+                                                 scan_rest(a.reg, a.rows, a.n, w, tag | t, a.filter != 0u);
                     part += x * (2ull * (j0 + q) + 1ull);
                 }
             }
@@ -158,7 +158,7 @@ __device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *
                 if (ycsb_is_update(w)) {
                     if (rmin < t) f |= LTPG_FLAG_WAR;
                     if (wmin < t) f |= LTPG_FLAG_WAW;
-                } else if (wmin < t) {
+                } else if (wmin < t || scan_rest_raw(a.reg, a.n, w, t, epoch)) {
                     f |= LTPG_FLAG_RAW;
                 }
             }
@@ -360,8 +360,9 @@ __global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t 
         unsigned long long part = 0;
 #pragma unroll
         for (int q = 0; q < OPS; ++q) {
-            const unsigned long long x = r[q][0].x ^ r[q][0].y ^ r[q][1].x ^ r[q][1].y ^ r[q][2].x ^ r[q][2].y ^
-                                         r[q][3].x ^ r[q][3].y ^ r[q][4].x ^ r[q][4].y;
+            unsigned long long x = r[q][0].x ^ r[q][0].y ^ r[q][1].x ^ r[q][1].y ^ r[q][2].x ^ r[q][2].y ^
+                                   r[q][3].x ^ r[q][3].y ^ r[q][4].x ^ r[q][4].y;
+            if (rd[q]) x ^= scan_rest(a.reg, a.rows, a.n, w[q], tag | t, kFilter);
             part += rd[q] ? x * (2ull * (j0 + q) + 1ull) : 0ull;
         }
         for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
@@ -475,6 +476,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             __threadfence_block();
             *reinterpret_cast<volatile uint32_t *>(&e->dig_ok) = 1u;
         }
+        if (rd) x ^= scan_rest(a.reg, a.rows, a.n, w, tag | t, kFilter);  // the rest of a range scan
         unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
         for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
         if (act && j == 0u) a.results[t] = (int64_t)part;

@@ -63,6 +63,14 @@ static inline int op_pad(uint32_t w) { return w == LTPG_YCSB_OP_PAD; }
 static inline int op_upd(uint32_t w) { return (int)(w >> 31); }
 static inline uint32_t op_key(uint32_t w) { return w & ((1u << LTPG_YCSB_KEY_BITS) - 1u); }
 static inline uint32_t op_field(uint32_t w) { return (w >> 27) & 0xFu; }
+/* Keys a read covers: key .. key + span within the table (a range scan when
+   span > 0, Y2/Execute.h:24-32, where every read scans YCSB_SCAN_SIZE keys;
+   its check tests Loc + 1 for every i, Y2/Execute.h:126-132, and checks
+   nothing else — here every covered key is checked, as it is registered). */
+static inline uint32_t op_last(uint32_t w, uint64_t n) {
+    const uint64_t last = (uint64_t)op_key(w) + (op_upd(w) ? 0u : op_field(w));
+    return (uint32_t)(last < n ? last : n - 1);
+}
 
 static inline uint32_t commit_rule(uint32_t f) {
     const int raw = (f & LTPG_FLAG_RAW) != 0, war = (f & LTPG_FLAG_WAR) != 0, waw = (f & LTPG_FLAG_WAW) != 0;
@@ -82,8 +90,7 @@ int64_t oracle_ycsb_batch(uint64_t *rows, uint64_t n, const ltpg_ycsb_batch *b, 
         const uint32_t w = b->ops[i];
         if (op_pad(w)) continue;
         if (op_key(w) >= n || (op_upd(w) && op_field(w) >= LTPG_YCSB_FIELDS)) return -1;
-        reg_r[op_key(w)] = NONE;
-        reg_w[op_key(w)] = NONE;
+        for (uint32_t key = op_key(w); key <= op_last(w, n); ++key) reg_r[key] = reg_w[key] = NONE;
     }
     /* phase 1: register (smallest TID wins) and read the batch-start rows */
     for (uint32_t t = 0; t < B; ++t) {
@@ -92,11 +99,14 @@ int64_t oracle_ycsb_batch(uint64_t *rows, uint64_t n, const ltpg_ycsb_batch *b, 
             const uint32_t w = b->ops[(uint64_t)t * stride + j];
             if (op_pad(w)) continue;
             const uint32_t key = op_key(w);
-            uint32_t *slot = op_upd(w) ? &reg_w[key] : &reg_r[key];
-            if (t < *slot) *slot = t;
-            if (!op_upd(w)) {
+            if (op_upd(w)) {
+                if (t < reg_w[key]) reg_w[key] = t;
+            } else {
                 uint64_t x = 0;
-                for (uint32_t f = 0; f < LTPG_YCSB_FIELDS; ++f) x ^= rows[(uint64_t)key * LTPG_YCSB_FIELDS + f];
+                for (uint32_t q = key; q <= op_last(w, n); ++q) {
+                    if (t < reg_r[q]) reg_r[q] = t;
+                    for (uint32_t f = 0; f < LTPG_YCSB_FIELDS; ++f) x ^= rows[(uint64_t)q * LTPG_YCSB_FIELDS + f];
+                }
                 dig += x * (2ull * j + 1ull);
             }
         }
@@ -114,8 +124,9 @@ int64_t oracle_ycsb_batch(uint64_t *rows, uint64_t n, const ltpg_ycsb_batch *b, 
             if (op_upd(w)) {
                 if (reg_r[key] < t) f |= LTPG_FLAG_WAR;
                 if (reg_w[key] < t) f |= LTPG_FLAG_WAW;
-            } else if (reg_w[key] < t) {
-                f |= LTPG_FLAG_RAW;
+            } else {
+                for (uint32_t q = key; q <= op_last(w, n); ++q)
+                    if (reg_w[q] < t) f |= LTPG_FLAG_RAW;
             }
         }
         f |= commit_rule(f);
@@ -164,8 +175,10 @@ static void *ycsb_mt_worker(void *p) {
     for (uint64_t i = (uint64_t)a->t0 * stride; i < (uint64_t)a->t1 * stride; ++i) {
         const uint32_t w = b->ops[i];
         if (op_pad(w)) continue;
-        __atomic_store_n(&a->reg_r[op_key(w)], NONE, __ATOMIC_RELAXED);
-        __atomic_store_n(&a->reg_w[op_key(w)], NONE, __ATOMIC_RELAXED);
+        for (uint32_t key = op_key(w); key <= op_last(w, a->n); ++key) {
+            __atomic_store_n(&a->reg_r[key], NONE, __ATOMIC_RELAXED);
+            __atomic_store_n(&a->reg_w[key], NONE, __ATOMIC_RELAXED);
+        }
     }
     pthread_barrier_wait(a->bar);
     for (uint32_t t = a->t0; t < a->t1; ++t) {
@@ -174,10 +187,15 @@ static void *ycsb_mt_worker(void *p) {
             const uint32_t w = b->ops[(uint64_t)t * stride + j];
             if (op_pad(w)) continue;
             const uint32_t key = op_key(w);
-            atomic_min_u32(op_upd(w) ? &a->reg_w[key] : &a->reg_r[key], t);
-            if (!op_upd(w)) {
+            if (op_upd(w)) {
+                atomic_min_u32(&a->reg_w[key], t);
+            } else {
                 uint64_t x = 0;
-                for (uint32_t f = 0; f < LTPG_YCSB_FIELDS; ++f) x ^= a->rows[(uint64_t)key * LTPG_YCSB_FIELDS + f];
+                for (uint32_t q = key; q <= op_last(w, a->n); ++q) {
+                    atomic_min_u32(&a->reg_r[q], t);
+                    for (uint32_t f = 0; f < LTPG_YCSB_FIELDS; ++f)
+                        x ^= a->rows[(uint64_t)q * LTPG_YCSB_FIELDS + f];
+                }
                 dig += x * (2ull * j + 1ull);
             }
         }
@@ -191,13 +209,12 @@ static void *ycsb_mt_worker(void *p) {
             const uint32_t w = b->ops[(uint64_t)t * stride + j];
             if (op_pad(w)) continue;
             const uint32_t key = op_key(w);
-            const uint32_t rmin = __atomic_load_n(&a->reg_r[key], __ATOMIC_RELAXED);
-            const uint32_t wmin = __atomic_load_n(&a->reg_w[key], __ATOMIC_RELAXED);
             if (op_upd(w)) {
-                if (rmin < t) f |= LTPG_FLAG_WAR;
-                if (wmin < t) f |= LTPG_FLAG_WAW;
-            } else if (wmin < t) {
-                f |= LTPG_FLAG_RAW;
+                if (__atomic_load_n(&a->reg_r[key], __ATOMIC_RELAXED) < t) f |= LTPG_FLAG_WAR;
+                if (__atomic_load_n(&a->reg_w[key], __ATOMIC_RELAXED) < t) f |= LTPG_FLAG_WAW;
+            } else {
+                for (uint32_t q = key; q <= op_last(w, a->n); ++q)
+                    if (__atomic_load_n(&a->reg_w[q], __ATOMIC_RELAXED) < t) f |= LTPG_FLAG_RAW;
             }
         }
         f |= commit_rule(f);

@@ -119,3 +119,50 @@ def test_golden_tpcc_generator_and_replay(built_lib):
         assert np.array_equal(flags, z[f"flags{bid}"]) and np.array_equal(results, z[f"results{bid}"])
     for t in range(abi.TPCC_TABLES):
         assert int(np.bitwise_xor.reduce(o.tables[t])) == int(z["xor"][t])
+
+
+def test_ycsb_range_scans_known_answers():
+    """Range-scan reads (span in a read's field bits; every read of the
+    reference's YCSB/2 scans 10 keys, Y2/Execute.h:24-32): every covered key
+    is registered and checked, keys past the table's end are left out, and the
+    result xors every covered row."""
+    n = 20
+    o = oracle.YcsbOracle(6, n)
+    rows0 = o.rows.reshape(n, 10).copy()
+    upd = lambda key, field: np.uint32(0x80000000 | (field << 27) | key)
+    scan = lambda key, span: np.uint32((span << 27) | key)
+    pad = np.uint32(0xFFFFFFFF)
+    ops = np.array([[upd(5, 2), pad, pad, pad],          # t0: writes key 5
+                    [scan(3, 3), pad, pad, pad],         # t1: reads keys 3..6 -> RAW (key 5), commits
+                    [upd(4, 0), pad, pad, pad],          # t2: writes key 4, read by t1 -> WAR, commits
+                    [scan(18, 5), upd(9, 1), pad, pad],  # t3: reads 18..19 (clamped), writes 9
+                    [scan(8, 1), pad, pad, pad]],        # t4: reads 8..9 -> RAW (key 9 by t3)
+                   dtype=np.uint32)
+    val_off = np.array([0, 1, 1, 2, 3, 3], dtype=np.uint32)
+    vals = np.array([111, 222, 333], dtype=np.uint64)
+    b = YcsbBatch(ops.ravel(), val_off, vals, 5, 1)
+    b.ops_per_txn, b.op_stride = 2, 4
+    flags, bitmap, results, commits = o.run(b)
+    assert flags[0] == abi.FLAG_COMMIT
+    assert flags[1] == abi.FLAG_RAW | abi.FLAG_COMMIT
+    assert flags[2] == abi.FLAG_WAR | abi.FLAG_COMMIT
+    assert flags[3] == abi.FLAG_COMMIT
+    assert flags[4] == abi.FLAG_RAW | abi.FLAG_COMMIT
+    x = lambda keys: int(np.bitwise_xor.reduce(rows0[keys].ravel()))
+    u64 = lambda v: int(v) & (2**64 - 1)  # results are int64 (mod 2^64)
+    assert u64(results[1]) == x([3, 4, 5, 6])
+    assert u64(results[3]) == x([18, 19])
+    assert u64(results[4]) == x([8, 9])
+    rows = o.rows.reshape(n, 10)
+    assert rows[5, 2] == 111 and rows[4, 0] == 222 and rows[9, 1] == 333
+
+
+def test_ycsb_generator_scans():
+    g = YcsbGenerator(3, 5000, 2000, 8, 20, 0.6, scan_len=10)
+    b = g.batch(0)
+    w = b.ops.reshape(b.n_txn, b.op_stride)[:, :8]
+    reads = (w >> 31) == 0
+    assert ((w[reads] >> 27) & 0xF == 9).all()  # span 9: 10 keys
+    assert g.batch(0).ops.tobytes() == b.ops.tobytes()
+    flags = oracle.YcsbOracle(3, 5000).run(b)[0]
+    assert ((flags & abi.FLAG_COMMIT) != 0).any()
