@@ -394,6 +394,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
     const uint64_t nw = (uint64_t)a.B << lsh;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     const uint32_t grp = lane / 5, chunk = lane % 5;  // row-read lane groups (6 x 5 lanes)
+    bool scans = false;  // some read of this thread's was a range scan
     for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
         const uint64_t v = base + threadIdx.x;
         const bool act = v < nw;
@@ -476,10 +477,35 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             __threadfence_block();
             *reinterpret_cast<volatile uint32_t *>(&e->dig_ok) = 1u;
         }
-        if (rd) x ^= scan_rest(a.reg, a.rows, a.n, w, tag | t, kFilter);  // the rest of a range scan
+        scans |= rd && ycsb_span(w) != 0u;
         unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
         for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
         if (act && j == 0u) a.results[t] = (int64_t)part;
+    }
+    // Range scans: the keys after each scan's first, in a second pass over the
+    // block's ops (kept out of the loop above, whose code is the point-read
+    // path: with the scan code inside, that loop ran 6 % slower on point-read
+    // batches).  The same thread leads a transaction in both passes, so its
+    // result is completed in program order.
+    if (__syncthreads_or(scans)) {
+        for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
+            const uint64_t v = base + threadIdx.x;
+            const bool act = v < nw;
+            const uint32_t t = (uint32_t)(v >> lsh);
+            const uint32_t j = (uint32_t)v & (lpt - 1u);
+            const uint32_t w = act && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
+            const bool rd = act && !ycsb_is_pad(w) && ycsb_key(w) < a.n && ycsb_span(w) != 0u;
+            // the first pass added x_first * (2j + 1); the read's term is
+            // (x_first ^ x_rest) * (2j + 1): add the difference (mod 2^64)
+            unsigned long long part = 0;
+            if (rd) {
+                const unsigned long long xf = row_xor(a.rows, ycsb_key(w));
+                const unsigned long long xr = scan_rest(a.reg, a.rows, a.n, w, tag | t, kFilter);
+                part = ((xf ^ xr) - xf) * (2ull * j + 1ull);
+            }
+            for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+            if (act && j == 0u && part) a.results[t] = (int64_t)((unsigned long long)a.results[t] + part);
+        }
     }
 }
 
