@@ -495,14 +495,41 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             const uint32_t j = (uint32_t)v & (lpt - 1u);
             const uint32_t w = act && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
             const bool rd = act && !ycsb_is_pad(w) && ycsb_key(w) < a.n && ycsb_span(w) != 0u;
-            // the first pass added x_first * (2j + 1); the read's term is
-            // (x_first ^ x_rest) * (2j + 1): add the difference (mod 2^64)
-            unsigned long long part = 0;
-            if (rd) {
-                const unsigned long long xf = row_xor(a.rows, ycsb_key(w));
-                const unsigned long long xr = scan_rest(a.reg, a.rows, a.n, w, tag | t, kFilter);
-                part = ((xf ^ xr) - xf) * (2ull * j + 1ull);
+            const uint32_t key = ycsb_key(w);
+            const uint32_t last = rd ? (uint32_t)scan_last(w, a.n) : 0u;
+            // the warp takes its scans one at a time: all lanes read the
+            // scan's rows as one contiguous range (16 B chunks, coalesced) and
+            // register its keys after the first, one key per lane
+            unsigned long long xf = 0, xa = 0;  // this lane's scan: first row, all rows
+            for (unsigned m = __ballot_sync(FULL, rd); m; m &= m - 1u) {
+                const uint32_t src = (uint32_t)__ffs(m) - 1u;
+                const uint32_t k0 = __shfl_sync(FULL, key, src), k1 = __shfl_sync(FULL, last, src);
+                const uint32_t ts = __shfl_sync(FULL, t, src);
+                const uint32_t chunks = (k1 - k0 + 1u) * 5u;
+                const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(a.rows + (uint64_t)k0 * LTPG_YCSB_FIELDS);
+                unsigned long long c_all = 0, c_first = 0;
+                for (uint32_t c = lane; c < chunks; c += 32u) {
+                    const ulonglong2 q = ld_nc16(p + c);
+                    c_all ^= q.x ^ q.y;
+                    if (c < 5u) c_first ^= q.x ^ q.y;
+                }
+                if (lane < k1 - k0) {
+                    unsigned long long *slot = &a.reg[(uint64_t)k0 + 1u + lane].r;
+                    const unsigned long long mine = tag | ts;
+                    if (!kFilter || ld_ca_u64(slot) > mine) red_min(slot, mine);
+                }
+                for (uint32_t o = 16; o >= 1u; o >>= 1) {
+                    c_all ^= __shfl_xor_sync(FULL, c_all, o);
+                    c_first ^= __shfl_xor_sync(FULL, c_first, o);
+                }
+                if (lane == src) {
+                    xa = c_all;
+                    xf = c_first;
+                }
             }
+            // the first pass added x_first * (2j + 1); the read's term is
+            // x_all * (2j + 1): add the difference (mod 2^64)
+            unsigned long long part = rd ? (xa - xf) * (2ull * j + 1ull) : 0ull;
             for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
             if (act && j == 0u && part) a.results[t] = (int64_t)((unsigned long long)a.results[t] + part);
         }
