@@ -279,6 +279,33 @@ int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t 
 int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
                         ltpg_tpcc_line *lines, ltpg_tpcc_batch *out);
 
+/* Device generation: the same batch as ltpg_gen_*_batch (byte for byte),
+ * made on the GPU in slot `slot` on the context stream, with no host
+ * generation and no host-to-device copy (the reference generates on host
+ * threads and copies, TF/Query.h:417-605).  YCSB generators are stateless
+ * and may mix host and device batches.  A TPC-C generator's counters and
+ * order memory move to the device at its first device batch; its host
+ * batches are refused (LTPG_ERR_STATE) from then on, and batches stay in
+ * order.  Device TPC-C generation needs cfg.max_lines >= 15 n_txn. */
+int ltpg_gen_ycsb_batch_device(ltpg_ctx *ctx, ltpg_gen *g, uint64_t batch_id, uint32_t slot);
+int ltpg_gen_tpcc_batch_device(ltpg_ctx *ctx, ltpg_gen *g, uint64_t batch_id, uint32_t slot);
+
+/* The batch held by a slot (uploaded or generated on the device), for
+ * inspection: its shape, then part `part` copied to host (YCSB 0 ops,
+ * 1 val_off, 2 vals; TPC-C 0 txns, 1 lines; `bytes` must be the part's size).
+ * Both synchronise the context stream. */
+typedef struct {
+    int32_t workload;     /* LTPG_WORKLOAD_YCSB / _TPCC */
+    uint32_t ops_per_txn; /* YCSB */
+    uint64_t n_txn;
+    uint64_t n_op_words;  /* YCSB: n_txn * op_stride */
+    uint64_t n_updates;   /* YCSB */
+    uint64_t n_lines;     /* TPC-C */
+    uint64_t txn_base;    /* TPC-C */
+} ltpg_batch_info;
+int ltpg_batch_info_get(ltpg_ctx *ctx, uint32_t slot, ltpg_batch_info *out);
+int ltpg_batch_download(ltpg_ctx *ctx, uint32_t slot, uint32_t part, void *host, size_t bytes);
+
 /* Replaces: Query::copy_to_device (TF/Query.h:532-605, Y1/Query.h:194-213).
  * Copies a host batch into device slot `slot` on the context stream. */
 int ltpg_batch_upload_ycsb(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b);

@@ -291,6 +291,35 @@ class Engine:
         else:
             self._ck(lib().ltpg_batch_upload_tpcc(self._h, slot, C.byref(cb)))
 
+    def generate(self, slot, gen, batch_id=None):
+        """Makes a generator's batch on the GPU, directly in `slot` (asynchronous
+        on the engine's stream): byte-identical to gen.batch(batch_id) /
+        gen.next().  A TPC-C generator continues in order from gen.next_id and
+        keeps its state on the GPU from then on (its host batches are refused)."""
+        if isinstance(gen, YcsbGenerator):
+            if batch_id is None:
+                raise ValueError("a YCSB batch needs its batch_id")
+            self._ck(lib().ltpg_gen_ycsb_batch_device(self._h, gen._h, batch_id, slot))
+        else:
+            self._ck(lib().ltpg_gen_tpcc_batch_device(self._h, gen._h, gen.next_id, slot))
+            gen.next_id += 1
+
+    def download_batch(self, slot):
+        """The batch held by `slot` (uploaded or generated on the GPU)."""
+        bi = abi.BatchInfoC()
+        self._ck(lib().ltpg_batch_info_get(self._h, slot, C.byref(bi)))
+
+        def part(i, dtype, count):
+            a = np.empty(count, dtype=dtype)
+            self._ck(lib().ltpg_batch_download(self._h, slot, i, _p(a) if count else None, a.nbytes))
+            return a
+
+        if bi.workload == abi.WORKLOAD_YCSB:
+            return YcsbBatch(part(0, np.uint32, bi.n_op_words), part(1, np.uint32, bi.n_txn + 1),
+                             part(2, np.uint64, bi.n_updates), bi.n_txn, bi.ops_per_txn)
+        return TpccBatch(part(0, TpccBatch.TXN_DTYPE, bi.n_txn), part(1, TpccBatch.LINE_DTYPE, bi.n_lines),
+                         bi.txn_base)
+
     def execute_register(self, slot):
         self._ck(lib().ltpg_execute_register(self._h, slot))
 

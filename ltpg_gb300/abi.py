@@ -83,6 +83,12 @@ class StatsC(C.Structure):
                 ("waw", C.c_uint64), ("staged_ops", C.c_uint64), ("total_ops", C.c_uint64)]
 
 
+class BatchInfoC(C.Structure):
+    _fields_ = [("workload", C.c_int32), ("ops_per_txn", C.c_uint32), ("n_txn", C.c_uint64),
+                ("n_op_words", C.c_uint64), ("n_updates", C.c_uint64), ("n_lines", C.c_uint64),
+                ("txn_base", C.c_uint64)]
+
+
 P = C.c_void_p
 U32, U64, I32 = C.c_uint32, C.c_uint64, C.c_int32
 SZ = C.c_size_t
@@ -108,6 +114,10 @@ SIGNATURES = {
     "ltpg_gen_capacity": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_gen_ycsb_batch": (C.c_int, [P, U64, P, P, P, C.POINTER(YcsbBatchC)]),
     "ltpg_gen_tpcc_batch": (C.c_int, [P, U64, P, P, C.POINTER(TpccBatchC)]),
+    "ltpg_gen_ycsb_batch_device": (C.c_int, [P, P, U64, U32]),
+    "ltpg_batch_info_get": (C.c_int, [P, U32, C.POINTER(BatchInfoC)]),
+    "ltpg_batch_download": (C.c_int, [P, U32, U32, P, C.c_size_t]),
+    "ltpg_gen_tpcc_batch_device": (C.c_int, [P, P, U64, U32]),
     "ltpg_batch_upload_ycsb": (C.c_int, [P, U32, C.POINTER(YcsbBatchC)]),
     "ltpg_batch_upload_tpcc": (C.c_int, [P, U32, C.POINTER(TpccBatchC)]),
     "ltpg_execute_register": (C.c_int, [P, U32]),

@@ -15,6 +15,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libltpg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include")]
+# the device generator's double arithmetic must round like the host's: no
+# contraction into fused multiply-adds
+EXTRA = {"gen_dev.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -29,7 +32,8 @@ def _sources():
 
 def _compile(src):
     obj = os.path.join(BUILD, src + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, "-lineinfo", "--expt-relaxed-constexpr", "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *ARCH, *COMMON, *EXTRA.get(src, []), "-lineinfo", "--expt-relaxed-constexpr", "-c",
+           os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -309,20 +309,20 @@ int ltpg_db_download(ltpg_ctx *c, uint32_t table, void *host, size_t bytes) {
 }
 
 // ---- batches ---------------------------------------------------------------------
-namespace {
-int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream_t st) {
+}  // extern "C"
+
+namespace ltpg {
+
+int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, uint32_t n_updates, Slot **out) {
     Slot *s = get_slot(c, slot);
-    if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (!s) return fail(c, LTPG_ERR_INVALID, "bad slot or batch");
     if (!c->ycsb.rows) return fail(c, LTPG_ERR_STATE, "no YCSB table loaded");
-    if (b->n_txn == 0 || b->n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
-    if (b->ops_per_txn == 0 || b->ops_per_txn > c->cfg.max_ops_per_txn || b->op_stride != ycsb_stride(b->ops_per_txn))
-        return fail(c, LTPG_ERR_INVALID, "bad ops_per_txn / op_stride");
-    if (!b->ops || !b->val_off || (b->n_updates && !b->vals)) return fail(c, LTPG_ERR_INVALID, "null batch array");
-    if (b->n_updates > (uint64_t)b->n_txn * b->ops_per_txn) return fail(c, LTPG_ERR_INVALID, "too many updates");
-    const uint64_t n_ops = (uint64_t)b->n_txn * b->op_stride;
-    const uint64_t cap_ops = (uint64_t)c->cfg.max_txn * ycsb_stride(c->cfg.max_ops_per_txn);
-    const uint64_t cap_vals = (uint64_t)c->cfg.max_txn * c->cfg.max_ops_per_txn;
+    if (n_txn == 0 || n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
+    if (k == 0 || k > c->cfg.max_ops_per_txn) return fail(c, LTPG_ERR_INVALID, "bad ops_per_txn / op_stride");
+    if (n_updates > (uint64_t)n_txn * k) return fail(c, LTPG_ERR_INVALID, "too many updates");
     if (!s->ops) {
+        const uint64_t cap_ops = (uint64_t)c->cfg.max_txn * ycsb_stride(c->cfg.max_ops_per_txn);
+        const uint64_t cap_vals = (uint64_t)c->cfg.max_txn * c->cfg.max_ops_per_txn;
         CK(dev_alloc(&s->ops, cap_ops), "alloc ops");
         CK(dev_alloc(&s->val_off, (uint64_t)c->cfg.max_txn + 1), "alloc val_off");
         CK(dev_alloc(&s->vals, cap_vals), "alloc vals");
@@ -330,29 +330,24 @@ int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream
         s->cap_vals = cap_vals;
         s->cap_txn_y = c->cfg.max_txn;
     }
-    int r = ensure_outputs(c, *s, b->n_txn);
+    int r = ensure_outputs(c, *s, n_txn);
     if (r) return r;
-    CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, st), "upload ops");
-    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, st),
-       "upload val_off");
-    if (b->n_updates)
-        CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, st), "upload vals");
-    if (s->workload != LTPG_WORKLOAD_YCSB || s->n_txn != b->n_txn || s->k != b->ops_per_txn) drop_graphs(c);
+    if (s->workload != LTPG_WORKLOAD_YCSB || s->n_txn != n_txn || s->k != k) drop_graphs(c);
     s->workload = LTPG_WORKLOAD_YCSB;
-    s->n_txn = b->n_txn;
-    s->k = b->ops_per_txn;
-    s->stride = b->op_stride;
-    s->n_updates = b->n_updates;
+    s->n_txn = n_txn;
+    s->k = k;
+    s->stride = ycsb_stride(k);
+    s->n_updates = n_updates;
+    *out = s;
     return LTPG_OK;
 }
 
-int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream_t st) {
+int slot_prepare_tpcc(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint64_t n_lines, uint64_t txn_base, Slot **out) {
     Slot *s = get_slot(c, slot);
-    if (!s || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (!s) return fail(c, LTPG_ERR_INVALID, "bad slot or batch");
     if (!c->tpcc.W) return fail(c, LTPG_ERR_STATE, "no TPC-C tables loaded");
-    if (b->n_txn == 0 || b->n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
-    if (b->n_lines > c->cfg.max_lines) return fail(c, LTPG_ERR_INVALID, "batch has more lines than max_lines");
-    if (!b->txns || (b->n_lines && !b->lines)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    if (n_txn == 0 || n_txn > c->cfg.max_txn) return fail(c, LTPG_ERR_INVALID, "batch larger than max_txn");
+    if (n_lines > c->cfg.max_lines) return fail(c, LTPG_ERR_INVALID, "batch has more lines than max_lines");
     if (!s->txns) {
         CK(dev_alloc(&s->txns, c->cfg.max_txn), "alloc txns");
         CK(dev_alloc(&s->lines, (uint64_t)c->cfg.max_lines + 1), "alloc lines");
@@ -360,7 +355,45 @@ int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream
         s->cap_txn_c = c->cfg.max_txn;
         s->cap_lines = c->cfg.max_lines;
     }
-    int r = ensure_outputs(c, *s, b->n_txn);
+    int r = ensure_outputs(c, *s, n_txn);
+    if (r) return r;
+    if (s->workload != LTPG_WORKLOAD_TPCC || s->n_txn != n_txn) drop_graphs(c);
+    s->workload = LTPG_WORKLOAD_TPCC;
+    s->n_txn = n_txn;
+    s->n_lines = (uint32_t)n_lines;
+    s->txn_base = txn_base;
+    *out = s;
+    return LTPG_OK;
+}
+
+int ctx_fail(ltpg_ctx *c, int code, const char *msg) { return fail(c, code, msg); }
+int ctx_cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what) { return cuda_fail(c, e, what); }
+
+}  // namespace ltpg
+
+namespace {
+int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream_t st) {
+    if (!c || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (b->ops_per_txn == 0 || b->op_stride != ycsb_stride(b->ops_per_txn))
+        return fail(c, LTPG_ERR_INVALID, "bad ops_per_txn / op_stride");
+    if (!b->ops || !b->val_off || (b->n_updates && !b->vals)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    Slot *s = nullptr;
+    int r = slot_prepare_ycsb(c, slot, b->n_txn, b->ops_per_txn, b->n_updates, &s);
+    if (r) return r;
+    const uint64_t n_ops = (uint64_t)b->n_txn * b->op_stride;
+    CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, st), "upload ops");
+    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, st),
+       "upload val_off");
+    if (b->n_updates)
+        CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, st), "upload vals");
+    return LTPG_OK;
+}
+
+int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream_t st) {
+    if (!c || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
+    if (!b->txns || (b->n_lines && !b->lines)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    Slot *s = nullptr;
+    int r = slot_prepare_tpcc(c, slot, b->n_txn, b->n_lines, b->txn_base, &s);
     if (r) return r;
     CK(cudaMemcpyAsync(s->txns, b->txns, (uint64_t)b->n_txn * sizeof(ltpg_tpcc_txn), cudaMemcpyHostToDevice, st),
        "upload txns");
@@ -374,14 +407,11 @@ int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream
     // upload may overwrite host_hdr at once
     CK(cudaMemcpyAsync(s->dev_hdr, s->host_hdr, sizeof s->host_hdr, cudaMemcpyHostToDevice, st),
        "upload slot header");
-    if (s->workload != LTPG_WORKLOAD_TPCC || s->n_txn != b->n_txn) drop_graphs(c);
-    s->workload = LTPG_WORKLOAD_TPCC;
-    s->n_txn = b->n_txn;
-    s->n_lines = b->n_lines;
-    s->txn_base = b->txn_base;
     return LTPG_OK;
 }
 }  // namespace
+
+extern "C" {
 
 int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b) {
     return c ? upload_ycsb(c, slot, b, c->stream) : LTPG_ERR_INVALID;
@@ -569,6 +599,60 @@ int ltpg_host_wait(ltpg_ctx *c, uint32_t slot) {
 }
 
 // ---- results -----------------------------------------------------------------
+int ltpg_batch_info_get(ltpg_ctx *c, uint32_t slot, ltpg_batch_info *out) {
+    Slot *s = get_slot(c, slot);
+    if (!s || !out) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    *out = ltpg_batch_info{};
+    // counts made on the device (device generation) are read from it
+    if (s->workload == LTPG_WORKLOAD_YCSB) {
+        uint32_t nu = 0;
+        CK(cudaMemcpyAsync(&nu, s->val_off + s->n_txn, 4, cudaMemcpyDeviceToHost, c->stream), "read update count");
+        int r = ltpg_sync(c);
+        if (r) return r;
+        out->workload = LTPG_WORKLOAD_YCSB;
+        out->ops_per_txn = s->k;
+        out->n_txn = s->n_txn;
+        out->n_op_words = (uint64_t)s->n_txn * s->stride;
+        out->n_updates = nu;
+        return LTPG_OK;
+    }
+    if (s->workload == LTPG_WORKLOAD_TPCC) {
+        uint64_t h[2] = {0, 0};
+        CK(cudaMemcpyAsync(h, s->dev_hdr, sizeof h, cudaMemcpyDeviceToHost, c->stream), "read slot header");
+        int r = ltpg_sync(c);
+        if (r) return r;
+        out->workload = LTPG_WORKLOAD_TPCC;
+        out->n_txn = s->n_txn;
+        out->n_lines = h[0];
+        out->txn_base = h[1];
+        return LTPG_OK;
+    }
+    return fail(c, LTPG_ERR_STATE, "slot holds no batch");
+}
+
+int ltpg_batch_download(ltpg_ctx *c, uint32_t slot, uint32_t part, void *host, size_t bytes) {
+    ltpg_batch_info bi;
+    int r = ltpg_batch_info_get(c, slot, &bi);
+    if (r) return r;
+    const uint64_t n = bi.n_txn;
+    if (!host) return fail(c, LTPG_ERR_INVALID, "null buffer");
+    Slot *s = get_slot(c, slot);
+    const void *src = nullptr;
+    size_t need = 0;
+    if (s->workload == LTPG_WORKLOAD_YCSB) {
+        if (part == 0) src = s->ops, need = bi.n_op_words * 4;
+        else if (part == 1) src = s->val_off, need = (n + 1) * 4;
+        else if (part == 2) src = s->vals, need = bi.n_updates * 8;
+    } else {
+        if (part == 0) src = s->txns, need = n * sizeof(ltpg_tpcc_txn);
+        else if (part == 1) src = s->lines, need = bi.n_lines * sizeof(ltpg_tpcc_line);
+    }
+    if (!src) return fail(c, LTPG_ERR_INVALID, "no such batch part");
+    if (bytes != need) return fail(c, LTPG_ERR_INVALID, "buffer size differs from the batch part");
+    if (need) CK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, c->stream), "batch download");
+    return ltpg_sync(c);
+}
+
 int ltpg_commit_bitmap(ltpg_ctx *c, uint32_t slot, uint32_t *host_bits, size_t words) {
     Slot *s = get_slot(c, slot);
     if (!s || !host_bits) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;

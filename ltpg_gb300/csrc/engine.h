@@ -151,6 +151,13 @@ namespace ltpg {
 void prof_mark(ltpg_ctx *c, int i);
 // Drops the cached CUDA graphs (launch settings changed).
 void drop_graphs_ctx(ltpg_ctx *c);
+// Readies slot `slot` for a batch of the given shape (buffers, outputs, graph
+// invalidation) and records the shape; the caller fills the batch buffers.
+int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, uint32_t n_updates, Slot **out);
+int slot_prepare_tpcc(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint64_t n_lines, uint64_t txn_base, Slot **out);
+// Record an error message on the context and return its code.
+int ctx_fail(ltpg_ctx *c, int code, const char *msg);
+int ctx_cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what);
 // Predictor step after a tuned YCSB batch (predictor.cu).
 cudaError_t predictor_after_batch(ltpg_ctx *c);
 void predictor_free(ltpg_ctx *c);

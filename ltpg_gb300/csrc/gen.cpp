@@ -16,118 +16,29 @@
 #include <thread>
 #include <vector>
 
-#include "proto.h"
+#include "gen_state.h"
 
 using namespace ltpg;
 
+using namespace ltpg::gen;
+
 namespace {
 
-constexpr uint64_t DOM_YCSB_OPS = 0x59435342ull;   // "YCSB"
-constexpr uint64_t DOM_YCSB_VAL = 0x56414C55ull;   // "VALU"
-constexpr uint64_t DOM_YCSB_PERM = 0x5045524Dull;  // "PERM"
-constexpr uint64_t DOM_TPCC = 0x54504343ull;       // "TPCC"
-
-struct Rng {
-    uint64_t s;
-    explicit Rng(uint64_t seed) : s(seed) {}
-    uint64_t next() {
-        s += 0x9E3779B97F4A7C15ull;
-        uint64_t z = s;
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        return z ^ (z >> 31);
-    }
-    // Uniform in [0, n) by Lemire's multiply-shift (no modulo bias worth noting
-    // at these sizes, integer only).
-    uint64_t below(uint64_t n) { return (uint64_t)(((unsigned __int128)next() * n) >> 64); }
-    // Uniform in [a, b].
-    uint64_t range(uint64_t a, uint64_t b) { return a + below(b - a + 1); }
-    double unit() { return (double)(next() >> 11) * 0x1.0p-53; }
-};
-
-// Bijection of [0, n) keyed by k: a 4-round Feistel network over the smallest
-// even bit width covering n, with cycle walking back into range.
-struct Perm {
-    uint64_t n = 0, key = 0;
-    uint32_t half = 1;
-    void init(uint64_t n_, uint64_t key_) {
-        n = n_;
-        key = key_;
-        uint32_t bits = 2;
-        while (bits < 64 && (1ull << bits) < n) bits += 2;
-        half = bits / 2;
-    }
-    uint64_t round_fn(uint64_t x, uint32_t r) const {
-        return splitmix64(x ^ (key + 0x1234567ull * (r + 1))) & ((1ull << half) - 1);
-    }
-    uint64_t once(uint64_t x) const {
-        const uint64_t m = (1ull << half) - 1;
-        uint64_t l = x >> half, rr = x & m;
-        for (uint32_t r = 0; r < 4; ++r) {
-            uint64_t t = l ^ round_fn(rr, r);
-            l = rr;
-            rr = t;
-        }
-        return (l << half) | rr;
-    }
-    uint64_t operator()(uint64_t x) const {
-        uint64_t y = once(x);
-        while (y >= n) y = once(y);
-        return y;
-    }
-};
-
-// Zipfian ranks by the method of Gray, Sundaresan, Englert, Baclawski and
-// Weinberger, "Quickly generating billion-record synthetic databases" (SIGMOD
-// 1994), the sampler YCSB uses.  Rank 0 is the most popular.
-struct Zipf {
-    uint64_t n = 0;
-    double theta = 0, zetan = 0, alpha = 0, eta = 0, half_pow = 0;
-    void init(uint64_t n_, double th) {
-        n = n_;
-        theta = th;
-        if (theta == 0.0) return;
-        double z = 0.0;
-        for (uint64_t i = 1; i <= n; ++i) z += 1.0 / std::pow((double)i, theta);
-        zetan = z;
-        const double zeta2 = 1.0 + std::pow(0.5, theta);
-        alpha = 1.0 / (1.0 - theta);
-        eta = (1.0 - std::pow(2.0 / (double)n, 1.0 - theta)) / (1.0 - zeta2 / zetan);
-        half_pow = std::pow(0.5, theta);
-    }
-    uint64_t sample(Rng &r) const {
-        if (theta == 0.0) return r.below(n);
-        const double u = r.unit();
-        const double uz = u * zetan;
-        if (uz < 1.0) return 0;
-        if (uz < 1.0 + half_pow) return n > 1 ? 1 : 0;
-        uint64_t v = (uint64_t)((double)n * std::pow(eta * u - eta + 1.0, alpha));
-        return v < n ? v : n - 1;
-    }
-};
+void zipf_init(Zipf &z, uint64_t n, double theta) {
+    z = Zipf{};
+    z.n = n;
+    z.theta = theta;
+    if (theta == 0.0) return;
+    double sum = 0.0;
+    for (uint64_t i = 1; i <= n; ++i) sum += 1.0 / std::pow((double)i, theta);
+    z.zetan = sum;
+    const double zeta2 = 1.0 + std::pow(0.5, theta);
+    z.alpha = 1.0 / (1.0 - theta);
+    z.eta = (1.0 - std::pow(2.0 / (double)n, 1.0 - theta)) / (1.0 - zeta2 / z.zetan);
+    z.half_pow = std::pow(0.5, theta);
+}
 
 }  // namespace
-
-struct ltpg_gen {
-    int kind = 0;
-    ltpg_ycsb_params y{};
-    ltpg_tpcc_params c{};
-    Zipf zipf;
-    // TPC-C per-warehouse counters (TF/Query.h:54-88,157-166).
-    std::vector<uint32_t> o_id, no_id, ol_id, h_id;
-    // By-name Payments: C_LAST of every customer of the loaded image and its
-    // rank among the customers of its district with that name, in C_ID order.
-    std::vector<uint16_t> cust_name;
-    std::vector<uint8_t> cust_rank;
-    // OrderStatus / Delivery: the orders this generator made, per warehouse
-    // (indexed by O_ID): customer, district, first OL_ID, line count; how many
-    // were made and delivered.
-    std::vector<uint16_t> o_cust;
-    std::vector<uint8_t> o_dist, o_cnt;
-    std::vector<uint32_t> o_ol;
-    std::vector<uint64_t> made, delivered;
-    uint64_t next_batch = 0, txn_base = 0;
-};
 
 extern "C" {
 
@@ -145,7 +56,7 @@ int ltpg_gen_create_ycsb(const ltpg_ycsb_params *p, ltpg_gen **out) {
     if (!g) return LTPG_ERR_NOMEM;
     g->kind = LTPG_WORKLOAD_YCSB;
     g->y = *p;
-    g->zipf.init(p->n_records, p->theta);
+    zipf_init(g->zipf, p->n_records, p->theta);
     *out = g;
     return LTPG_OK;
 }
@@ -194,6 +105,7 @@ int ltpg_gen_create_tpcc(const ltpg_tpcc_params *p, ltpg_gen **out) {
 }
 
 int ltpg_gen_destroy(ltpg_gen *g) {
+    if (g) gen_dev_free(g);
     delete g;
     return LTPG_OK;
 }
@@ -222,40 +134,8 @@ int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t 
     // Pass 1: op words and per-transaction update counts, in parallel over
     // transactions (each has its own stream, so the split does not matter).
     auto fill = [&](uint32_t t0, uint32_t t1) {
-        uint32_t keys[LTPG_YCSB_MAX_OPS];
-        for (uint32_t t = t0; t < t1; ++t) {
-            Rng r(hash3(p.seed ^ DOM_YCSB_OPS, batch_id, t));
-            uint32_t nupd = 0;
-            uint32_t *w = ops + (uint64_t)t * stride;
-            for (uint32_t j = 0; j < k; ++j) {
-                uint64_t key = 0;
-                for (uint32_t attempt = 0;; ++attempt) {
-                    uint64_t rank = g->zipf.sample(r);
-                    key = rotate ? perm(rank) : rank;
-                    if (attempt >= 64) {  // pathological tiny tables: walk to a free key
-                        for (;;) {
-                            bool dup = false;
-                            for (uint32_t q = 0; q < j; ++q) dup |= keys[q] == key;
-                            if (!dup) break;
-                            key = (key + 1) % p.n_records;
-                        }
-                        break;
-                    }
-                    bool dup = false;
-                    for (uint32_t q = 0; q < j; ++q) dup |= keys[q] == key;
-                    if (!dup) break;
-                }
-                keys[j] = (uint32_t)key;
-                const bool upd = r.below(100) < p.update_pct;
-                const uint32_t field = (uint32_t)r.below(LTPG_YCSB_FIELDS);
-                // a read scans scan_len keys when scan_len >= 2 (span in the field bits)
-                const uint32_t span = p.scan_len >= 2u ? p.scan_len - 1u : 0u;
-                w[j] = ycsb_word((uint32_t)key, upd, upd ? field : span);
-                nupd += upd;
-            }
-            for (uint32_t j = k; j < stride; ++j) w[j] = LTPG_YCSB_OP_PAD;
-            val_off[t + 1] = nupd;
-        }
+        for (uint32_t t = t0; t < t1; ++t)
+            val_off[t + 1] = ycsb_txn(p, g->zipf, rotate ? &perm : nullptr, batch_id, t, ops + (uint64_t)t * stride);
     };
     unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     if ((uint64_t)B * k < 200000) nth = 1;
@@ -275,7 +155,7 @@ int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t 
         uint32_t v = val_off[t];
         const uint32_t *w = ops + (uint64_t)t * stride;
         for (uint32_t j = 0; j < k; ++j)
-            if (ycsb_is_update(w[j])) vals[v++] = hash3(p.seed ^ DOM_YCSB_VAL, txn0 + t, j);
+            if (ycsb_is_update(w[j])) vals[v++] = ycsb_value(p, txn0 + t, j);
     }
     out->n_txn = B;
     out->ops_per_txn = k;
@@ -291,145 +171,63 @@ int ltpg_gen_tpcc_batch(ltpg_gen *g, uint64_t batch_id, ltpg_tpcc_txn *txns,
                         ltpg_tpcc_line *lines, ltpg_tpcc_batch *out) {
     if (!g || g->kind != LTPG_WORKLOAD_TPCC || !txns || !lines || !out) return LTPG_ERR_INVALID;
     if (batch_id != g->next_batch) return LTPG_ERR_STATE;  // counters advance in batch order
+    if (g->dev_bound) return LTPG_ERR_STATE;  // the counters live on the device
     const ltpg_tpcc_params &p = g->c;
-    const uint32_t W = p.warehouses;
-    // NURand of the reference, without the run-time constant C (Random.h:72-75).
-    auto nurand = [](Rng &r, uint64_t A, uint64_t x, uint64_t y) {
-        return ((r.range(0, A) | r.range(x, y)) % (y - x + 1)) + x;
-    };
-    auto other_w = [&](Rng &r, uint32_t w) {
-        uint32_t o = (uint32_t)r.below(W - 1);
-        return o >= w ? o + 1 : o;
-    };
+    const bool tracking = !g->made.empty();
+    const uint16_t *cname = g->cust_name.data();
+    const uint8_t *crank = g->cust_rank.data();
     uint32_t nl = 0;
     for (uint32_t t = 0; t < p.n_txn; ++t) {
         Rng r(hash3(p.seed ^ DOM_TPCC, batch_id, t));
         ltpg_tpcc_txn &x = txns[t];
         memset(&x, 0, sizeof x);
         x.line_off = nl;
-        // kind: NewOrder, then OrderStatus, Delivery, StockLevel, else Payment
-        const uint32_t u = (uint32_t)r.below(100);
-        const bool is_no = u < p.neworder_pct;
-        const uint32_t c_os = p.neworder_pct + p.orderstatus_pct, c_dl = c_os + p.delivery_pct,
-                       c_sl = c_dl + p.stocklevel_pct;
-        const uint32_t w = (uint32_t)r.below(W), d = (uint32_t)r.below(10);
+        const TpccHead h = tpcc_head(p, r);
+        const uint32_t w = h.w;
         x.w = w;
-        const bool tracking = !g->made.empty();
-        // by last name (TF/Query.h:174-181): the query names customer (cw, cd,
-        // c) by its C_LAST and its rank among that name's holders
-        auto by_name = [&](uint32_t cw, uint32_t cd) {
-            if (p.by_name_pct && r.below(100) < p.by_name_pct) {
-                const uint64_t row = 30000ull * cw + 3000ull * cd + x.c_id;
-                if (g->cust_rank[row] < 255u) {
-                    x.kind_info |= LTPG_PAY_BY_NAME;
-                    x.c_id = ((uint32_t)g->cust_name[row] << 8) | g->cust_rank[row];
-                }
-            }
+        auto order = [&](uint32_t o) {
+            const size_t k = 30000ull * w + o;
+            return TpccOrder{g->o_cust[k], g->o_dist[k], g->o_ol[k], g->o_cnt[k]};
         };
-        if (!is_no && u < c_os) {
-            // OrderStatus (TA/Query.h:214-246): a recent order of warehouse w
-            // and one of its lines, read with its customer
-            uint32_t cd = d, o, ol;
-            if (tracking && g->made[w]) {
-                const uint64_t back = r.below(std::min<uint64_t>(g->made[w], 1000));
-                o = (uint32_t)((g->o_id[w] + 30000u - 1u - (uint32_t)back) % 30000u);
-                const size_t k = 30000ull * w + o;
-                cd = g->o_dist[k];
-                x.c_id = g->o_cust[k];
-                ol = (uint32_t)((g->o_ol[k] + r.below(std::max<uint32_t>(1u, g->o_cnt[k]))) % 450000u);
-            } else {
-                x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
-                o = (uint32_t)r.below(30000);
-                ol = (uint32_t)r.below(450000);
-            }
-            x.kind_info = LTPG_TPCC_ORDERSTATUS | (cd << 16) | (cd << 24);
-            x.c_w = w;
-            x.a = o;
-            x.b = ol;
-            by_name(w, cd);
-            continue;
-        }
-        if (!is_no && u < c_dl) {
-            // Delivery (TA/Query.h:247-269): the oldest undelivered order of w
-            uint32_t cd = d, o, ol;
-            if (tracking && g->delivered[w] < g->made[w]) {
+        switch (h.kind) {
+        case LTPG_TPCC_ORDERSTATUS:
+            tpcc_orderstatus(p, r, h, x, tracking ? g->made[w] : 0u, g->o_id[w], order, cname, crank);
+            break;
+        case LTPG_TPCC_DELIVERY: {
+            const bool tracked = tracking && g->delivered[w] < g->made[w];
+            uint32_t o = 0;
+            if (tracked) {
                 if (g->made[w] - g->delivered[w] > 30000u) g->delivered[w] = g->made[w] - 30000u;
                 o = (uint32_t)(g->delivered[w]++ % 30000u);
-                const size_t k = 30000ull * w + o;
-                cd = g->o_dist[k];
-                x.c_id = g->o_cust[k];
-                ol = g->o_ol[k];
-            } else {
-                x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
-                o = (uint32_t)r.below(30000);
-                ol = (uint32_t)r.below(450000);
             }
-            const uint32_t carrier = (uint32_t)r.range(1, 10);
-            x.kind_info = LTPG_TPCC_DELIVERY | (carrier << 8) | (cd << 16);
-            x.c_w = w;
-            x.a = o;
-            x.b = o;  // NO_ID and O_ID advance together (TF/Query.h:54-88)
-            x.c = ol;
-            continue;
+            tpcc_delivery(r, h, x, tracked, o, order);
+            break;
         }
-        if (!is_no && u < c_sl) {
-            // StockLevel (TA/Query.h:270-296): one stock row of w
-            const uint32_t threshold = (uint32_t)r.range(10, 20);
-            x.kind_info = LTPG_TPCC_STOCKLEVEL | (threshold << 8) | (d << 16);
-            x.c_w = w;
-            x.a = (uint32_t)nurand(r, 8191, 1, 100000) - 1;
-            continue;
-        }
-        if (is_no) {
-            const uint32_t cnt = (uint32_t)r.range(5, LTPG_TPCC_MAX_LINES);
-            x.kind_info = LTPG_TPCC_NEWORDER | (cnt << 8) | (d << 16);
-            x.c_w = w;
-            x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
+        case LTPG_TPCC_STOCKLEVEL:
+            tpcc_stocklevel(r, h, x);
+            break;
+        case LTPG_TPCC_NEWORDER:
             x.a = g->o_id[w];
             g->o_id[w] = (g->o_id[w] + 1) % 30000u;
             x.b = g->no_id[w];
             g->no_id[w] = (g->no_id[w] + 1) % 30000u;
             x.c = g->ol_id[w];
-            g->ol_id[w] = (g->ol_id[w] + cnt) % 450000u;
+            g->ol_id[w] = (g->ol_id[w] + h.cnt) % 450000u;
+            tpcc_neworder(p, r, h, x, lines + nl);
             if (tracking) {
                 const size_t k = 30000ull * w + x.a;
                 g->o_cust[k] = (uint16_t)x.c_id;
-                g->o_dist[k] = (uint8_t)d;
+                g->o_dist[k] = (uint8_t)h.d;
                 g->o_ol[k] = x.c;
-                g->o_cnt[k] = (uint8_t)cnt;
+                g->o_cnt[k] = (uint8_t)h.cnt;
                 g->made[w]++;
             }
-            for (uint32_t i = 0; i < cnt; ++i) {
-                ltpg_tpcc_line &ln = lines[nl + i];
-                uint32_t item;
-                for (;;) {  // distinct items within an order (TF/Query.h:103-114)
-                    item = (uint32_t)nurand(r, 8191, 1, 100000) - 1;
-                    bool dup = false;
-                    for (uint32_t q = 0; q < i; ++q) dup |= lines[nl + q].i_id == item;
-                    if (!dup) break;
-                }
-                ln.i_id = item;
-                const bool remote = W > 1 && r.below(100) < p.remote_line_pct;
-                ln.supply_w = (uint16_t)(remote ? other_w(r, w) : w);
-                ln.qty = (uint16_t)r.range(1, 10);
-            }
-            nl += cnt;
-        } else {
-            const bool remote = W > 1 && r.below(100) < p.remote_pay_pct;
-            uint32_t c_w = w, c_d = d;
-            if (remote) {
-                c_w = other_w(r, w);
-                c_d = (uint32_t)r.below(10);
-            }
-            x.kind_info = LTPG_TPCC_PAYMENT | (d << 16) | (c_d << 24);
-            x.c_w = c_w;
-            x.c_id = (uint32_t)nurand(r, 1023, 1, 3000) - 1;
-            const uint64_t amount = r.range(100, 500000);
+            nl += h.cnt;
+            break;
+        default:  // Payment
             x.a = g->h_id[w];
             g->h_id[w] = (g->h_id[w] + 1) % 30000u;
-            x.b = (uint32_t)amount;
-            x.c = (uint32_t)(amount >> 32);
-            by_name(c_w, c_d);
+            tpcc_payment(p, r, h, x, cname, crank);
         }
     }
     out->n_txn = p.n_txn;
