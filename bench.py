@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=32)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
+    ap.add_argument("--no-device-gen", action="store_true", help="skip the device-generator section")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
     ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--no-reference-gpu", action="store_true",
@@ -125,10 +126,16 @@ class Clocks:
         self.p = None
 
     def __enter__(self):
+        import select
+        self.first = ""
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # the first sample is taken before the region opens, so a region
+            # shorter than the sampling period still has the state at its start
+            if select.select([self.p.stdout], [], [], 5.0)[0]:
+                self.first = self.p.stdout.readline()
         except OSError:
             self.p = None
         self.t0 = time.time()
@@ -141,7 +148,7 @@ class Clocks:
             return
         self.p.terminate()
         out, _ = self.p.communicate(timeout=10)
-        for line in out.strip().splitlines():
+        for line in (self.first + out).strip().splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) >= 8:
                 self.rows.append(f)
@@ -637,6 +644,8 @@ def main():
         line["reference_shapes"] = engine_on_ref_shapes(200)
     if not args.no_serving and args.workload == "ycsb_hc":
         line["serving"] = serving_section(args)
+    if not args.no_device_gen and args.workload in ("ycsb_hc", "tpcc", "tpcc_mix"):
+        line["device_generator"] = device_gen_section(w)
     if args.sweep and w["kind"] == "ycsb":
         sweep = {}
         for th in [0.0, 0.6, 0.8, 0.99]:
@@ -645,6 +654,62 @@ def main():
                               "plain": r["plain"]["commits"] / r["plain"]["secs"]}
         line["theta_sweep"] = sweep
     print(json.dumps(line), flush=True)
+
+
+def device_gen_section(w, reps=8):
+    """Batches of this workload generated on the GPU (ltpg_gen_*_batch_device,
+    byte-identical to the host generator): ms per batch on the device (CUDA
+    events) and on the host (one call, all host threads for YCSB, one for the
+    sequential TPC-C loop), and committed txn/s of steps that generate their
+    batch on the device and run it (graph mode)."""
+    import torch
+    import ltpg_gb300 as L
+    B = w["n_txn"]
+    if w["kind"] == "ycsb":
+        e = L.Engine(device=0, n_slots=2, max_txn=B, max_ops_per_txn=w["ops"])
+        e.load_ycsb(SEED, w["n_records"])
+        g = L.YcsbGenerator(SEED, w["n_records"], B, w["ops"], w["update_pct"], w["theta"], w["rotate_every"],
+                            w.get("scan_len", 0))
+        gen = lambda slot, i: e.generate(slot, g, 100 + i)  # noqa: E731
+        t0 = time.time()
+        g.batch(99)
+        host_ms = (time.time() - t0) * 1e3
+    else:
+        e = L.Engine(device=0, n_slots=2, max_txn=B, max_ops_per_txn=16, max_lines=15 * B)
+        e.load_tpcc(SEED, w["warehouses"])
+        gh = L.TpccGenerator(SEED + 1, w["warehouses"], B, **w.get("mix", {}))
+        t0 = time.time()
+        gh.next()
+        host_ms = (time.time() - t0) * 1e3
+        g = L.TpccGenerator(SEED + 1, w["warehouses"], B, **w.get("mix", {}))
+        gen = lambda slot, i: e.generate(slot, g)  # noqa: E731
+    try:
+        stream = torch.cuda.ExternalStream(e.stream())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for i in range(3):
+            gen(i % 2, i)
+            e.run_batch(i % 2, "graph")
+        e.sync()
+        ev[0].record(stream)
+        for i in range(reps):
+            gen(i % 2, 3 + i)
+        ev[1].record(stream)
+        c0 = e.counters()[0]
+        ev[2].record(stream)
+        for i in range(reps):
+            gen(i % 2, 3 + reps + i)
+            e.run_batch(i % 2, "graph")
+        ev[3].record(stream)
+        e.sync()
+        commits = e.counters()[0] - c0
+        gen_ms = ev[0].elapsed_time(ev[1]) / reps
+        step_ms = ev[2].elapsed_time(ev[3]) / reps
+    finally:
+        e.close()
+    return {"device_ms_per_batch": gen_ms, "host_ms_per_batch": host_ms,
+            "host_threads": os.cpu_count() if w["kind"] == "ycsb" else 1,
+            "generate_and_run": {"value": commits / (step_ms * reps / 1e3), "unit": "txn/s",
+                                 "ms_per_step": step_ms}}
 
 
 def serving_section(args):

@@ -7,7 +7,7 @@
 // into fused multiply-adds (host: -ffp-contract=off; device: -fmad=false):
 // those round the same on x86-64, aarch64 and the GPU.  Library pow / exp / log
 // are not correctly rounded and differ between glibc and CUDA in the last ulp,
-// so the sampler's power is computed by the series below.
+// so the sampler's power is computed below from series and tables of our own.
 #pragma once
 #include <string.h>
 
@@ -176,6 +176,77 @@ LTPG_HDI double det_pow(double x, double a) {
     return det_exp(a * det_log(x));
 }
 
+// ---- table-driven power (the sampler's) ---------------------------------
+// Tang's table-driven methods (P. T. P. Tang, "Table-driven implementation of
+// the exponential function in IEEE floating-point arithmetic", ACM TOMS 15,
+// 1989; "... of the logarithm function", ACM TOMS 16, 1990): a table entry
+// takes the argument to within 2^-8 (log) or ln 2 / 128 (exp) of an anchor,
+// where a degree-7 / degree-6 polynomial suffices — about half the
+// operations of the series above and no division.  The tables are filled
+// once on the host by the series functions and copied to the device as they
+// are, so both sides hold the same bits.
+struct PowTables {
+    double log_r[97];  // r_j = 1 / (3/4 + j / 128), rounded
+    double log_c[97];  // -ln r_j
+    double exp_t[64];  // 2^(j / 64)
+};
+inline void pow_tables_fill(PowTables &t) {
+    for (int j = 0; j <= 96; ++j) {
+        t.log_r[j] = 1.0 / (0.75 + j / 128.0);
+        t.log_c[j] = -det_log(t.log_r[j]);
+    }
+    for (int j = 0; j < 64; ++j) t.exp_t[j] = det_exp(j * (LN2 / 64.0));
+}
+// ln x for normal x > 0: x = m 2^e with m in [3/4, 3/2) (so that x near 1
+// has e = 0 and nothing cancels), j = m's nearest 1/128 step from 3/4;
+// ln m = -ln r_j + ln(m r_j), m r_j - 1 exact (Sterbenz), |z| < 2^-7.
+LTPG_HDI double tab_log(const PowTables &t, double x) {
+    const uint64_t b = dbits(x);
+    int e = (int)((b >> 52) & 0x7FF) - 1023;
+    const uint64_t mant = b & 0x000FFFFFFFFFFFFFull;
+    double m = dfrom(mant | 0x3FF0000000000000ull);  // [1, 2)
+    if (mant >= (1ull << 51)) {                        // m >= 3/2
+        m = m * 0.5;
+        e += 1;
+    }
+    const int j = (int)dfloor((m - 0.75) * 128.0 + 0.5);  // 0 .. 96; m - 3/4 exact
+    const double z = m * t.log_r[j] - 1.0;
+    double p = 1.0 / 7.0;
+    p = p * z - 1.0 / 6.0;
+    p = p * z + 1.0 / 5.0;
+    p = p * z - 1.0 / 4.0;
+    p = p * z + 1.0 / 3.0;
+    p = p * z - 0.5;
+    p = p * z + 1.0;
+    return ((double)e * LN2 + t.log_c[j]) + p * z;
+}
+// e^y for y <= 0: y = (64 k + j) ln 2 / 64 + r (Cody-Waite, |r| <= ln 2 / 128),
+// e^y = 2^k 2^(j/64) e^r.
+LTPG_HDI double tab_exp(const PowTables &t, double y) {
+    if (y < -745.0) return 0.0;
+    const double kd = dfloor(y * (64.0 / LN2) + 0.5);
+    const double r = (y - kd * (LN2_HI / 64.0)) - kd * (LN2_LO / 64.0);
+    double p = 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    const int ki = (int)kd;
+    int k = ki >> 6;  // floor division (arithmetic shift)
+    double v = t.exp_t[ki & 63] * p;
+    if (k < -1022) {  // subnormal result: two exact-exponent steps
+        v = v * dfrom((uint64_t)(1023 - 600) << 52);
+        k += 600;
+    }
+    return v * dfrom((uint64_t)(k + 1023) << 52);
+}
+LTPG_HDI double tab_pow(const PowTables &t, double x, double a) {
+    if (!(x >= 2.2250738585072014e-308)) return 0.0;
+    return tab_exp(t, a * tab_log(t, x));
+}
+
 // Zipfian ranks by the method of Gray, Sundaresan, Englert, Baclawski and
 // Weinberger, "Quickly generating billion-record synthetic databases" (SIGMOD
 // 1994), the sampler YCSB uses.  Rank 0 is the most popular.  The constants
@@ -183,13 +254,13 @@ LTPG_HDI double det_pow(double x, double a) {
 struct Zipf {
     uint64_t n = 0;
     double theta = 0, zetan = 0, alpha = 0, eta = 0, half_pow = 0;
-    LTPG_HDI uint64_t sample(Rng &r) const {
+    LTPG_HDI uint64_t sample(Rng &r, const PowTables &tab) const {
         if (theta == 0.0) return r.below(n);
         const double u = r.unit();
         const double uz = u * zetan;
         if (uz < 1.0) return 0;
         if (uz < 1.0 + half_pow) return n > 1 ? 1 : 0;
-        const uint64_t v = (uint64_t)((double)n * det_pow(eta * u - eta + 1.0, alpha));
+        const uint64_t v = (uint64_t)((double)n * tab_pow(tab, eta * u - eta + 1.0, alpha));
         return v < n ? v : n - 1;
     }
 };
@@ -197,8 +268,8 @@ struct Zipf {
 // Op words of YCSB transaction t of batch batch_id (distinct keys; a read
 // scans scan_len keys when scan_len >= 2, its span in the field bits); pads to
 // the op stride.  Returns the number of updates.
-LTPG_HDI uint32_t ycsb_txn(const ltpg_ycsb_params &p, const Zipf &zipf, const Perm *perm, uint64_t batch_id,
-                           uint32_t t, uint32_t *w) {
+LTPG_HDI uint32_t ycsb_txn(const ltpg_ycsb_params &p, const Zipf &zipf, const PowTables &tab, const Perm *perm,
+                           uint64_t batch_id, uint32_t t, uint32_t *w) {
     Rng r(hash3(p.seed ^ DOM_YCSB_OPS, batch_id, t));
     const uint32_t k = p.ops_per_txn, stride = ycsb_stride(k);
     uint32_t keys[LTPG_YCSB_MAX_OPS];
@@ -206,7 +277,7 @@ LTPG_HDI uint32_t ycsb_txn(const ltpg_ycsb_params &p, const Zipf &zipf, const Pe
     for (uint32_t j = 0; j < k; ++j) {
         uint64_t key = 0;
         for (uint32_t attempt = 0;; ++attempt) {
-            const uint64_t rank = zipf.sample(r);
+            const uint64_t rank = zipf.sample(r, tab);
             key = perm ? (*perm)(rank) : rank;
             if (attempt >= 64) {  // pathological tiny tables: walk to a free key
                 for (;;) {

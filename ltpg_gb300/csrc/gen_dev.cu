@@ -140,6 +140,7 @@ uint32_t scan_scratch(uint32_t n) { return (n + SCAN_BLOCK - 1) / SCAN_BLOCK + 1
 struct YcsbGenArgs {
     ltpg_ycsb_params p;
     Zipf zipf;
+    const PowTables *tab;
     Perm perm;
     bool rotate;
     uint64_t batch_id;
@@ -152,7 +153,8 @@ __global__ void __launch_bounds__(TB) ycsb_gen_ops(YcsbGenArgs a) {
     if (t == 0) a.val_off[0] = 0;
     if (t >= a.p.n_txn) return;
     const uint32_t stride = ycsb_stride(a.p.ops_per_txn);
-    a.val_off[t + 1] = ycsb_txn(a.p, a.zipf, a.rotate ? &a.perm : nullptr, a.batch_id, t, a.ops + (uint64_t)t * stride);
+    a.val_off[t + 1] =
+        ycsb_txn(a.p, a.zipf, *a.tab, a.rotate ? &a.perm : nullptr, a.batch_id, t, a.ops + (uint64_t)t * stride);
 }
 
 __global__ void __launch_bounds__(TB) ycsb_gen_vals(YcsbGenArgs a) {
@@ -459,9 +461,11 @@ uint32_t blocks(uint64_t n, uint32_t per) { return (uint32_t)((n + per - 1) / pe
 
 }  // namespace
 
-// Device copy of a TPC-C generator's state, and the scratch of one batch.
+// Device side of a generator: YCSB, the sampler's power tables; TPC-C, the
+// generator's state and the scratch of one batch.
 struct ltpg_gen_dev {
     int device = -1;
+    PowTables *tab = nullptr;
     uint32_t G = 0, C = 0;
     uint32_t *o_id = nullptr, *no_id = nullptr, *ol_id = nullptr, *h_id = nullptr;
     uint64_t *made = nullptr, *delivered = nullptr;
@@ -554,6 +558,21 @@ cudaError_t bind_tpcc(ltpg_gen *g, int device) {
     return cudaSuccess;
 }
 
+// The YCSB generator's power tables on the device (first device batch).
+cudaError_t bind_ycsb(ltpg_gen *g, int device) {
+    ltpg_gen_dev *d = new (std::nothrow) ltpg_gen_dev();
+    if (!d) return cudaErrorMemoryAllocation;
+    d->device = device;
+    cudaError_t e = dalloc(d, &d->tab, 1);
+    if (e == cudaSuccess) e = cudaMemcpy(d->tab, &host_pow_tables(), sizeof(PowTables), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        free_dev(d);
+        return e;
+    }
+    g->dev = d;
+    return cudaSuccess;
+}
+
 }  // namespace
 
 void gen_dev_free(ltpg_gen *g) {
@@ -569,12 +588,17 @@ int ltpg_gen_ycsb_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint
     const ltpg_ycsb_params &p = g->y;
     if (cudaSetDevice(c->device) != cudaSuccess) return ctx_fail(c, LTPG_ERR_CUDA, "set device");
     if (p.n_records > c->ycsb.n) return ctx_fail(c, LTPG_ERR_INVALID, "generator keys exceed the loaded table");
+    if (g->dev && g->dev->device != c->device)
+        return ctx_fail(c, LTPG_ERR_INVALID, "generator tables live on another device");
     Slot *s = nullptr;
     int r = slot_prepare_ycsb(c, slot, p.n_txn, p.ops_per_txn, 0, &s);
     if (r) return r;
+    cudaError_t e0 = cudaSuccess;
+    if (!g->dev && (e0 = bind_ycsb(g, c->device)) != cudaSuccess) return ctx_cuda_fail(c, e0, "generator tables");
     YcsbGenArgs a;
     a.p = p;
     a.zipf = g->zipf;
+    a.tab = g->dev->tab;
     a.rotate = p.rotate_every != 0;
     if (a.rotate) a.perm.init(p.n_records, hash3(p.seed ^ DOM_YCSB_PERM, batch_id / p.rotate_every, 0));
     a.batch_id = batch_id;

@@ -34,3 +34,5 @@ struct ltpg_gen {
 
 // Frees the device state of g (gen_dev.cu).
 void gen_dev_free(ltpg_gen *g);
+// The sampler's power tables, filled once (gen.cpp).
+const ltpg::gen::PowTables &host_pow_tables();
