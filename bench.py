@@ -598,7 +598,7 @@ def main():
         kernel, kbytes, kms = (ek, eb, exec_ms) if exec_ms >= cwb_ms else ("ycsb_checkwb_tuned", cb, cwb_ms)
     else:
         # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
-        eb, cb = tpcc_bytes_per_txn(w.get("mix"))
+        eb, cb = tpcc_bytes_per_txn(w.get("mix"), commit_rate)
         kernel, kbytes, kms = ("tpcc_exec_tuned", eb, exec_ms) if exec_ms >= cwb_ms else \
             ("tpcc_checkwb_tuned", cb, cwb_ms)
     achieved = kbytes * B / (kms / 1e3) / 1e9 if kms > 0 else None
@@ -777,7 +777,7 @@ def predictor_section(w, batches):
     return out
 
 
-def tpcc_bytes_per_txn(mix=None):
+def tpcc_bytes_per_txn(mix=None, commit_rate=1.0):
     """Algorithmic bytes per TPC-C transaction (10 lines per NewOrder on
     average), weighted by the workload's mix (default 50/50 NewOrder/Payment).
     Only ops that can conflict register and check: no transaction writes a
@@ -788,20 +788,24 @@ def tpcc_bytes_per_txn(mix=None):
     StockLevel 1.  Execute: 32 B record + 8 B per line, 16 B registration per
     op (Delivery's read-and-write rows: 32), reads W/D tax, C discount, item
     price, balance, OL_AMOUNT, S_QUANTITY (8 B each).  Check+write-back: record
-    and lines again, 16 B slot load per op, committed writes (NewOrder: ORDER
-    64, NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE 80 + price and
-    dist reads 16; Payment: 2 hot adds 16, customer 3x8 read+write, HISTORY 64;
-    Delivery: NEW-ORDER 24, carrier 8, delivery date 8, customer 2x8 read+write)."""
+    and lines again, 16 B slot load per op, flag and bitmap bytes, and the
+    writes of committed transactions, weighted by the measured commit rate
+    (NewOrder: ORDER 64, NEW-ORDER 24, per line stock 4x8 read+write, ORDER-LINE
+    80 + price and dist reads 16; Payment: 2 hot adds 16, customer 3x8
+    read+write, HISTORY 64; Delivery: NEW-ORDER 24, carrier 8, delivery date 8,
+    customer 2x8 read+write)."""
     mix = mix or {}
     no = mix.get("neworder_pct", 50)
     os_, dl, sl = mix.get("orderstatus_pct", 0), mix.get("delivery_pct", 0), mix.get("stocklevel_pct", 0)
     pay = 100 - no - os_ - dl - sl
     ex = {"no": 32 + 80 + 16 * 23 + 24 + 8 * 10 + 8, "pay": 32 + 16 * 3 + 8 + 8, "os": 32 + 16 * 3 + 8,
           "dl": 32 + 16 * 6 + 8, "sl": 32 + 16 + 8}
-    cw = {"no": 32 + 80 + 16 * 23 + 64 + 24 + 10 * (64 + 80 + 16) + 2, "pay": 32 + 16 * 3 + 16 + 48 + 64 + 2,
-          "os": 32 + 16 * 3 + 2, "dl": 32 + 16 * 4 + 24 + 8 + 8 + 32 + 2, "sl": 32 + 16 + 2}
+    ck = {"no": 32 + 80 + 16 * 23 + 2, "pay": 32 + 16 * 3 + 2, "os": 32 + 16 * 3 + 2, "dl": 32 + 16 * 4 + 2,
+          "sl": 32 + 16 + 2}
+    wr = {"no": 64 + 24 + 10 * (64 + 80 + 16), "pay": 16 + 48 + 64, "os": 0, "dl": 24 + 8 + 8 + 32, "sl": 0}
     share = {"no": no, "pay": pay, "os": os_, "dl": dl, "sl": sl}
-    return (sum(ex[k] * share[k] for k in ex) / 100.0, sum(cw[k] * share[k] for k in cw) / 100.0)
+    return (sum(ex[k] * share[k] for k in ex) / 100.0,
+            sum((ck[k] + commit_rate * wr[k]) * share[k] for k in ck) / 100.0)
 
 
 if __name__ == "__main__":

@@ -367,7 +367,7 @@ typedef struct {
     uint32_t blocks_per_sm;   /* cap on resident blocks per SM, 0 = occupancy   */
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
     uint32_t filter;          /* 1 = read the slot before its atomicMin         */
-    uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any)    */
+    uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any; TPC-C: header ops) */
 } ltpg_launch;
 int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
 int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);

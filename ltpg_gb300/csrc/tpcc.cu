@@ -591,6 +591,7 @@ struct TpccTunedArgs {
     DevStats *st;
     DevCtl *ctl;
     uint32_t filter;
+    uint32_t dedupe;  // one registration per distinct slot of a warp (header ops)
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64t(const unsigned long long *p) {
@@ -705,7 +706,7 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT
             const uint64_t s1 = it.head ? a.db.base[it.op.table] + it.op.row : a.db.base[LTPG_T_STOCK] + srow;
             const bool w1 = it.head ? (it.op.flags & OPF_REG_W) != 0u : true;
             const bool f1 = filt && (it.head ? it.op.table == LTPG_T_CUSTOMER : true);
-            tuned_register(a, it.valid, s1, w1, mine, true, f1);
+            tuned_register(a, it.valid, s1, w1, mine, a.dedupe != 0u, f1);
             // second registration: a line's ORDER-LINE insert, or the read half
             // of a header op that reads and writes its row (Delivery)
             const bool rw = it.head && (it.op.flags & OPF_REG_R) && (it.op.flags & OPF_REG_W);
@@ -890,6 +891,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.st = s.stats;
     a.ctl = c->ctl;
     a.filter = c->launch_c.filter;
+    a.dedupe = c->launch_c.dedupe;
     const size_t smem = a.db.W <= HOT_SMEM_MAX_W ? 11u * a.db.W * sizeof(long long) : 0u;
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
     if (e != cudaSuccess) return e;

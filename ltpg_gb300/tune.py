@@ -57,8 +57,8 @@ def candidates(workload, staging=False):
         grid = itertools.product([1, 2, 4], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
         return [dict(block_threads=256, ops_per_thread=o, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w)
                 for o, b, f, d, w in grid]
-    return [dict(block_threads=256, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=1, stage_ways=4)
-            for b, f in itertools.product([0, 2, 4, 6], [0, 1])]
+    return [dict(block_threads=256, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4)
+            for b, f, d in itertools.product([0, 2, 4, 6], [0, 1], [0, 1])]
 
 
 def _time_batches(eng, slots, reps, mode, torch):

@@ -84,3 +84,20 @@ def test_mix_known_answers(eng, mode):
         o = oracle.TpccOracle(2, 1)
         _same(eng, o, batch(rows, list(lines)), 0, mode)
         _tables(eng, o)
+
+
+@pytest.mark.parametrize("filt,dedupe,bps", [(0, 0, 0), (1, 0, 2), (0, 1, 6), (1, 1, 0)])
+def test_launch_shapes_do_not_change_outcomes(eng, filt, dedupe, bps):
+    """Every TPC-C launch shape the autotuner can pick (slot filter, warp
+    dedupe of header registrations, blocks per SM) gives the oracle's outcome."""
+    W = 3
+    eng.load_tpcc(37, W)
+    o = oracle.TpccOracle(37, W)
+    g = TpccGenerator(37, W, 30000, **MIX)
+    try:
+        eng.set_launch("tpcc", filter=filt, dedupe=dedupe, blocks_per_sm=bps)
+        for i, mode in enumerate(["fused", "persistent", "graph"]):
+            _same(eng, o, g.next(), i % 2, mode)
+        _tables(eng, o)
+    finally:
+        eng.set_launch("tpcc", filter=0, dedupe=1, blocks_per_sm=0)
