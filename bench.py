@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=32)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-device-gen", action="store_true", help="skip the device-generator section")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="the engine's default launch shape, no autotuning (profiling runs)")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
     ap.add_argument("--serve-seconds", type=float, default=0.25)
     ap.add_argument("--no-reference-gpu", action="store_true",
@@ -291,7 +293,9 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
         for i, b in enumerate(batches):
             eng.upload(i, b)
         for mode in ["plain", args.mode]:
-            if mode != "plain":
+            if mode != "plain" and args.no_tune:
+                res["launch"] = dict(eng.get_launch("ycsb"), source="default")
+            elif mode != "plain":
                 from ltpg_gb300 import tune
                 wkey = f"{args.workload}|theta={theta}"
                 cfg, how = tune.apply_cached_or_tune(eng, "ycsb", wkey, list(range(min(8, n_slots))),
@@ -373,7 +377,9 @@ def tpcc_bench(args, w, dist, want_extras=True):
         for i, b in enumerate(batches):
             eng.upload(i, b)
         for mode in ["plain", args.mode]:
-            if mode != "plain":
+            if mode != "plain" and args.no_tune:
+                res["launch"] = dict(eng.get_launch("tpcc"), source="default")
+            elif mode != "plain":
                 from ltpg_gb300 import tune
                 cfg, how = tune.apply_cached_or_tune(eng, "tpcc", args.workload, list(range(min(4, n_slots))),
                                                      lambda: eng.load_tpcc(SEED, w["warehouses"]))

@@ -100,4 +100,4 @@ def test_launch_shapes_do_not_change_outcomes(eng, filt, dedupe, bps):
             _same(eng, o, g.next(), i % 2, mode)
         _tables(eng, o)
     finally:
-        eng.set_launch("tpcc", filter=0, dedupe=1, blocks_per_sm=0)
+        eng.set_launch("tpcc", filter=0, dedupe=0, blocks_per_sm=0)
