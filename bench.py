@@ -250,6 +250,21 @@ def timed(eng, torch, n_slots, steps, mode, start, dist):
     return ev0.elapsed_time(ev1) / 1e3, c1 - c0, l1 - l0, nxt
 
 
+def modes_run(eng, torch, n_slots, steps, reload):
+    """The same resident batches through each execution mode of the tuned
+    path: fused (two kernels per batch), graph (one CUDA graph over the
+    slots), persistent (one cooperative kernel per batch, grid barrier between
+    the phases).  Committed txn/s and ms per batch."""
+    out = {}
+    for m in ["fused", "graph", "persistent"]:
+        reload()
+        eng.sync()
+        nxt = run_steps(eng, n_slots, 4, m)
+        secs, commits, launches, _ = timed(eng, torch, n_slots, steps, m, nxt, None)
+        out[m] = {"value": commits / secs, "ms_per_batch": secs * 1e3 / steps, "launches_per_batch": launches / steps}
+    return out
+
+
 def e2e_run(eng, pinned, mode, steps, n_slots, n_txn, dist, depth=3):
     """End to end through the pipelined host-buffer calls (ltpg_submit_*_host /
     ltpg_host_wait): every step copies its pinned host batch to the device,
@@ -313,6 +328,9 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                 kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
                 eng.set_profiling(False)
             res[mode] = dict(secs=secs, commits=commits, launches=launches, clocks=clk.summary(), kt=kt)
+        if want_extras:
+            res["modes"] = modes_run(eng, torch, n_slots, min(args.steps, 64),
+                                     lambda: eng.load_ycsb(SEED, w["n_records"]))
         # access-pattern ceilings of this GPU (the practical rooflines of the kernels' parts)
         if want_extras:
             res["ceilings"] = {
@@ -396,6 +414,9 @@ def tpcc_bench(args, w, dist, want_extras=True):
                 kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
                 eng.set_profiling(False)
             res[mode] = dict(secs=secs, commits=commits, launches=launches, clocks=clk.summary(), kt=kt)
+        if want_extras:
+            res["modes"] = modes_run(eng, torch, n_slots, min(args.steps, 64),
+                                     lambda: eng.load_tpcc(SEED, w["warehouses"]))
         ref = {}
         for mode in ["plain", args.mode]:
             eng.load_tpcc(SEED, w["warehouses"])
@@ -636,6 +657,8 @@ def main():
         "launch": launch,
         "clocks": tuned["clocks"],
     }
+    if res.get("modes"):
+        line["modes"] = res["modes"]
     if not args.no_cpu_baseline:
         if w["kind"] == "ycsb":
             v, s, c = cpu_baseline_ycsb(w, batches, args.cpu_batches)

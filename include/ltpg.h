@@ -361,8 +361,8 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
 /* ---- tuning ----------------------------------------------------------------
  * Launch shape of the tuned kernels of one workload; the autotuner writes it.
  * None of these settings can change a commit decision or the table image.
- * Defaults: 256 threads, 1 op per thread, occupancy, 4 ways, filter 1;
- * dedupe 1 for YCSB, 0 for TPC-C. */
+ * Defaults: 256 threads, 1 op per thread, occupancy, 4 ways, filter 1,
+ * dedupe 0. */
 typedef struct {
     uint32_t block_threads;   /* threads per block, multiple of 32, <= 512      */
     uint32_t ops_per_thread;  /* YCSB op words per thread: 1, 2, 4 or 8         */

@@ -153,9 +153,6 @@ int ltpg_create(const ltpg_config *cfg, ltpg_ctx **out) {
     }
     c->stream = c->own_stream;
     c->slots.resize(cfg->n_slots);
-    // TPC-C header registrations rarely repeat within a warp (NURand over
-    // 30,000 customers per warehouse): the warp dedupe costs more than it saves
-    c->launch_c.dedupe = 0;
     *out = c;
     return LTPG_OK;
 }
