@@ -40,10 +40,10 @@ void zipf_init(Zipf &z, uint64_t n, double theta) {
 
 }  // namespace
 
-const PowTables &host_pow_tables() {
-    static const PowTables t = [] {
-        PowTables x;
-        pow_tables_fill(x);
+const FixTables &host_fix_tables() {
+    static const FixTables t = [] {
+        FixTables x;
+        fix_tables_fill(x);
         return x;
     }();
     return t;
@@ -142,7 +142,7 @@ int ltpg_gen_ycsb_batch(ltpg_gen *g, uint64_t batch_id, uint32_t *ops, uint32_t 
 
     // Pass 1: op words and per-transaction update counts, in parallel over
     // transactions (each has its own stream, so the split does not matter).
-    const PowTables &tab = host_pow_tables();
+    const FixTables &tab = host_fix_tables();
     auto fill = [&](uint32_t t0, uint32_t t1) {
         for (uint32_t t = t0; t < t1; ++t)
             val_off[t + 1] = ycsb_txn(p, g->zipf, tab, rotate ? &perm : nullptr, batch_id, t, ops + (uint64_t)t * stride);

@@ -7,7 +7,8 @@
 // into fused multiply-adds (host: -ffp-contract=off; device: -fmad=false):
 // those round the same on x86-64, aarch64 and the GPU.  Library pow / exp / log
 // are not correctly rounded and differ between glibc and CUDA in the last ulp,
-// so the sampler's power is computed below from series and tables of our own.
+// so the sampler's power is computed below in fixed point, from tables filled
+// by series of our own.
 #pragma once
 #include <string.h>
 
@@ -176,75 +177,90 @@ LTPG_HDI double det_pow(double x, double a) {
     return det_exp(a * det_log(x));
 }
 
-// ---- table-driven power (the sampler's) ---------------------------------
-// Tang's table-driven methods (P. T. P. Tang, "Table-driven implementation of
-// the exponential function in IEEE floating-point arithmetic", ACM TOMS 15,
-// 1989; "... of the logarithm function", ACM TOMS 16, 1990): a table entry
-// takes the argument to within 2^-8 (log) or ln 2 / 128 (exp) of an anchor,
-// where a degree-7 / degree-6 polynomial suffices — about half the
-// operations of the series above and no division.  The tables are filled
-// once on the host by the series functions and copied to the device as they
-// are, so both sides hold the same bits.
-struct PowTables {
-    double log_r[97];  // r_j = 1 / (3/4 + j / 128), rounded
-    double log_c[97];  // -ln r_j
-    double exp_t[64];  // 2^(j / 64)
+// ---- fixed-point power (the sampler's) -----------------------------------
+// The sampler needs v = floor(n b^a) for b in (0, 1], a = 1 / (1 - theta) >= 1.
+// It is computed in 64-bit fixed point (Q63: 1.0 = 2^63) by table-driven
+// log2 and exp2 in the manner of Tang (ACM TOMS 1989/1990): b = m 2^-K,
+// m = (1 + j/128)(1 + r), |r| < 2^-7, log2(1 + r) by the atanh-free series
+// ln(1 + r) = r - r^2/2 + ... (nine terms); a log2(1/b) = I + k/64 + g,
+// 2^-(k/64) from a table and 2^-g = e^(-g ln 2) by its Taylor series (eight
+// terms).  Integer arithmetic only, so host and GPU give the same v by
+// construction, and GB300's integer pipes run it about ten times faster than
+// the double-precision evaluation (whose FP64 rate is low on this part).  The
+// tables are filled once on the host from the series functions above.
+struct FixTables {
+    uint64_t log2c[128];  // log2(1 + j/128), Q63
+    uint64_t rcp[128];    // floor((2^64 - 1) / (128 + j))
+    uint64_t exp2n[64];   // 2^(-k/64), Q63
 };
-inline void pow_tables_fill(PowTables &t) {
-    for (int j = 0; j <= 96; ++j) {
-        t.log_r[j] = 1.0 / (0.75 + j / 128.0);
-        t.log_c[j] = -det_log(t.log_r[j]);
+constexpr uint64_t Q63_ONE = 1ull << 63;
+inline void fix_tables_fill(FixTables &t) {
+    for (int j = 0; j < 128; ++j) {
+        t.log2c[j] = (uint64_t)(det_log(1.0 + j / 128.0) / LN2 * 0x1p63);
+        t.rcp[j] = ~0ull / (uint64_t)(128 + j);
     }
-    for (int j = 0; j < 64; ++j) t.exp_t[j] = det_exp(j * (LN2 / 64.0));
+    for (int k = 0; k < 64; ++k) t.exp2n[k] = k == 0 ? Q63_ONE : (uint64_t)(det_exp(-k * (LN2 / 64.0)) * 0x1p63);
 }
-// ln x for normal x > 0: x = m 2^e with m in [3/4, 3/2) (so that x near 1
-// has e = 0 and nothing cancels), j = m's nearest 1/128 step from 3/4;
-// ln m = -ln r_j + ln(m r_j), m r_j - 1 exact (Sterbenz), |z| < 2^-7.
-LTPG_HDI double tab_log(const PowTables &t, double x) {
-    const uint64_t b = dbits(x);
-    int e = (int)((b >> 52) & 0x7FF) - 1023;
-    const uint64_t mant = b & 0x000FFFFFFFFFFFFFull;
-    double m = dfrom(mant | 0x3FF0000000000000ull);  // [1, 2)
-    if (mant >= (1ull << 51)) {                        // m >= 3/2
-        m = m * 0.5;
-        e += 1;
-    }
-    const int j = (int)dfloor((m - 0.75) * 128.0 + 0.5);  // 0 .. 96; m - 3/4 exact
-    const double z = m * t.log_r[j] - 1.0;
-    double p = 1.0 / 7.0;
-    p = p * z - 1.0 / 6.0;
-    p = p * z + 1.0 / 5.0;
-    p = p * z - 1.0 / 4.0;
-    p = p * z + 1.0 / 3.0;
-    p = p * z - 0.5;
-    p = p * z + 1.0;
-    return ((double)e * LN2 + t.log_c[j]) + p * z;
+// (a b) >> 63 for Q63 operands whose product is below 2, the low bit dropped.
+LTPG_HDI uint64_t q63mul(uint64_t a, uint64_t b) { return mulhi64(a, b) << 1; }
+struct U128 {
+    uint64_t hi, lo;
+};
+LTPG_HDI U128 mul64(uint64_t a, uint64_t b) { return U128{mulhi64(a, b), a * b}; }
+LTPG_HDI uint64_t shr128(U128 x, uint32_t s) {  // (x >> s) mod 2^64, s < 128
+    if (s == 0) return x.lo;
+    if (s < 64) return (x.hi << (64 - s)) | (x.lo >> s);
+    return x.hi >> (s - 64);
 }
-// e^y for y <= 0: y = (64 k + j) ln 2 / 64 + r (Cody-Waite, |r| <= ln 2 / 128),
-// e^y = 2^k 2^(j/64) e^r.
-LTPG_HDI double tab_exp(const PowTables &t, double y) {
-    if (y < -745.0) return 0.0;
-    const double kd = dfloor(y * (64.0 / LN2) + 0.5);
-    const double r = (y - kd * (LN2_HI / 64.0)) - kd * (LN2_LO / 64.0);
-    double p = 1.0 / 720.0;
-    p = p * r + 1.0 / 120.0;
-    p = p * r + 1.0 / 24.0;
-    p = p * r + 1.0 / 6.0;
-    p = p * r + 0.5;
-    p = p * r + 1.0;
-    p = p * r + 1.0;
-    const int ki = (int)kd;
-    int k = ki >> 6;  // floor division (arithmetic shift)
-    double v = t.exp_t[ki & 63] * p;
-    if (k < -1022) {  // subnormal result: two exact-exponent steps
-        v = v * dfrom((uint64_t)(1023 - 600) << 52);
-        k += 600;
-    }
-    return v * dfrom((uint64_t)(k + 1023) << 52);
-}
-LTPG_HDI double tab_pow(const PowTables &t, double x, double a) {
-    if (!(x >= 2.2250738585072014e-308)) return 0.0;
-    return tab_exp(t, a * tab_log(t, x));
+// floor(n b^a) for b in (0, 1] (normal), 1 <= a < 2^20, n < 2^40.
+LTPG_HDI uint64_t fix_pow_floor(const FixTables &t, double b, double a, uint64_t n) {
+    const uint64_t bb = dbits(b), ab = dbits(a);
+    const uint32_t eb = (uint32_t)((bb >> 52) & 0x7FF), ea = (uint32_t)((ab >> 52) & 0x7FF);
+    if (eb == 0 || eb > 1023) return eb > 1023 ? n : 0;  // b > 1 cannot occur; b subnormal -> 0
+    const uint64_t M = (bb & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+    const uint32_t j = (uint32_t)(M >> 45) - 128u;       // 0 .. 127
+    const uint64_t D = M & ((1ull << 45) - 1);
+    const uint64_t r = shr128(mul64(D, t.rcp[j]), 46);   // Q63, < 2^-7
+    // ln(1 + r) = r (1 - r (1/2 - r (1/3 - ... - r/9))), every bracket positive
+    uint64_t p = Q63_ONE / 9;
+    p = Q63_ONE / 8 - q63mul(r, p);
+    p = Q63_ONE / 7 - q63mul(r, p);
+    p = Q63_ONE / 6 - q63mul(r, p);
+    p = Q63_ONE / 5 - q63mul(r, p);
+    p = Q63_ONE / 4 - q63mul(r, p);
+    p = Q63_ONE / 3 - q63mul(r, p);
+    p = Q63_ONE / 2 - q63mul(r, p);
+    p = Q63_ONE - q63mul(r, p);
+    const uint64_t inv_ln2 = (uint64_t)((1.0 / LN2) * 0x1p63);
+    const uint64_t lm = t.log2c[j] + q63mul(q63mul(r, p), inv_ln2);  // log2 m, Q63, < 1
+    // L = log2(1/b) = K - log2 m, K = 1023 - eb; as 128 bits in Q63
+    const uint64_t K = 1023u - eb;
+    const uint64_t lo0 = (K & 1u) << 63;
+    U128 L{(K >> 1) - (lo0 < lm ? 1u : 0u), lo0 - lm};
+    if (K == 0) L = U128{0, 0};  // b = 1 (then lm = 0)
+    // Y = a L in Q63: a = Ma 2^(ea - 1075), Ma < 2^53
+    const uint64_t Ma = (ab & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+    const U128 pl = mul64(L.lo, Ma);
+    const U128 prod{pl.hi + L.hi * Ma, pl.lo};
+    const uint32_t s = 1075u - ea;  // 32 < s <= 52 for 1 <= a < 2^20
+    const U128 Y{prod.hi >> s, (prod.hi << (64 - s)) | (prod.lo >> s)};
+    if (Y.hi >= 64u) return 0;  // 2^-I with I >= 128
+    const uint32_t I = (uint32_t)((Y.hi << 1) | (Y.lo >> 63));
+    const uint64_t F = Y.lo & (Q63_ONE - 1);
+    const uint32_t k = (uint32_t)(F >> 57);
+    const uint64_t x = q63mul(F & ((1ull << 57) - 1), (uint64_t)(LN2 * 0x1p63));  // g ln 2 < 0.011
+    // e^-x = 1 - x (1 - x (1/2 - x (1/6 - x (1/24 - x (1/120 - x (1/720 - x/5040))))))
+    uint64_t e = Q63_ONE / 5040;
+    e = Q63_ONE / 720 - q63mul(x, e);
+    e = Q63_ONE / 120 - q63mul(x, e);
+    e = Q63_ONE / 24 - q63mul(x, e);
+    e = Q63_ONE / 6 - q63mul(x, e);
+    e = Q63_ONE / 2 - q63mul(x, e);
+    e = Q63_ONE - q63mul(x, e);
+    e = Q63_ONE - q63mul(x, e);
+    const uint64_t P = q63mul(t.exp2n[k], e);  // b^a 2^I, Q63, in (1/2, 1]
+    const uint32_t sh = 63u + I;
+    return sh >= 128u ? 0 : shr128(mul64(n, P), sh);
 }
 
 // Zipfian ranks by the method of Gray, Sundaresan, Englert, Baclawski and
@@ -254,13 +270,13 @@ LTPG_HDI double tab_pow(const PowTables &t, double x, double a) {
 struct Zipf {
     uint64_t n = 0;
     double theta = 0, zetan = 0, alpha = 0, eta = 0, half_pow = 0;
-    LTPG_HDI uint64_t sample(Rng &r, const PowTables &tab) const {
+    LTPG_HDI uint64_t sample(Rng &r, const FixTables &tab) const {
         if (theta == 0.0) return r.below(n);
         const double u = r.unit();
         const double uz = u * zetan;
         if (uz < 1.0) return 0;
         if (uz < 1.0 + half_pow) return n > 1 ? 1 : 0;
-        const uint64_t v = (uint64_t)((double)n * tab_pow(tab, eta * u - eta + 1.0, alpha));
+        const uint64_t v = fix_pow_floor(tab, eta * u - eta + 1.0, alpha, n);
         return v < n ? v : n - 1;
     }
 };
@@ -268,7 +284,7 @@ struct Zipf {
 // Op words of YCSB transaction t of batch batch_id (distinct keys; a read
 // scans scan_len keys when scan_len >= 2, its span in the field bits); pads to
 // the op stride.  Returns the number of updates.
-LTPG_HDI uint32_t ycsb_txn(const ltpg_ycsb_params &p, const Zipf &zipf, const PowTables &tab, const Perm *perm,
+LTPG_HDI uint32_t ycsb_txn(const ltpg_ycsb_params &p, const Zipf &zipf, const FixTables &tab, const Perm *perm,
                            uint64_t batch_id, uint32_t t, uint32_t *w) {
     Rng r(hash3(p.seed ^ DOM_YCSB_OPS, batch_id, t));
     const uint32_t k = p.ops_per_txn, stride = ycsb_stride(k);

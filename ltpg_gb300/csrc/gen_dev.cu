@@ -140,7 +140,7 @@ uint32_t scan_scratch(uint32_t n) { return (n + SCAN_BLOCK - 1) / SCAN_BLOCK + 1
 struct YcsbGenArgs {
     ltpg_ycsb_params p;
     Zipf zipf;
-    const PowTables *tab;
+    const FixTables *tab;
     Perm perm;
     bool rotate;
     uint64_t batch_id;
@@ -465,7 +465,7 @@ uint32_t blocks(uint64_t n, uint32_t per) { return (uint32_t)((n + per - 1) / pe
 // generator's state and the scratch of one batch.
 struct ltpg_gen_dev {
     int device = -1;
-    PowTables *tab = nullptr;
+    FixTables *tab = nullptr;
     uint32_t G = 0, C = 0;
     uint32_t *o_id = nullptr, *no_id = nullptr, *ol_id = nullptr, *h_id = nullptr;
     uint64_t *made = nullptr, *delivered = nullptr;
@@ -564,7 +564,7 @@ cudaError_t bind_ycsb(ltpg_gen *g, int device) {
     if (!d) return cudaErrorMemoryAllocation;
     d->device = device;
     cudaError_t e = dalloc(d, &d->tab, 1);
-    if (e == cudaSuccess) e = cudaMemcpy(d->tab, &host_pow_tables(), sizeof(PowTables), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d->tab, &host_fix_tables(), sizeof(FixTables), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         free_dev(d);
         return e;

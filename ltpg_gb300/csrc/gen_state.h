@@ -35,4 +35,4 @@ struct ltpg_gen {
 // Frees the device state of g (gen_dev.cu).
 void gen_dev_free(ltpg_gen *g);
 // The sampler's power tables, filled once (gen.cpp).
-const ltpg::gen::PowTables &host_pow_tables();
+const ltpg::gen::FixTables &host_fix_tables();
