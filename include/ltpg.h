@@ -346,6 +346,12 @@ int ltpg_submit_ycsb_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b
 int ltpg_submit_tpcc_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, int mode,
                           uint32_t *host_bitmap);
 int ltpg_host_wait(ltpg_ctx *ctx, uint32_t slot);
+/* The same pipeline with the batch made on the GPU: generator g's batch
+ * batch_id (in order for TPC-C) is generated into `slot` on the copy stream,
+ * so it overlaps the kernels of the batches before it, then run and its
+ * bitmap queued for download; ltpg_host_wait(slot) as above. */
+int ltpg_submit_generated(ltpg_ctx *ctx, ltpg_gen *g, uint64_t batch_id, uint32_t slot, int mode,
+                          uint32_t *host_bitmap);
 
 /* ---- results (statistic_query / copy_to_host surface) ------------------- */
 /* Replaces: Query::copy_to_host (TF/Query.h:606-631), which reads back only

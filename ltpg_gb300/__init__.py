@@ -304,6 +304,23 @@ class Engine:
             self._ck(lib().ltpg_gen_tpcc_batch_device(self._h, gen._h, gen.next_id, slot))
             gen.next_id += 1
 
+    def submit_generated(self, slot, gen, mode, bitmap, batch_id=None):
+        """Pipelined device generation: gen's batch is made on the GPU in `slot`
+        on the copy stream (overlapping earlier batches' kernels), run in `mode`,
+        and its commit bitmap copied to `bitmap` (pinned, from pinned_empty);
+        host_wait(slot) returns when it is there.  TPC-C: the next batch in
+        order (batch_id ignored)."""
+        m = MODES[mode] if isinstance(mode, str) else mode
+        if isinstance(gen, YcsbGenerator):
+            if batch_id is None:
+                raise ValueError("a YCSB batch needs its batch_id")
+            bid = batch_id
+        else:
+            bid = gen.next_id
+        self._ck(lib().ltpg_submit_generated(self._h, gen._h, bid, slot, m, _p(bitmap) if bitmap is not None else None))
+        if not isinstance(gen, YcsbGenerator):
+            gen.next_id += 1
+
     def download_batch(self, slot):
         """The batch held by `slot` (uploaded or generated on the GPU)."""
         bi = abi.BatchInfoC()

@@ -115,6 +115,7 @@ SIGNATURES = {
     "ltpg_gen_ycsb_batch": (C.c_int, [P, U64, P, P, P, C.POINTER(YcsbBatchC)]),
     "ltpg_gen_tpcc_batch": (C.c_int, [P, U64, P, P, C.POINTER(TpccBatchC)]),
     "ltpg_gen_ycsb_batch_device": (C.c_int, [P, P, U64, U32]),
+    "ltpg_submit_generated": (C.c_int, [P, P, U64, U32, C.c_int, P]),
     "ltpg_batch_info_get": (C.c_int, [P, U32, C.POINTER(BatchInfoC)]),
     "ltpg_batch_download": (C.c_int, [P, U32, U32, P, C.c_size_t]),
     "ltpg_gen_tpcc_batch_device": (C.c_int, [P, P, U64, U32]),

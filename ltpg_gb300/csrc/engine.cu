@@ -591,6 +591,13 @@ int ltpg_submit_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, 
     return submit_host(c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_tpcc(c, slot, b, st); });
 }
 
+int ltpg_submit_generated(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, int mode,
+                          uint32_t *host_bitmap) {
+    if (!c || !g) return c ? fail(c, LTPG_ERR_INVALID, "null generator") : LTPG_ERR_INVALID;
+    return submit_host(c, slot, mode, host_bitmap,
+                       [&](cudaStream_t st) { return gen_device_batch(c, g, batch_id, slot, st); });
+}
+
 int ltpg_host_wait(ltpg_ctx *c, uint32_t slot) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;

@@ -155,6 +155,8 @@ void drop_graphs_ctx(ltpg_ctx *c);
 // invalidation) and records the shape; the caller fills the batch buffers.
 int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, uint32_t n_updates, Slot **out);
 int slot_prepare_tpcc(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint64_t n_lines, uint64_t txn_base, Slot **out);
+// Makes generator g's batch batch_id in slot `slot` on stream st (gen_dev.cu).
+int gen_device_batch(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, cudaStream_t st);
 // Record an error message on the context and return its code.
 int ctx_fail(ltpg_ctx *c, int code, const char *msg);
 int ctx_cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what);

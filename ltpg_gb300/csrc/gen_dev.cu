@@ -582,9 +582,11 @@ void gen_dev_free(ltpg_gen *g) {
 
 extern "C" {
 
-int ltpg_gen_ycsb_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot) {
-    if (!c || !g || g->kind != LTPG_WORKLOAD_YCSB) return c ? ctx_fail(c, LTPG_ERR_INVALID, "not a YCSB generator")
-                                                           : LTPG_ERR_INVALID;
+}  // extern "C"
+
+namespace {
+
+int gen_ycsb(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, cudaStream_t st) {
     const ltpg_ycsb_params &p = g->y;
     if (cudaSetDevice(c->device) != cudaSuccess) return ctx_fail(c, LTPG_ERR_CUDA, "set device");
     if (p.n_records > c->ycsb.n) return ctx_fail(c, LTPG_ERR_INVALID, "generator keys exceed the loaded table");
@@ -606,27 +608,25 @@ int ltpg_gen_ycsb_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint
     a.val_off = s->val_off;
     a.vals = s->vals;
     const uint32_t nb = blocks(p.n_txn, TB);
-    ycsb_gen_ops<<<nb, TB, 0, c->stream>>>(a);
+    ycsb_gen_ops<<<nb, TB, 0, st>>>(a);
     count_launch(c);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) {
         // the scan's block totals borrow the slot's vals buffer, whose values
         // are written after the scan
         uint64_t launches = 0;
-        e = inclusive_scan(s->val_off + 1, p.n_txn, reinterpret_cast<uint32_t *>(s->vals), c->stream, launches);
+        e = inclusive_scan(s->val_off + 1, p.n_txn, reinterpret_cast<uint32_t *>(s->vals), st, launches);
         count_launch(c, launches);
     }
     if (e == cudaSuccess) {
-        ycsb_gen_vals<<<nb, TB, 0, c->stream>>>(a);
+        ycsb_gen_vals<<<nb, TB, 0, st>>>(a);
         count_launch(c);
         e = cudaGetLastError();
     }
     return e == cudaSuccess ? LTPG_OK : ctx_cuda_fail(c, e, "device YCSB generation");
 }
 
-int ltpg_gen_tpcc_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot) {
-    if (!c || !g || g->kind != LTPG_WORKLOAD_TPCC) return c ? ctx_fail(c, LTPG_ERR_INVALID, "not a TPC-C generator")
-                                                           : LTPG_ERR_INVALID;
+int gen_tpcc(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, cudaStream_t st) {
     if (batch_id != g->next_batch) return ctx_fail(c, LTPG_ERR_STATE, "TPC-C batches are drawn in order");
     const ltpg_tpcc_params &p = g->c;
     if (cudaSetDevice(c->device) != cudaSuccess) return ctx_fail(c, LTPG_ERR_CUDA, "set device");
@@ -675,7 +675,6 @@ int ltpg_gen_tpcc_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint
     a.txns = s->txns;
     a.lines = s->lines;
     a.hdr = s->dev_hdr;
-    cudaStream_t st = c->stream;
     const uint32_t nb = blocks(a.B, TB);
     uint64_t launches = 0;
     e = cudaMemsetAsync(a.cc, 0, 4ull * a.W * a.G * sizeof(uint32_t), st);
@@ -705,6 +704,31 @@ int ltpg_gen_tpcc_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint
     g->txn_base += p.n_txn;
     g->next_batch++;
     return LTPG_OK;
+}
+
+}  // namespace
+
+namespace ltpg {
+int gen_device_batch(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, cudaStream_t st) {
+    if (!c || !g) return c ? ctx_fail(c, LTPG_ERR_INVALID, "null generator") : LTPG_ERR_INVALID;
+    if (g->kind == LTPG_WORKLOAD_YCSB) return gen_ycsb(c, g, batch_id, slot, st);
+    if (g->kind == LTPG_WORKLOAD_TPCC) return gen_tpcc(c, g, batch_id, slot, st);
+    return ctx_fail(c, LTPG_ERR_INVALID, "unknown generator");
+}
+}  // namespace ltpg
+
+extern "C" {
+
+int ltpg_gen_ycsb_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot) {
+    if (!c || !g || g->kind != LTPG_WORKLOAD_YCSB)
+        return c ? ctx_fail(c, LTPG_ERR_INVALID, "not a YCSB generator") : LTPG_ERR_INVALID;
+    return gen_ycsb(c, g, batch_id, slot, c->stream);
+}
+
+int ltpg_gen_tpcc_batch_device(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot) {
+    if (!c || !g || g->kind != LTPG_WORKLOAD_TPCC)
+        return c ? ctx_fail(c, LTPG_ERR_INVALID, "not a TPC-C generator") : LTPG_ERR_INVALID;
+    return gen_tpcc(c, g, batch_id, slot, c->stream);
 }
 
 }  // extern "C"

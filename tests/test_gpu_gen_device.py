@@ -112,3 +112,43 @@ def test_device_generation_checks(eng):
         assert ei.value.code == abi.ERR_INVALID
     finally:
         small.close()
+
+
+def test_pipelined_device_generation(eng):
+    """ltpg_submit_generated: each batch generated on the copy stream while the
+    one before it runs, two slots in flight; bitmaps, flags and the final image
+    equal the oracle's run of the host generator's batches."""
+    from ltpg_gb300 import pinned_empty
+    depth = 2
+    n, B = 200_000, 20000
+    eng.load_ycsb(17, n)
+    yo = oracle.YcsbOracle(17, n)
+    g = YcsbGenerator(17, n, B, 16, 5, 0.99, 4)
+    want = [yo.run(g.batch(i))[1] for i in range(6)]
+    bits = [pinned_empty((B + 31) // 32) for _ in range(depth)]
+    for i in range(6):
+        if i >= depth:
+            eng.host_wait(i % depth)
+            assert np.array_equal(bits[i % depth], want[i - depth]), i - depth
+        eng.submit_generated(i % depth, g, "graph", bits[i % depth], batch_id=i)
+    for i in range(6 - depth, 6):
+        eng.host_wait(i % depth)
+        assert np.array_equal(bits[i % depth], want[i]), i
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), yo.rows)
+
+    W = 2
+    eng.load_tpcc(19, W)
+    to = oracle.TpccOracle(19, W)
+    gd, gh = TpccGenerator(19, W, B, by_name_pct=60, **MIX), TpccGenerator(19, W, B, by_name_pct=60, **MIX)
+    want = [to.run(gh.next()) for _ in range(6)]
+    for i in range(6):
+        if i >= depth:
+            eng.host_wait(i % depth)
+            assert np.array_equal(bits[i % depth], want[i - depth][1]), i - depth
+        eng.submit_generated(i % depth, gd, "fused", bits[i % depth])
+    for i in range(6 - depth, 6):
+        eng.host_wait(i % depth)
+        assert np.array_equal(bits[i % depth], want[i][1]), i
+        assert np.array_equal(eng.txn_flags(i % depth, B), want[i][0])
+    for t in range(abi.TPCC_TABLES):
+        assert np.array_equal(eng.download_table(t), to.tables[t]), t
