@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--mode", default="graph", choices=["fused", "graph", "persistent"])
     ap.add_argument("--sweep", action="store_true", help="also time theta 0/0.6/0.8/0.99 (YCSB)")
-    ap.add_argument("--cpu-batches", type=int, default=2, help="batches in the CPU-baseline sample")
+    ap.add_argument("--cpu-batches", type=int, default=12,
+                    help="batches in the CPU-baseline sample (about 10 s of oracle replay at the default sizes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=32)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
@@ -663,9 +664,9 @@ def main():
         if w["kind"] == "ycsb":
             v, s, c = cpu_baseline_ycsb(w, batches, args.cpu_batches)
         else:
-            v, s, c = cpu_baseline_tpcc(w, batches, min(args.cpu_batches, 2))
+            v, s, c = cpu_baseline_tpcc(w, batches, args.cpu_batches)
         line["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
-                                "sample": f"{min(args.cpu_batches, len(batches))} whole batches of {B} txn, "
+                                "sample": f"{min(args.cpu_batches, len(batches))} whole batches of {B} txn in order, "
                                           f"single-threaded oracle replay, {s:.1f} s"}
     if not args.no_predictor and w["kind"] == "ycsb" and w["n_txn"] >= (1 << 18):
         line["predictor"] = predictor_section(w, batches)
