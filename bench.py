@@ -89,8 +89,13 @@ def dist_setup():
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        # one process per GPU over NCCL; gloo where there is no GPU (the
+        # reference arm's CPU replay, and the multi-rank tests)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
         return ws, rank, local, dist
     return 1, 0, 0, None
 
@@ -100,11 +105,15 @@ def barrier(dist):
         dist.barrier()
 
 
+def _reduce_device(dist):
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def reduce_max(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -113,7 +122,7 @@ def reduce_sum(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
@@ -557,18 +566,18 @@ def reference_arm(args, w, rank):
         import oracle
         from ltpg_gb300 import TpccGenerator
         g = TpccGenerator(SEED, w["warehouses"], w["n_txn"], **w.get("mix", {}))
-        nb = 2
+        nb = 4
         batches = [g.next() for _ in range(nb)]
         o = oracle.TpccOracle(SEED, w["warehouses"])
-        threads = 1
-        for i in range(min(args.warmup, 1)):
-            o.run(batches[i % nb])
+        # each step: one whole batch replayed with all host threads, the
+        # generator's batches in a cycle over the advancing image
+        for i in range(args.warmup):
+            o.run(batches[i % nb], threads=threads)
         commits, t0 = 0, time.perf_counter()
-        steps = min(args.steps, 4)
-        for i in range(steps):
-            commits += o.run(batches[i % nb])[3]
+        for i in range(args.steps):
+            commits += o.run(batches[(args.warmup + i) % nb], threads=threads)[3]
         secs = time.perf_counter() - t0
-        sample = f"{steps} whole batches of {w['n_txn']} txn, single-threaded replay"
+        sample = f"{args.steps} whole batches of {w['n_txn']} txn, {nb} distinct, multi-threaded replay"
         kind = "port"
     v = commits / secs
     line = {"impl": "reference", "metric": "committed txns/s", "value": v, "unit": "txn/s",

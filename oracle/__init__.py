@@ -56,6 +56,9 @@ def lib():
         _lib.oracle_tpcc_resolve.argtypes = [C.POINTER(P), U32, C.POINTER(abi.TpccBatchC), C.c_int, P, P]
         _lib.oracle_tpcc_batch.restype = I64
         _lib.oracle_tpcc_batch.argtypes = [C.POINTER(P), U32, C.POINTER(abi.TpccBatchC), C.c_int, P, P, P, P, P]
+        _lib.oracle_tpcc_batch_mt.restype = I64
+        _lib.oracle_tpcc_batch_mt.argtypes = [C.POINTER(P), U32, C.POINTER(abi.TpccBatchC), C.c_int, P, P, P, P, P,
+                                              C.c_int]
     return _lib
 
 
@@ -102,7 +105,8 @@ class YcsbOracle:
 
 
 class TpccOracle:
-    """Single-threaded replay over host copies of the nine TPC-C tables."""
+    """Replay over host copies of the nine TPC-C tables (one thread, or
+    several for the CPU baseline)."""
 
     def __init__(self, seed, warehouses, strict=False, ref_name_lookup=False):
         self.W = int(warehouses)
@@ -127,14 +131,20 @@ class TpccOracle:
         lib().oracle_tpcc_resolve(self._ptrs, self.W, C.byref(cb), self.strict, _p(cid), _p(found))
         return cid, found.astype(bool)
 
-    def run(self, batch):
+    def run(self, batch, threads=1):
+        """Replays one batch; threads > 1: the same phases on that many host
+        threads (identical outputs and image)."""
         B = batch.n_txn
         flags = np.zeros(B, dtype=np.uint8)
         bitmap = np.zeros((B + 31) // 32, dtype=np.uint32)
         results = np.zeros(B, dtype=np.int64)
         cb = batch.as_c()
-        commits = lib().oracle_tpcc_batch(self._ptrs, self.W, C.byref(cb), self.strict, _p(self.reg_r),
-                                          _p(self.reg_w), _p(flags), _p(bitmap), _p(results))
+        if threads > 1:
+            commits = lib().oracle_tpcc_batch_mt(self._ptrs, self.W, C.byref(cb), self.strict, _p(self.reg_r),
+                                                 _p(self.reg_w), _p(flags), _p(bitmap), _p(results), int(threads))
+        else:
+            commits = lib().oracle_tpcc_batch(self._ptrs, self.W, C.byref(cb), self.strict, _p(self.reg_r),
+                                              _p(self.reg_w), _p(flags), _p(bitmap), _p(results))
         if commits < 0:
             raise ValueError("invalid TPC-C batch")
         return flags, bitmap, results, int(commits)

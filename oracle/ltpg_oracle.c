@@ -512,6 +512,22 @@ void oracle_tpcc_resolve(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, i
     }
 }
 
+/* The records with by-name customers resolved (rx) and the not-found marks. */
+static void tpcc_resolve_into(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int cfg_flags, ltpg_tpcc_txn *rx,
+                              uint8_t *nf) {
+    for (uint32_t t = 0; t < b->n_txn; ++t) {
+        ltpg_tpcc_txn x = b->txns[t];
+        const uint32_t c_d = k_cd(x.kind_info);
+        if ((k_kind(x.kind_info) == LTPG_TPCC_PAYMENT || k_kind(x.kind_info) == LTPG_TPCC_ORDERSTATUS) &&
+            (x.kind_info & LTPG_PAY_BY_NAME) && x.c_w < W && c_d < 10) {
+            const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
+            if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) x.c_id = ref_name_lookup(tab, W, x.c_w, c_d, name, nth);
+            else if (!name_lookup(tab, x.c_w, c_d, name, nth, &x.c_id)) nf[t] = 1;
+        }
+        rx[t] = x;
+    }
+}
+
 int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int cfg_flags, uint32_t *reg_r,
                           uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap, int64_t *results) {
     /* resolve by-name Payments first (the reference's KERNEL_CID pre-phase,
@@ -524,17 +540,7 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
         free(nf);
         return -1;
     }
-    for (uint32_t t = 0; t < B; ++t) {
-        ltpg_tpcc_txn x = b->txns[t];
-        const uint32_t c_d = k_cd(x.kind_info);
-        if ((k_kind(x.kind_info) == LTPG_TPCC_PAYMENT || k_kind(x.kind_info) == LTPG_TPCC_ORDERSTATUS) &&
-            (x.kind_info & LTPG_PAY_BY_NAME) && x.c_w < W && c_d < 10) {
-            const uint32_t name = x.c_id >> 8, nth = x.c_id & 0xFFu;
-            if (cfg_flags & LTPG_CFG_REF_NAME_LOOKUP) x.c_id = ref_name_lookup(tab, W, x.c_w, c_d, name, nth);
-            else if (!name_lookup(tab, x.c_w, c_d, name, nth, &x.c_id)) nf[t] = 1;
-        }
-        rx[t] = x;
-    }
+    tpcc_resolve_into(tab, W, b, cfg_flags, rx, nf);
     ltpg_tpcc_batch rb = *b;
     rb.txns = rx;
     const int64_t r = tpcc_batch_resolved(tab, W, &rb, nf, cfg_flags & LTPG_CFG_STRICT_INSERT, reg_r, reg_w, flags,
@@ -544,14 +550,136 @@ int64_t oracle_tpcc_batch(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, 
     return r;
 }
 
-static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, const uint8_t *nf,
-                                   int strict, uint32_t *reg_r, uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap,
-                                   int64_t *results) {
-    uint64_t base[LTPG_TPCC_TABLES], acc = 0;
+/* One transaction's registrations and execute-phase reads (its result).
+   atomic: concurrent registration by several threads. */
+static void tpcc_exec_one(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int strict, const uint64_t *base,
+                          uint32_t *reg_r, uint32_t *reg_w, int64_t *results, uint32_t t, int atomic) {
+    cc_op ops[5 + 3 * LTPG_TPCC_MAX_LINES];
+    const ltpg_tpcc_txn *x = &b->txns[t];
+    const int m = txn_ops(x, b->lines, b->n_lines, W, strict, ops);
+    for (int j = 0; j < m; ++j) {
+        const uint64_t s = base[ops[j].table] + ops[j].row;
+        if (atomic) {
+            if (ops[j].flags & R_REG) atomic_min_u32(&reg_r[s], t);
+            if (ops[j].flags & W_REG) atomic_min_u32(&reg_w[s], t);
+        } else {
+            if ((ops[j].flags & R_REG) && t < reg_r[s]) reg_r[s] = t;
+            if ((ops[j].flags & W_REG) && t < reg_w[s]) reg_w[s] = t;
+        }
+    }
+    const uint32_t d = k_d(x->kind_info);
+    if (k_kind(x->kind_info) == LTPG_TPCC_NEWORDER) {
+        int64_t sum = 0;
+        for (uint32_t i = 0; i < k_cnt(x->kind_info); ++i) {
+            const ltpg_tpcc_line *ln = &b->lines[x->line_off + i];
+            sum += (int64_t)ln->qty * (int64_t)*colp(tab, LTPG_T_ITEM, ln->i_id, 2);
+        }
+        const int64_t disc = (int64_t)*colp(tab, LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, 4);
+        const int64_t wtax = (int64_t)*colp(tab, LTPG_T_WAREHOUSE, x->w, 1);
+        const int64_t dtax = (int64_t)*colp(tab, LTPG_T_DISTRICT, 10ull * x->w + d, 2);
+        results[t] = sum * (10000 - disc) * (10000 + wtax + dtax) / 100000000;
+    } else if (k_kind(x->kind_info) == LTPG_TPCC_PAYMENT) {
+        const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
+        results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5) - amount_of(x);
+    } else if (k_kind(x->kind_info) == LTPG_TPCC_ORDERSTATUS) {  /* C_BALANCE */
+        const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
+        results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5);
+    } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {  /* the line's OL_AMOUNT */
+        results[t] = (int64_t)*colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 8);
+    } else {  /* StockLevel: S_QUANTITY */
+        results[t] = (int64_t)*colp(tab, LTPG_T_STOCK, 100000ull * x->w + x->a, 2);
+    }
+}
+
+/* One transaction's conflict flags and commit bit. */
+static uint32_t tpcc_check_one(uint32_t W, const ltpg_tpcc_batch *b, int strict, const uint64_t *base,
+                               const uint32_t *reg_r, const uint32_t *reg_w, uint32_t t) {
+    cc_op ops[5 + 3 * LTPG_TPCC_MAX_LINES];
+    const int m = txn_ops(&b->txns[t], b->lines, b->n_lines, W, strict, ops);
+    uint32_t f = 0;
+    for (int j = 0; j < m; ++j) {
+        const uint64_t s = base[ops[j].table] + ops[j].row;
+        if ((ops[j].flags & C_RAW) && reg_w[s] < t) f |= LTPG_FLAG_RAW;
+        if ((ops[j].flags & C_WAR) && reg_r[s] < t) f |= LTPG_FLAG_WAR;
+        if ((ops[j].flags & C_WAW) && reg_w[s] < t) f |= LTPG_FLAG_WAW;
+    }
+    return f | commit_rule(f);
+}
+
+/* Write-back of one committed transaction.  atomic: the warehouse / district
+   YTD adds (the only rows several committed transactions write) are atomic. */
+static void tpcc_write_one(uint64_t **tab, const ltpg_tpcc_batch *b, const int64_t *results, uint32_t t,
+                           int atomic) {
+    const ltpg_tpcc_txn *x = &b->txns[t];
+    const uint32_t d = k_d(x->kind_info);
+    const uint64_t date = b->txn_base + t;
+    if (k_kind(x->kind_info) == LTPG_TPCC_NEWORDER) {
+        const uint32_t cnt = k_cnt(x->kind_info);
+        int all_local = 1;
+        for (uint32_t i = 0; i < cnt; ++i) {
+            const ltpg_tpcc_line *ln = &b->lines[x->line_off + i];
+            const uint64_t srow = 100000ull * ln->supply_w + ln->i_id;
+            all_local &= ln->supply_w == x->w;
+            uint64_t *s = colp(tab, LTPG_T_STOCK, srow, 0);
+            /* S_QUANTITY rule of TPC-C clause 2.4.2.2 */
+            s[2] = s[2] >= (uint64_t)ln->qty + 10u ? s[2] - ln->qty : s[2] - ln->qty + 91u;
+            s[3] += ln->qty;
+            s[4] += 1;
+            s[5] += ln->supply_w != x->w;
+            uint64_t *o = colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + (x->c + i) % 450000u, 0);
+            o[0] = x->a; o[1] = d; o[2] = x->w; o[3] = i + 1; o[4] = ln->i_id; o[5] = ln->supply_w;
+            o[6] = 0; o[7] = ln->qty; o[8] = (uint64_t)ln->qty * *colp(tab, LTPG_T_ITEM, ln->i_id, 2);
+            o[9] = *colp(tab, LTPG_T_STOCK, srow, 6 + d);
+        }
+        uint64_t *o = colp(tab, LTPG_T_ORDER, 30000ull * x->w + x->a, 0);
+        o[0] = x->a; o[1] = d; o[2] = x->w; o[3] = x->c_id; o[4] = date; o[5] = 0; o[6] = cnt;
+        o[7] = (uint64_t)all_local;
+        uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
+        no[0] = x->a; no[1] = d; no[2] = x->w;
+    } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {
+        uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
+        no[0] = no[1] = no[2] = ~0ull; /* deleted */
+        *colp(tab, LTPG_T_ORDER, 30000ull * x->w + x->a, 5) = k_cnt(x->kind_info);   /* O_CARRIER_ID */
+        *colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 6) = date;              /* OL_DELIVERY_D */
+        uint64_t *c = colp(tab, LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, 0);
+        c[5] = (uint64_t)((int64_t)c[5] + results[t]);                                 /* C_BALANCE */
+        c[8] += 1;                                                                     /* C_DELIVERY_CNT */
+    } else if (k_kind(x->kind_info) != LTPG_TPCC_PAYMENT) {
+        /* OrderStatus, StockLevel: read-only */
+    } else {
+        const int64_t amt = amount_of(x);
+        const uint32_t c_d = k_cd(x->kind_info);
+        uint64_t *wy = colp(tab, LTPG_T_WAREHOUSE, x->w, 2), *dy = colp(tab, LTPG_T_DISTRICT, 10ull * x->w + d, 3);
+        if (atomic) {
+            __atomic_fetch_add(wy, (uint64_t)amt, __ATOMIC_RELAXED);
+            __atomic_fetch_add(dy, (uint64_t)amt, __ATOMIC_RELAXED);
+        } else {
+            *wy += (uint64_t)amt;
+            *dy += (uint64_t)amt;
+        }
+        uint64_t *c = colp(tab, LTPG_T_CUSTOMER, 30000ull * x->c_w + 3000ull * c_d + x->c_id, 0);
+        c[5] = (uint64_t)((int64_t)c[5] - amt);
+        c[6] = (uint64_t)((int64_t)c[6] + amt);
+        c[7] += 1;
+        uint64_t *h = colp(tab, LTPG_T_HISTORY, 30000ull * x->w + x->a, 0);
+        h[0] = x->c_id; h[1] = c_d; h[2] = x->c_w; h[3] = d; h[4] = x->w; h[5] = (uint64_t)amt; h[6] = date;
+        h[7] = 0;
+    }
+}
+
+static void tpcc_bases(uint32_t W, uint64_t *base) {
+    uint64_t acc = 0;
     for (uint32_t t = 0; t < LTPG_TPCC_TABLES; ++t) {
         base[t] = acc;
         acc += oracle_tpcc_rows(t, W);
     }
+}
+
+static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, const uint8_t *nf,
+                                   int strict, uint32_t *reg_r, uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap,
+                                   int64_t *results) {
+    uint64_t base[LTPG_TPCC_TABLES];
+    tpcc_bases(W, base);
     cc_op ops[5 + 3 * LTPG_TPCC_MAX_LINES];
     const uint32_t B = b->n_txn;
     /* validate and clear the touched slots */
@@ -563,39 +691,8 @@ static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_b
     }
     /* phase 1: register + reads of the execute phase */
     for (uint32_t t = 0; t < B; ++t) {
-        const ltpg_tpcc_txn *x = &b->txns[t];
-        if (nf[t]) {
-            results[t] = 0;
-            continue;
-        }
-        const int m = txn_ops(x, b->lines, b->n_lines, W, strict, ops);
-        for (int j = 0; j < m; ++j) {
-            const uint64_t s = base[ops[j].table] + ops[j].row;
-            if ((ops[j].flags & R_REG) && t < reg_r[s]) reg_r[s] = t;
-            if ((ops[j].flags & W_REG) && t < reg_w[s]) reg_w[s] = t;
-        }
-        const uint32_t d = k_d(x->kind_info);
-        if (k_kind(x->kind_info) == LTPG_TPCC_NEWORDER) {
-            int64_t sum = 0;
-            for (uint32_t i = 0; i < k_cnt(x->kind_info); ++i) {
-                const ltpg_tpcc_line *ln = &b->lines[x->line_off + i];
-                sum += (int64_t)ln->qty * (int64_t)*colp(tab, LTPG_T_ITEM, ln->i_id, 2);
-            }
-            const int64_t disc = (int64_t)*colp(tab, LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, 4);
-            const int64_t wtax = (int64_t)*colp(tab, LTPG_T_WAREHOUSE, x->w, 1);
-            const int64_t dtax = (int64_t)*colp(tab, LTPG_T_DISTRICT, 10ull * x->w + d, 2);
-            results[t] = sum * (10000 - disc) * (10000 + wtax + dtax) / 100000000;
-        } else if (k_kind(x->kind_info) == LTPG_TPCC_PAYMENT) {
-            const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
-            results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5) - amount_of(x);
-        } else if (k_kind(x->kind_info) == LTPG_TPCC_ORDERSTATUS) {  /* C_BALANCE */
-            const uint64_t crow = 30000ull * x->c_w + 3000ull * k_cd(x->kind_info) + x->c_id;
-            results[t] = (int64_t)*colp(tab, LTPG_T_CUSTOMER, crow, 5);
-        } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {  /* the line's OL_AMOUNT */
-            results[t] = (int64_t)*colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 8);
-        } else {  /* StockLevel: S_QUANTITY */
-            results[t] = (int64_t)*colp(tab, LTPG_T_STOCK, 100000ull * x->w + x->a, 2);
-        }
+        if (nf[t]) results[t] = 0;
+        else tpcc_exec_one(tab, W, b, strict, base, reg_r, reg_w, results, t, 0);
     }
     /* phase 2: check */
     int64_t commits = 0;
@@ -605,15 +702,7 @@ static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_b
             flags[t] = LTPG_FLAG_NOT_FOUND;
             continue;
         }
-        const int m = txn_ops(&b->txns[t], b->lines, b->n_lines, W, strict, ops);
-        uint32_t f = 0;
-        for (int j = 0; j < m; ++j) {
-            const uint64_t s = base[ops[j].table] + ops[j].row;
-            if ((ops[j].flags & C_RAW) && reg_w[s] < t) f |= LTPG_FLAG_RAW;
-            if ((ops[j].flags & C_WAR) && reg_r[s] < t) f |= LTPG_FLAG_WAR;
-            if ((ops[j].flags & C_WAW) && reg_w[s] < t) f |= LTPG_FLAG_WAW;
-        }
-        f |= commit_rule(f);
+        const uint32_t f = tpcc_check_one(W, b, strict, base, reg_r, reg_w, t);
         flags[t] = (uint8_t)f;
         if (f & LTPG_FLAG_COMMIT) {
             bitmap[t >> 5] |= 1u << (t & 31);
@@ -621,57 +710,117 @@ static int64_t tpcc_batch_resolved(uint64_t **tab, uint32_t W, const ltpg_tpcc_b
         }
     }
     /* phase 3: write-back of committed transactions in TID order */
-    for (uint32_t t = 0; t < B; ++t) {
-        if (!(flags[t] & LTPG_FLAG_COMMIT)) continue;
-        const ltpg_tpcc_txn *x = &b->txns[t];
-        const uint32_t d = k_d(x->kind_info);
-        const uint64_t date = b->txn_base + t;
-        if (k_kind(x->kind_info) == LTPG_TPCC_NEWORDER) {
-            const uint32_t cnt = k_cnt(x->kind_info);
-            int all_local = 1;
-            for (uint32_t i = 0; i < cnt; ++i) {
-                const ltpg_tpcc_line *ln = &b->lines[x->line_off + i];
-                const uint64_t srow = 100000ull * ln->supply_w + ln->i_id;
-                all_local &= ln->supply_w == x->w;
-                uint64_t *s = colp(tab, LTPG_T_STOCK, srow, 0);
-                /* S_QUANTITY rule of TPC-C clause 2.4.2.2 */
-                s[2] = s[2] >= (uint64_t)ln->qty + 10u ? s[2] - ln->qty : s[2] - ln->qty + 91u;
-                s[3] += ln->qty;
-                s[4] += 1;
-                s[5] += ln->supply_w != x->w;
-                uint64_t *o = colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + (x->c + i) % 450000u, 0);
-                o[0] = x->a; o[1] = d; o[2] = x->w; o[3] = i + 1; o[4] = ln->i_id; o[5] = ln->supply_w;
-                o[6] = 0; o[7] = ln->qty; o[8] = (uint64_t)ln->qty * *colp(tab, LTPG_T_ITEM, ln->i_id, 2);
-                o[9] = *colp(tab, LTPG_T_STOCK, srow, 6 + d);
-            }
-            uint64_t *o = colp(tab, LTPG_T_ORDER, 30000ull * x->w + x->a, 0);
-            o[0] = x->a; o[1] = d; o[2] = x->w; o[3] = x->c_id; o[4] = date; o[5] = 0; o[6] = cnt;
-            o[7] = (uint64_t)all_local;
-            uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
-            no[0] = x->a; no[1] = d; no[2] = x->w;
-        } else if (k_kind(x->kind_info) == LTPG_TPCC_DELIVERY) {
-            uint64_t *no = colp(tab, LTPG_T_NEWORDER, 30000ull * x->w + x->b, 0);
-            no[0] = no[1] = no[2] = ~0ull; /* deleted */
-            *colp(tab, LTPG_T_ORDER, 30000ull * x->w + x->a, 5) = k_cnt(x->kind_info);   /* O_CARRIER_ID */
-            *colp(tab, LTPG_T_ORDERLINE, 450000ull * x->w + x->c, 6) = date;              /* OL_DELIVERY_D */
-            uint64_t *c = colp(tab, LTPG_T_CUSTOMER, 30000ull * x->w + 3000ull * d + x->c_id, 0);
-            c[5] = (uint64_t)((int64_t)c[5] + results[t]);                                 /* C_BALANCE */
-            c[8] += 1;                                                                     /* C_DELIVERY_CNT */
-        } else if (k_kind(x->kind_info) != LTPG_TPCC_PAYMENT) {
-            /* OrderStatus, StockLevel: read-only */
-        } else {
-            const int64_t amt = amount_of(x);
-            const uint32_t c_d = k_cd(x->kind_info);
-            *colp(tab, LTPG_T_WAREHOUSE, x->w, 2) += (uint64_t)amt;
-            *colp(tab, LTPG_T_DISTRICT, 10ull * x->w + d, 3) += (uint64_t)amt;
-            uint64_t *c = colp(tab, LTPG_T_CUSTOMER, 30000ull * x->c_w + 3000ull * c_d + x->c_id, 0);
-            c[5] = (uint64_t)((int64_t)c[5] - amt);
-            c[6] = (uint64_t)((int64_t)c[6] + amt);
-            c[7] += 1;
-            uint64_t *h = colp(tab, LTPG_T_HISTORY, 30000ull * x->w + x->a, 0);
-            h[0] = x->c_id; h[1] = c_d; h[2] = x->c_w; h[3] = d; h[4] = x->w; h[5] = (uint64_t)amt; h[6] = date;
-            h[7] = 0;
+    for (uint32_t t = 0; t < B; ++t)
+        if (flags[t] & LTPG_FLAG_COMMIT) tpcc_write_one(tab, b, results, t, 0);
+    return commits;
+}
+
+/* ---- multi-threaded TPC-C replay (CPU baseline with all host threads) ----
+   The same phases on nthreads threads, a barrier between them.  Registration
+   is an atomic minimum; write-back order does not matter: every row but the
+   warehouse / district YTD (atomic adds) has at most one committed writer,
+   and the columns write-back reads (item price, S_DIST_xx) are never
+   written. */
+typedef struct {
+    uint64_t **tab;
+    uint32_t W;
+    const ltpg_tpcc_batch *b;
+    const uint8_t *nf;
+    int strict;
+    const uint64_t *base;
+    uint32_t *reg_r, *reg_w;
+    uint8_t *flags;
+    uint32_t *bitmap;
+    int64_t *results;
+    uint32_t t0, t1;
+    pthread_barrier_t *bar;
+    int *err;
+    int64_t commits;
+} tmt_arg;
+
+static void *tpcc_mt_worker(void *p) {
+    tmt_arg *a = (tmt_arg *)p;
+    cc_op ops[5 + 3 * LTPG_TPCC_MAX_LINES];
+    for (uint32_t t = a->t0; t < a->t1; ++t) {
+        if (a->nf[t]) continue;
+        const int m = txn_ops(&a->b->txns[t], a->b->lines, a->b->n_lines, a->W, a->strict, ops);
+        if (m < 0) {
+            __atomic_store_n(a->err, 1, __ATOMIC_RELAXED);
+            break;
+        }
+        for (int j = 0; j < m; ++j) {
+            const uint64_t s = a->base[ops[j].table] + ops[j].row;
+            __atomic_store_n(&a->reg_r[s], NONE, __ATOMIC_RELAXED);
+            __atomic_store_n(&a->reg_w[s], NONE, __ATOMIC_RELAXED);
         }
     }
-    return commits;
+    pthread_barrier_wait(a->bar);
+    if (__atomic_load_n(a->err, __ATOMIC_RELAXED)) return NULL;
+    for (uint32_t t = a->t0; t < a->t1; ++t) {
+        if (a->nf[t]) a->results[t] = 0;
+        else tpcc_exec_one(a->tab, a->W, a->b, a->strict, a->base, a->reg_r, a->reg_w, a->results, t, 1);
+    }
+    pthread_barrier_wait(a->bar);
+    int64_t commits = 0;
+    for (uint32_t t = a->t0; t < a->t1; ++t) {
+        if (a->nf[t]) {
+            a->flags[t] = LTPG_FLAG_NOT_FOUND;
+            continue;
+        }
+        const uint32_t f = tpcc_check_one(a->W, a->b, a->strict, a->base, a->reg_r, a->reg_w, t);
+        a->flags[t] = (uint8_t)f;
+        if (f & LTPG_FLAG_COMMIT) {
+            __atomic_fetch_or(&a->bitmap[t >> 5], 1u << (t & 31), __ATOMIC_RELAXED);
+            ++commits;
+        }
+    }
+    a->commits = commits;
+    pthread_barrier_wait(a->bar);
+    for (uint32_t t = a->t0; t < a->t1; ++t)
+        if (a->flags[t] & LTPG_FLAG_COMMIT) tpcc_write_one(a->tab, a->b, a->results, t, 1);
+    return NULL;
+}
+
+/* oracle_tpcc_batch on nthreads host threads: the same outputs and image. */
+int64_t oracle_tpcc_batch_mt(uint64_t **tab, uint32_t W, const ltpg_tpcc_batch *b, int cfg_flags, uint32_t *reg_r,
+                             uint32_t *reg_w, uint8_t *flags, uint32_t *bitmap, int64_t *results, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    const uint32_t B = b->n_txn;
+    ltpg_tpcc_txn *rx = (ltpg_tpcc_txn *)malloc((size_t)(B ? B : 1) * sizeof *rx);
+    uint8_t *nf = (uint8_t *)calloc(B ? B : 1, 1);
+    if (!rx || !nf) {
+        free(rx);
+        free(nf);
+        return -1;
+    }
+    tpcc_resolve_into(tab, W, b, cfg_flags, rx, nf);
+    ltpg_tpcc_batch rb = *b;
+    rb.txns = rx;
+    uint64_t base[LTPG_TPCC_TABLES];
+    tpcc_bases(W, base);
+    memset(bitmap, 0, ((size_t)B + 31) / 32 * 4);
+    pthread_t th[256];
+    tmt_arg args[256];
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)nthreads);
+    int err = 0;
+    const uint32_t chunk = (B + (uint32_t)nthreads - 1) / (uint32_t)nthreads;
+    for (int i = 0; i < nthreads; ++i) {
+        uint32_t t0 = (uint32_t)i * chunk, t1 = t0 + chunk;
+        if (t0 > B) t0 = B;
+        if (t1 > B) t1 = B;
+        args[i] = (tmt_arg){tab, W, &rb, nf, cfg_flags & LTPG_CFG_STRICT_INSERT, base, reg_r, reg_w, flags,
+                            bitmap, results, t0, t1, &bar, &err, 0};
+        pthread_create(&th[i], NULL, tpcc_mt_worker, &args[i]);
+    }
+    int64_t commits = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        pthread_join(th[i], NULL);
+        commits += args[i].commits;
+    }
+    pthread_barrier_destroy(&bar);
+    free(rx);
+    free(nf);
+    return err ? -1 : commits;
 }

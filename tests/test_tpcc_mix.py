@@ -99,3 +99,20 @@ def test_mix_generator_shares_and_stream_stability():
     assert np.array_equal(dl["a"], dl["b"])
     carrier = (dl["kind_info"] >> 8) & 0xFF
     assert carrier.min() >= 1 and carrier.max() <= 10
+
+
+def test_multithreaded_replay_equals_single_threaded():
+    """The oracle's pthreads replay (the reference arm's CPU baseline) gives the
+    single-threaded replay's flags, bitmap, results and image, batch after
+    batch, with names, all five kinds and hot YTD adds."""
+    W, B = 2, 20000
+    kw = dict(neworder_pct=45, orderstatus_pct=4, delivery_pct=4, stocklevel_pct=4, by_name_pct=60)
+    o1, o8 = oracle.TpccOracle(41, W), oracle.TpccOracle(41, W)
+    g = TpccGenerator(41, W, B, **kw)
+    for _ in range(3):
+        b = g.next()
+        a, m = o1.run(b), o8.run(b, threads=8)
+        for x, y in zip(a, m):
+            assert np.array_equal(x, y)
+    for t1, t8 in zip(o1.tables, o8.tables):
+        assert np.array_equal(t1, t8)
