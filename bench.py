@@ -260,6 +260,20 @@ def timed(eng, torch, n_slots, steps, mode, start, dist):
     return ev0.elapsed_time(ev1) / 1e3, c1 - c0, l1 - l0, nxt
 
 
+def kernel_split(eng, n_slots, mode, start):
+    """Per-kernel times of one more pass over the slots, after the timed region:
+    the events that split a batch into its kernels are recorded only here, so
+    the timed region carries no instrumentation (on 40-us batches it cost a
+    quarter of the time).  Rows: slots; columns: execute, check+write-back,
+    (unused)."""
+    eng.set_profiling(True)
+    run_steps(eng, n_slots, n_slots, mode, start)
+    eng.sync()
+    kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
+    eng.set_profiling(False)
+    return kt
+
+
 def modes_run(eng, torch, n_slots, steps, reload):
     """The same resident batches through each execution mode of the tuned
     path: fused (two kernels per batch), graph (one CUDA graph over the
@@ -329,14 +343,9 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
             eng.load_ycsb(SEED, w["n_records"])
             eng.sync()
             nxt = run_steps(eng, n_slots, args.warmup, mode)
-            if mode != "plain" and want_extras:
-                eng.set_profiling(True)
             with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-                secs, commits, launches, _ = timed(eng, torch, n_slots, args.steps, mode, nxt, dist)
-            kt = None
-            if mode != "plain" and want_extras:
-                kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
-                eng.set_profiling(False)
+                secs, commits, launches, nxt = timed(eng, torch, n_slots, args.steps, mode, nxt, dist)
+            kt = kernel_split(eng, n_slots, mode, nxt) if mode != "plain" and want_extras else None
             res[mode] = dict(secs=secs, commits=commits, launches=launches, clocks=clk.summary(), kt=kt)
         if want_extras:
             res["modes"] = modes_run(eng, torch, n_slots, min(args.steps, 64),
@@ -415,14 +424,9 @@ def tpcc_bench(args, w, dist, want_extras=True):
             eng.load_tpcc(SEED, w["warehouses"])
             eng.sync()
             nxt = run_steps(eng, n_slots, args.warmup, mode)
-            if mode != "plain":
-                eng.set_profiling(True)
             with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-                secs, commits, launches, _ = timed(eng, torch, n_slots, args.steps, mode, nxt, dist)
-            kt = None
-            if mode != "plain":
-                kt = np.array([eng.kernel_times(s) for s in range(n_slots)])
-                eng.set_profiling(False)
+                secs, commits, launches, nxt = timed(eng, torch, n_slots, args.steps, mode, nxt, dist)
+            kt = kernel_split(eng, n_slots, mode, nxt) if mode != "plain" else None
             res[mode] = dict(secs=secs, commits=commits, launches=launches, clocks=clk.summary(), kt=kt)
         if want_extras:
             res["modes"] = modes_run(eng, torch, n_slots, min(args.steps, 64),
