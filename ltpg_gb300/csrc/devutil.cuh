@@ -105,17 +105,6 @@ __device__ __forceinline__ void finish_batch(DevCtl *ctl) {
     }
 }
 
-// Warp-cooperative scatter list: lane L owns n_L items (inclusive prefix incl);
-// returns the lane that owns item e (0 <= e < total).
-__device__ __forceinline__ int owner_lane(int incl, unsigned e) {
-    int lo = 0;
-#pragma unroll
-    for (int s = 16; s >= 1; s >>= 1) {
-        const unsigned v = (unsigned)__shfl_sync(FULL, incl, lo + s - 1);
-        if (v <= e) lo += s;
-    }
-    return lo;
-}
 __device__ __forceinline__ int warp_incl_scan(int v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll

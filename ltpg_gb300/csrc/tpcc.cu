@@ -463,11 +463,24 @@ __device__ __forceinline__ void tpcc_apply_write(const TpccDev &db, const ltpg_t
         const ltpg_tpcc_line ln = load_line(lines, (uint64_t)x.line_off + i);
         const uint64_t srow = 100000ull * ln.supply_w + ln.i_id;
         if ((q & 1u) == 0u) {
+            // Atomic, so that an order listing one stock row twice (the
+            // reference's generator draws distinct items, a caller's batch
+            // need not) updates it once per line.  Order does not matter: for
+            // S_QUANTITY in [10, 100] and quantities <= 91 the rule keeps the
+            // value in [10, 100], so after any set of lines it is
+            // 10 + ((q - sum - 10) mod 91) whatever their order; the counters
+            // add.  No other committed transaction writes the row (WAW).
             uint64_t *s = col_ptr(db, LTPG_T_STOCK, srow, 0);
-            s[S_QUANTITY] = stock_after(s[S_QUANTITY], ln.qty);
-            s[S_YTD] += ln.qty;
-            s[S_ORDER_CNT] += 1u;
-            s[S_REMOTE_CNT] += (ln.supply_w != x.w) ? 1u : 0u;
+            unsigned long long *qp = reinterpret_cast<unsigned long long *>(s + S_QUANTITY);
+            unsigned long long cur = *qp;
+            for (uint32_t tries = 0; tries < 64u; ++tries) {  // contenders: the order's own lines
+                const unsigned long long prev = atomicCAS(qp, cur, (unsigned long long)stock_after(cur, ln.qty));
+                if (prev == cur) break;
+                cur = prev;
+            }
+            red_add_u64(reinterpret_cast<unsigned long long *>(s + S_YTD), ln.qty);
+            red_add_u64(reinterpret_cast<unsigned long long *>(s + S_ORDER_CNT), 1ull);
+            if (ln.supply_w != x.w) red_add_u64(reinterpret_cast<unsigned long long *>(s + S_REMOTE_CNT), 1ull);
         } else {
             uint64_t *o = col_ptr(db, LTPG_T_ORDERLINE, tpcc_ol_row(x.w, x.c, i), 0);
             o[OL_O_ID] = x.a; o[OL_D_ID] = d; o[OL_W_ID] = x.w; o[OL_NUMBER] = i + 1u;

@@ -100,29 +100,11 @@ __global__ void __launch_bounds__(256) ycsb_check_plain(const uint32_t *__restri
     }
 }
 
-// Writes of one committed transaction, found by rank r among its updates.
-__device__ __forceinline__ void ycsb_apply_update(const uint32_t *__restrict__ ops, uint32_t t, uint32_t k,
-                                                  uint32_t stride, uint32_t r, uint64_t value,
-                                                  uint64_t *__restrict__ rows, uint64_t n) {
-    const uint32_t *w = ops + (uint64_t)t * stride;
-    uint32_t seen = 0;
-    for (uint32_t j = 0; j < k; ++j) {
-        const uint32_t x = w[j];
-        if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
-        if (seen == r) {
-            const uint32_t key = ycsb_key(x), f = ycsb_field(x);
-            if (key < n && f < LTPG_YCSB_FIELDS) rows[(uint64_t)key * LTPG_YCSB_FIELDS + f] = value;
-            return;
-        }
-        ++seen;
-    }
-}
-
 // ---- plain phase 3: write-back (KERNEL_WRITEBACK, Y1/ycsb.cu:41-58) ----------
 // One thread per transaction.  The commit bitmap word of a warp is its ballot.
-// The warp's committed updates are compacted by a prefix sum over their counts
-// and scattered by all 32 lanes, so idle lanes of aborted or read-only
-// transactions take part in the stores.
+// A committed transaction's updates are stored by its own thread in op order,
+// so one that updates a field twice leaves its later value (as a sequential
+// replay does); no two committed transactions write one row (WAW).
 __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__restrict__ flags, uint32_t B,
                                                             const uint32_t *__restrict__ ops, uint32_t k,
                                                             uint32_t stride, const uint32_t *__restrict__ val_off,
@@ -148,22 +130,15 @@ __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__res
         if (bwar) red_add_u64(&st->war, __popc(bwar));
         if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
     }
-    uint32_t v0 = 0, nu = 0;
-    if (com) {
-        v0 = val_off[t];
-        nu = val_off[t + 1] - v0;
-    }
-    const int incl = warp_incl_scan((int)nu);
-    const unsigned total = (unsigned)__shfl_sync(FULL, incl, 31);
-    const uint32_t t_warp = t - lane;
-    for (unsigned base = 0; base < total; base += 32) {
-        const unsigned e = base + lane;
-        const int L = owner_lane(incl, e);
-        const int excl_L = __shfl_sync(FULL, incl, L) - __shfl_sync(FULL, (int)nu, L);
-        const uint32_t v0_L = (uint32_t)__shfl_sync(FULL, (int)v0, L);
-        if (e < total) {
-            const uint32_t r = e - (unsigned)excl_L;
-            ycsb_apply_update(ops, t_warp + L, k, stride, r, vals[v0_L + r], rows, n);
+    if (com && val_off[t + 1] != val_off[t]) {
+        uint32_t v = val_off[t];
+        const uint32_t *w = ops + (uint64_t)t * stride;
+        for (uint32_t j = 0; j < k; ++j) {
+            const uint32_t x = w[j];
+            if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
+            const uint32_t key = ycsb_key(x), f = ycsb_field(x);
+            if (key < n && f < LTPG_YCSB_FIELDS) rows[(uint64_t)key * LTPG_YCSB_FIELDS + f] = vals[v];
+            ++v;
         }
     }
     finish_batch(ctl);

@@ -12,8 +12,8 @@
 //     tags are smaller, and within a batch atomicMin only lowers), so any value
 //     observed, stale or not, is >= the current one: the skip is exact;
 //   * check and write-back run in one kernel: the commit decision of a tile is
-//     made in shared memory and the tile's committed updates are compacted per
-//     warp (ballot + prefix sum) before they are scattered.
+//     made in shared memory, then each committed transaction's thread stores
+//     its updates in op order.
 #include "stage.cuh"
 
 namespace ltpg {
@@ -125,11 +125,10 @@ __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long
 }
 
 // ---- check + write-back over all tiles assigned to this block ------------------
-// fl: tile flags; wbuf: per-warp compaction buffers of 128 (address, value) pairs.
-__device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *fl, ulonglong2 *wbuf,
+// fl: tile flags.
+__device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *fl,
                                               uint32_t epoch) {
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    ulonglong2 *mybuf = wbuf + warp * 128;
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t nvec_tile = a.tile * a.stride / 4;
     const uint32_t n_tiles = (a.B + a.tile - 1) / a.tile;
     unsigned long long c_com = 0, c_raw = 0, c_war = 0, c_waw = 0;
@@ -187,55 +186,28 @@ __device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *
             }
         }
         __syncthreads();
-        // pass 3: committed updates, compacted per warp, then scattered
-        for (uint32_t base = 0; base < nvec_tile; base += blockDim.x) {
-            const uint32_t v = base + threadIdx.x;
-            const bool act = v < nvec;
-            uint4 w4 = make_uint4(LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD);
-            uint32_t lt = 0, j0 = 0;
-            bool com = false;
-            if (act) {
-                lt = (v * 4) / a.stride;
-                j0 = v * 4 - lt * a.stride;
-                com = (fl[lt] & LTPG_FLAG_COMMIT) != 0u && a.val_off[t0 + lt + 1] != a.val_off[t0 + lt];
-                if (com) w4 = ld_nc_u4(vp + v);
-            }
-            const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
-            uint32_t mask = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (!ycsb_is_pad(words[q]) && ycsb_is_update(words[q])) mask |= 1u << q;
-            const int cnt = __popc(mask);
-            const int incl = warp_incl_scan(cnt);
-            const int total = __shfl_sync(FULL, incl, 31);
-            if (total == 0) continue;
-            if (cnt) {
-                // rank of this thread's first update among its transaction's updates
-                const uint32_t t = t0 + lt;
-                const uint32_t *tw = a.ops + (uint64_t)t * a.stride;
-                uint32_t rank = 0;
-                for (uint32_t j = 0; j < j0; ++j) {
-                    const uint32_t x = tw[j];
-                    rank += !ycsb_is_pad(x) && ycsb_is_update(x);
-                }
-                const uint32_t vb = a.val_off[t] + rank;
-                int slot = incl - cnt, r = 0;
+        // pass 3: committed updates, one thread per transaction in op order:
+        // a transaction that updates a field twice leaves its later value (as a
+        // sequential replay does), and no two committed transactions write one
+        // row (WAW)
+        for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
+            if (!(fl[i] & LTPG_FLAG_COMMIT)) continue;
+            const uint32_t t = t0 + i;
+            uint32_t v = a.val_off[t];
+            if (v == a.val_off[t + 1]) continue;
+            const uint4 *tw = reinterpret_cast<const uint4 *>(a.ops + (uint64_t)t * a.stride);
+            for (uint32_t q4 = 0; q4 < a.stride / 4u; ++q4) {
+                const uint4 w4 = ld_nc_u4(tw + q4);
+                const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    if (!(mask & (1u << q))) continue;
-                    const uint32_t key = ycsb_key(words[q]), fld = ycsb_field(words[q]);
-                    const bool ok = key < a.n && fld < LTPG_YCSB_FIELDS;
-                    const uint64_t addr = ok ? (uint64_t)(a.rows + (uint64_t)key * LTPG_YCSB_FIELDS + fld) : 0ull;
-                    mybuf[slot++] = make_ulonglong2(addr, a.vals[vb + r]);
-                    ++r;
+                    const uint32_t x = words[q];
+                    if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
+                    const uint32_t key = ycsb_key(x), fld = ycsb_field(x);
+                    if (key < a.n && fld < LTPG_YCSB_FIELDS) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = a.vals[v];
+                    ++v;
                 }
             }
-            __syncwarp();
-            for (int e = lane; e < total; e += 32) {
-                const ulonglong2 x = mybuf[e];
-                if (x.x) *reinterpret_cast<uint64_t *>(x.x) = x.y;
-            }
-            __syncwarp();
         }
         __syncthreads();
     }
@@ -559,17 +531,17 @@ __global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
     }
 }
 
-// Shared memory layout: [dig: tile u64][fl: tile u32][wbuf: warps*128*16 B][stage table]
+// Shared memory layout: [dig: tile u64][fl: tile u32][stage table]
 __host__ __device__ __forceinline__ size_t ycsb_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage_entries) {
+    (void)threads;
     const size_t a = ((size_t)tile * 8 + 15) / 16 * 16;
     const size_t b = ((size_t)tile * 4 + 15) / 16 * 16;
-    return a + b + (size_t)(threads / 32) * 128 * 16 + (size_t)stage_entries * sizeof(StageEnt);
+    return a + b + (size_t)stage_entries * sizeof(StageEnt);
 }
 
 struct SmemPtrs {
     unsigned long long *dig;
     uint32_t *fl;
-    ulonglong2 *wbuf;
     StageEnt *tab;
 };
 __device__ __forceinline__ SmemPtrs carve(char *base, uint32_t tile) {
@@ -578,8 +550,7 @@ __device__ __forceinline__ SmemPtrs carve(char *base, uint32_t tile) {
     const size_t b = ((size_t)tile * 4 + 15) / 16 * 16;
     p.dig = reinterpret_cast<unsigned long long *>(base);
     p.fl = reinterpret_cast<uint32_t *>(base + a);
-    p.wbuf = reinterpret_cast<ulonglong2 *>(base + a + b);
-    p.tab = reinterpret_cast<StageEnt *>(base + a + b + (blockDim.x / 32) * 128 * 16);
+    p.tab = reinterpret_cast<StageEnt *>(base + a + b);
     return p;
 }
 
@@ -603,7 +574,7 @@ __global__ void __launch_bounds__(512) ycsb_exec_tuned(YcsbTunedArgs a) {
 __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     const SmemPtrs p = carve(smem, a.tile);
-    checkwb_tiles(a, p.fl, p.wbuf, a.ctl->epoch);
+    checkwb_tiles(a, p.fl, a.ctl->epoch);
     finish_batch(a.ctl);
 }
 
@@ -630,7 +601,7 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         const uint32_t ops = stage_flush(p.tab, a.stage_entries, a.reg, tag, a.bucket_counts);
         if (ops) red_add_u64(&a.st->staged_ops, ops);
     }
-    if (grid_barrier(a.ctl, 2000000000ull)) checkwb_tiles(a, p.fl, p.wbuf, epoch);
+    if (grid_barrier(a.ctl, 2000000000ull)) checkwb_tiles(a, p.fl, epoch);
     finish_batch(a.ctl);
 }
 
