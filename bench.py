@@ -70,7 +70,8 @@ def parse():
     ap.add_argument("--cpu-batches", type=int, default=12,
                     help="batches in the CPU-baseline sample (about 10 s of oracle replay at the default sizes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=32)
+    ap.add_argument("--e2e-steps", type=int, default=64,
+                    help="steps of the end-to-end leg (host wall clock; long enough to average out host stalls)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-device-gen", action="store_true", help="skip the device-generator section")
     ap.add_argument("--no-tune", action="store_true",
