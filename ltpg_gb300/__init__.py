@@ -464,7 +464,7 @@ class Engine:
         return a.value, b.value
 
     MICROBENCH = {"copy": 0, "gather_thread": 1, "gather_coop": 2, "slot_load": 3, "red_random": 4,
-                  "red_hot": 5}
+                  "red_hot": 5, "h2d_kernel": 6, "h2d_copy": 7}
 
     def microbench(self, kind, n_items, iters=5):
         """Rate of one access pattern alone (see ltpg_microbench in include/ltpg.h)."""

@@ -6,6 +6,7 @@
 // pattern alone over buffers as large as the real ones, so the measured rate
 // is the practical roofline of that pattern (a streaming copy is included as
 // the HBM reference).  Buffers are allocated per call.
+#include <cstring>
 #include <vector>
 
 #include "devutil.cuh"
@@ -90,6 +91,13 @@ __global__ void mb_slot_load(const RegSlot *__restrict__ slots, uint64_t n_slots
     if (acc == 0x1234567ull) *sink = acc;
 }
 
+// Host-to-device transfer by a kernel: 16-byte loads straight from pinned host
+// memory (addressable by the GPU), stores to device memory.
+__global__ void mb_h2d_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 __global__ void mb_red_random(RegSlot *slots, uint64_t n_slots, uint64_t n_ops) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_ops; i += (uint64_t)gridDim.x * blockDim.x)
         red_min(&slots[mb_hash(i, 3) % n_slots].r, 0xFFFFFFFF00000000ull | (i & 0xFFFFFFFFull));
@@ -111,6 +119,13 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
     void *buf_a = nullptr, *buf_b = nullptr;
     unsigned long long *sink = nullptr;
     size_t bytes_a = 0, bytes_b = 0;
+    void *host = nullptr;
+    if (kind == 6 || kind == 7) {  // host-to-device: pinned host source, device destination
+        if (cudaMallocHost(&host, n_items * 16) != cudaSuccess) return LTPG_ERR_NOMEM;
+        memset(host, 0x5A, n_items * 16);
+        bytes_b = n_items * 16;
+        bytes_a = 16;
+    }
     if (kind == 0) bytes_a = bytes_b = n_items * 16;
     else if (kind == 1 || kind == 2) bytes_a = n_rows * 80;
     else bytes_a = n_slots * sizeof(RegSlot);
@@ -153,6 +168,8 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
                 else mb_slot_load<8><<<grid, block, 0, c->stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
                 break;
             case 4: mb_red_random<<<grid, block, 0, c->stream>>>((RegSlot *)buf_a, n_slots, n_items); break;
+            case 6: mb_h2d_kernel<<<grid, block, 0, c->stream>>>((const uint4 *)host, (uint4 *)buf_b, n_items); break;
+            case 7: cudaMemcpyAsync(buf_b, host, n_items * 16, cudaMemcpyHostToDevice, c->stream); break;
             default: mb_red_hot<<<grid, block, 0, c->stream>>>((RegSlot *)buf_a, n_items); break;
             }
         };
@@ -171,10 +188,15 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
     cudaFree(buf_a);
     cudaFree(buf_b);
     cudaFree(sink);
+    if (host) cudaFreeHost(host);
     if (e != cudaSuccess) return LTPG_ERR_CUDA;
     const double secs = ms / 1e3 / iters;
-    // kind 0: bytes moved (read + write); 1, 2: useful row bytes; 3: slot loads; 4, 5: atomics
-    const double units = kind == 0 ? 32.0 * n_items : (kind == 1 || kind == 2) ? 80.0 * n_items : (double)n_items;
+    // kind 0: bytes moved (read + write); 1, 2: useful row bytes; 3: slot loads; 4, 5: atomics;
+    // 6, 7: bytes moved host to device (kernel, copy engine)
+    const double units = kind == 0 ? 32.0 * n_items
+                         : (kind == 1 || kind == 2) ? 80.0 * n_items
+                         : (kind == 6 || kind == 7) ? 16.0 * n_items
+                                                    : (double)n_items;
     *rate = units / secs;
     return LTPG_OK;
 }

@@ -83,15 +83,15 @@ def _no(w, d, c_id, o_id, ol_id, items, line_off):
 
 @pytest.mark.parametrize("mode", MODES)
 def test_tpcc_repeated_items_and_line_counts(eng, mode):
-    """NewOrders listing one item twice (both stock updates apply, in line
-    order), and of 1 and 15 lines; a second NewOrder on a shared stock row."""
+    """NewOrders listing one item twice (both stock updates apply, as in line
+    order), of 0, 1 and 15 lines, and NewOrders sharing stock rows."""
     W = 2
     eng.load_tpcc(5, W)
     o = oracle.TpccOracle(5, W)
     txns, lines = [], []
     rng = np.random.default_rng(9)
     for t in range(400):
-        cnt = [1, 15, 5, 3][t % 4]
+        cnt = [1, 15, 5, 3, 0][t % 5]
         items = [int(rng.integers(0, 40)) for _ in range(cnt)]  # 40 items: repeats within and across orders
         txns.append(_no(t % W, t % 10, t % 3000, t % 30000, (15 * t) % 450000, items, len(lines)))
         for it in items:
