@@ -53,6 +53,10 @@ WORKLOADS = {
                           "1,048,576 txn per batch"),
     "tpcc_prof": dict(kind="tpcc", warehouses=16, n_txn=1 << 18, n_batches=4,
                       name="TPC-C NewOrder+Payment 50/50, profiling size: W=16, 262,144 txn per batch"),
+    "tpcc_mix_prof": dict(kind="tpcc", warehouses=16, n_txn=1 << 18, n_batches=4,
+                          mix=dict(neworder_pct=45, orderstatus_pct=4, delivery_pct=4, stocklevel_pct=4,
+                                   by_name_pct=60),
+                          name="TPC-C five-transaction mix, profiling size: W=16, 262,144 txn per batch"),
 }
 SEED = 20261203
 

@@ -128,7 +128,7 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
     }
     if (kind == 0) bytes_a = bytes_b = n_items * 16;
     else if (kind == 1 || kind == 2) bytes_a = n_rows * 80;
-    else bytes_a = n_slots * sizeof(RegSlot);
+    else if (kind != 6 && kind != 7) bytes_a = n_slots * sizeof(RegSlot);
     cudaError_t e = cudaMalloc(&buf_a, bytes_a);
     if (e == cudaSuccess && bytes_b) e = cudaMalloc(&buf_b, bytes_b);
     if (e == cudaSuccess) e = cudaMalloc(&sink, 8);
