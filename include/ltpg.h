@@ -367,10 +367,11 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
 /* ---- tuning ----------------------------------------------------------------
  * Launch shape of the tuned kernels of one workload; the autotuner writes it.
  * None of these settings can change a commit decision or the table image.
- * Defaults: 256 threads, 1 op per thread, occupancy, 4 ways, filter 1,
- * dedupe 0. */
+ * Defaults: 256 threads (TPC-C 128), 1 op per thread, occupancy, 4 ways,
+ * filter 1, dedupe 0. */
 typedef struct {
-    uint32_t block_threads;   /* threads per block, multiple of 32, <= 512      */
+    uint32_t block_threads;   /* threads per block, multiple of 32, <= 512 (YCSB;
+                                 the tuned TPC-C kernels use 128)               */
     uint32_t ops_per_thread;  /* YCSB op words per thread: 1, 2, 4 or 8         */
     uint32_t blocks_per_sm;   /* cap on resident blocks per SM, 0 = occupancy   */
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */

@@ -153,6 +153,7 @@ int ltpg_create(const ltpg_config *cfg, ltpg_ctx **out) {
     }
     c->stream = c->own_stream;
     c->slots.resize(cfg->n_slots);
+    c->launch_c.block = 128;  // the tuned TPC-C kernels' fixed block (64-transaction tiles)
     *out = c;
     return LTPG_OK;
 }

@@ -217,8 +217,10 @@ __device__ __forceinline__ bool resolve_by_name(const TpccDev &db, ltpg_tpcc_txn
 }
 
 constexpr uint32_t PT = 64;    // transactions per tile (plain path)
-constexpr uint32_t PTT = 128;  // transactions per tile (tuned path)
-constexpr uint32_t PBS = 256;  // threads per block
+constexpr uint32_t PTT = 64;   // transactions per tile (tuned path)
+constexpr uint32_t PBS = 256;  // threads per block (plain path)
+constexpr uint32_t TBS = 128;  // threads per block (tuned path): 64-transaction tiles, so a
+                               // tile's barriers hold 4 warps, not 8
 
 template <uint32_t N>
 struct TileHdrN {
@@ -862,12 +864,12 @@ __device__ __forceinline__ void hot_flush(const TpccDev &db, const long long *ho
     }
 }
 
-__global__ void __launch_bounds__(PBS) tpcc_exec_tuned(TpccTunedArgs a) {
+__global__ void __launch_bounds__(TBS) tpcc_exec_tuned(TpccTunedArgs a) {
     __shared__ TileHdrT h;
     tpcc_exec_tiles(a, h, slot_tag(a.ctl->epoch));
 }
 
-__global__ void __launch_bounds__(PBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
+__global__ void __launch_bounds__(TBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
     __shared__ TileHdrT h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
@@ -877,7 +879,7 @@ __global__ void __launch_bounds__(PBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
     finish_batch(a.ctl);
 }
 
-__global__ void __launch_bounds__(PBS) tpcc_persistent(TpccTunedArgs a) {
+__global__ void __launch_bounds__(TBS) tpcc_persistent(TpccTunedArgs a) {
     __shared__ TileHdrT h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
@@ -912,7 +914,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mode == LTPG_MODE_PERSISTENT
                                                                   ? (const void *)tpcc_persistent
                                                                   : (const void *)tpcc_checkwb_tuned,
-                                                      PBS, smem);
+                                                      TBS, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     if (c->launch_c.blocks_per_sm && (int)c->launch_c.blocks_per_sm < per_sm) per_sm = (int)c->launch_c.blocks_per_sm;
@@ -922,7 +924,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         prof_mark(c, 0);
         void *args[] = {&a};
         count_launch(c);
-        e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent, dim3(grid), dim3(PBS), args, smem, c->stream);
+        e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent, dim3(grid), dim3(TBS), args, smem, c->stream);
         if (e != cudaSuccess) return e;
         prof_mark(c, 1);
         prof_mark(c, 2);
@@ -931,11 +933,11 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     }
     prof_mark(c, 0);
     count_launch(c);
-    tpcc_exec_tuned<<<grid, PBS, 0, c->stream>>>(a);
+    tpcc_exec_tuned<<<grid, TBS, 0, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 1);
     count_launch(c);
-    tpcc_checkwb_tuned<<<grid, PBS, smem, c->stream>>>(a);
+    tpcc_checkwb_tuned<<<grid, TBS, smem, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 2);
     prof_mark(c, 3);

@@ -57,8 +57,9 @@ def candidates(workload, staging=False):
         grid = itertools.product([1, 2, 4], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
         return [dict(block_threads=256, ops_per_thread=o, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w)
                 for o, b, f, d, w in grid]
-    return [dict(block_threads=256, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4)
-            for b, f, d in itertools.product([0, 2, 4, 6], [0, 1], [0, 1])]
+    # TPC-C: 128-thread blocks (fixed), up to 16 resident per SM
+    return [dict(block_threads=128, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4)
+            for b, f, d in itertools.product([0, 4, 8, 12], [0, 1], [0, 1])]
 
 
 def _time_batches(eng, slots, reps, mode, torch):
