@@ -41,6 +41,14 @@ __device__ __forceinline__ uint4 ld_nc_u4(const void *p) {
 __device__ __forceinline__ void red_min(unsigned long long *p, unsigned long long v) {
     asm volatile("red.global.min.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// The same reduction without the compiler memory barrier, for the execute
+// phases: it stays ordered with other volatile asm (the slot filter's load)
+// and with barriers, but the compiler may move independent loads (rows, order
+// lines, prices) across it, so they are in flight together.  Nothing in the
+// execute phase reads back a slot it reduces into.
+__device__ __forceinline__ void red_min_exec(unsigned long long *p, unsigned long long v) {
+    asm volatile("red.global.min.u64 [%0], %1;" ::"l"(p), "l"(v));
+}
 __device__ __forceinline__ void red_add_u64(unsigned long long *p, unsigned long long v) {
     asm volatile("red.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }

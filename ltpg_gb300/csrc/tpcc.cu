@@ -644,7 +644,7 @@ __device__ __forceinline__ void tuned_register(const TpccTunedArgs &a, bool vali
     if (!leader) return;
     RegSlot *s = a.reg + slot_idx;
     unsigned long long *p = is_w ? &s->w : &s->r;
-    if (!filter || ld_ca_u64t(p) > mine) red_min(p, mine);
+    if (!filter || ld_ca_u64t(p) > mine) red_min_exec(p, mine);
 }
 
 // Order line e of a tile whose line prefix is h.off: owner transaction and

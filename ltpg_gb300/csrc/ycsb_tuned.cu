@@ -425,7 +425,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             atomicAdd(&e->cnt, (uint32_t)__popc(peers));
         }
         const unsigned long long mine = tag | t;
-        if (need_global && (kDedupe ? leader : true) && cur > mine) red_min(slot, mine);
+        if (need_global && (kDedupe ? leader : true) && cur > mine) red_min_exec(slot, mine);
         // fold the five chunks of each row onto its group's first lane (5g),
         // then hand the row's xor to the lane that owns the op
         const uint32_t my_rank = __popc(need & lanes_below);
