@@ -7,7 +7,9 @@ reference: its sources are compiled where they lie.
 
   * <prog>.cubin  — the reference program compiled for sm_103a with
                     `nvcc -cubin` (device code only; its host main is ignored).
-                    YCSB/1/ycsb.cu and TPCC-allopt-final/tp.cu, as shipped.
+                    YCSB/1/ycsb.cu and TPCC-allopt-final/tp.cu, as shipped;
+                    tf50: tp.cu with NEWORDER_PERCENT = 50 (compiled from a
+                    temporary copy outside the repository).
   * <prog>_layout.json — sizes and field offsets of the reference's buffer
                     structs and its launch constants, printed by a small host
                     program of ours that includes the reference's Predefine.h /
@@ -16,8 +18,11 @@ reference: its sources are compiled where they lie.
 """
 import json
 import os
+import re
+import shutil
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
@@ -56,6 +61,14 @@ int main() {
   printf("\"grids\": [%u, %u, %u], \"blocks\": [%u, %u, %u],", EXECUTE_GRID_SIZE, CHECK_GRID_SIZE,
          WRITEBACK_GRID_SIZE, EXECUTE_BLOCK_SIZE, CHECK_BLOCK_SIZE, WRITEBACK_BLOCK_SIZE);
   printf("\"neworder_set\": %zu, \"neworder_query\": %zu,", sizeof(NEWORDER_SET), sizeof(NEWORDER_QUERY));
+  printf("\"neworder_counters\": {\"war\": %zu, \"raw\": %zu, \"waw\": %zu},", OFF(NEWORDER_SET, war),
+         OFF(NEWORDER_SET, raw), OFF(NEWORDER_SET, waw));
+  printf("\"neworder_fields\": {\"W_ID\": %zu, \"D_ID\": %zu, \"C_ID\": %zu, \"O_ID\": %zu, \"N_O_ID\": %zu, "
+         "\"O_OL_CNT\": %zu, \"O_OL_ID\": %zu, \"OL_I_ID\": %zu, \"OL_SUPPLY_W_ID\": %zu, \"OL_QUANTITY\": %zu, "
+         "\"TID\": %zu},", OFF(NEWORDER_QUERY, W_ID), OFF(NEWORDER_QUERY, D_ID), OFF(NEWORDER_QUERY, C_ID),
+         OFF(NEWORDER_QUERY, O_ID), OFF(NEWORDER_QUERY, N_O_ID), OFF(NEWORDER_QUERY, O_OL_CNT),
+         OFF(NEWORDER_QUERY, O_OL_ID), OFF(NEWORDER_QUERY, OL_I_ID), OFF(NEWORDER_QUERY, OL_SUPPLY_W_ID),
+         OFF(NEWORDER_QUERY, OL_QUANTITY), OFF(NEWORDER_QUERY, TID));
   printf("\"payment_set\": {\"size\": %zu, \"war\": %zu, \"raw\": %zu, \"waw\": %zu},", sizeof(PAYMENT_SET),
          OFF(PAYMENT_SET, war), OFF(PAYMENT_SET, raw), OFF(PAYMENT_SET, waw));
   printf("\"payment_query\": {\"size\": %zu, \"W_ID\": %zu, \"D_ID\": %zu, \"C_ID\": %zu, \"C_LAST\": %zu, "
@@ -74,6 +87,12 @@ int main() {
               "_Z12KERNEL_CHECKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
               "_Z16KERNEL_WRITEBACKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX"]),
 }
+# The same program with half its batch NewOrders: the shipped sources copied to
+# a temporary directory outside the repository, NEWORDER_PERCENT (a const in
+# Predefine.h, so not settable by -D) changed from 0 to 50, compiled there.
+PROGRAMS["tf50"] = dict(PROGRAMS["tf"], patch=("Predefine.h", r"NEWORDER_PERCENT\s*=\s*\(unsigned int\)0;",
+                                               "NEWORDER_PERCENT =(unsigned int)50;"))
+LAYOUT_VERSION = 2  # neworder_counters / neworder_fields
 
 
 def available():
@@ -87,12 +106,33 @@ def build(force=False):
     os.makedirs(OUT, exist_ok=True)
     for name, p in PROGRAMS.items():
         src_dir = os.path.join(REF, p["dir"])
-        cubin = os.path.join(OUT, f"{name}.cubin")
-        layout = os.path.join(OUT, f"{name}_layout.json")
+        tmp = None
+        if "patch" in p:
+            tmp = tempfile.mkdtemp(prefix="ltpg_ref_")
+            shutil.copytree(src_dir, os.path.join(tmp, "src"))
+            src_dir = os.path.join(tmp, "src")
+            fname, pattern, repl = p["patch"]
+            path = os.path.join(src_dir, fname)
+            text, n = re.subn(pattern, repl, open(path).read())
+            if n != 1:
+                raise RuntimeError(f"{name}: patch of {fname} matched {n} times")
+            open(path, "w").write(text)
+        try:
+            _build_one(name, p, src_dir, force)
+        finally:
+            if tmp:
+                shutil.rmtree(tmp, ignore_errors=True)
+    return True
+
+
+def _build_one(name, p, src_dir, force):
+    cubin = os.path.join(OUT, f"{name}.cubin")
+    layout = os.path.join(OUT, f"{name}_layout.json")
+    if True:
         if force or not os.path.exists(cubin):
             subprocess.run([NVCC, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
                             "-w", "-o", cubin, os.path.join(src_dir, p["main"])], check=True, capture_output=True)
-        stale = os.path.exists(layout) and "cid_kernel" in p and "cid_grid" not in json.load(open(layout))
+        stale = os.path.exists(layout) and json.load(open(layout)).get("layout_version", 1) < LAYOUT_VERSION
         if force or stale or not os.path.exists(layout):
             cpp = os.path.join(OUT, f"{name}_layout.cpp")
             exe = os.path.join(OUT, f"{name}_layout")
@@ -103,13 +143,13 @@ def build(force=False):
             out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
             data = json.loads(out)
             data["kernels"] = p["kernels"]
+            data["layout_version"] = LAYOUT_VERSION
             if "cid_kernel" in p:
                 data["cid_kernel"] = p["cid_kernel"]
             with open(layout, "w") as f:
                 json.dump(data, f, indent=1)
             os.remove(exe)
             os.remove(cpp)
-    return True
 
 
 if __name__ == "__main__":

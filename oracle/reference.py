@@ -8,7 +8,9 @@ oracle/ref_build.py (oracle/_ref/) and runs them through ref_harness.cu:
          for it use keys 1 .. N-1.
   RefTF  LTPG/TPCC-allopt-final as shipped: 65,536 Payments (NEWORDER_PERCENT
          = 0), 64 warehouses (TF/Predefine.h:8-10), customers by id; and its
-         KERNEL_CID by-name lookup (TF/tp.cu:11-23) on its own.
+         KERNEL_CID by-name lookup (TF/tp.cu:11-23) on its own.  RefTF("tf50"):
+         the same sources with NEWORDER_PERCENT = 50 (32,768 NewOrders +
+         32,768 Payments).
 Both return per-transaction flags rebuilt from the reference's conflict
 counters raw / war / waw (the commit flag from its own rule,
 TF/Execute_payment.h:607, Y1/Execute.h:187).
@@ -27,9 +29,9 @@ HARNESS = os.path.join(BUILD, "libref_harness.so")
 _lib = None
 
 
-def available():
-    return all(os.path.exists(os.path.join(REF, f)) for f in ["y1.cubin", "y1_layout.json", "tf.cubin",
-                                                             "tf_layout.json"])
+def available(prog=None):
+    progs = [prog] if prog else ["y1", "tf"]
+    return all(os.path.exists(os.path.join(REF, f"{p}{ext}")) for p in progs for ext in [".cubin", "_layout.json"])
 
 
 def build_harness(force=False):
@@ -157,54 +159,98 @@ class RefY1:
 
 
 class RefTF:
-    def __init__(self):
-        self.L = json.load(open(os.path.join(REF, "tf_layout.json")))
-        self.B = self.L["payment_cnt"]
+    """LTPG/TPCC-allopt-final's three kernels: prog "tf" as shipped (65,536
+    Payments), or "tf50" (the same sources with NEWORDER_PERCENT = 50:
+    32,768 NewOrders + 32,768 Payments per batch)."""
+
+    def __init__(self, prog="tf"):
+        self.prog = prog
+        self.L = json.load(open(os.path.join(REF, f"{prog}_layout.json")))
+        self.B = self.L["batch"]
         self.W = self.L["warehouses"]
         # 147 / 93 / 67 warp roles per 32 transactions (TF/Predefine.h:38-40)
         self.covered = covered_txns(self.L, [147, 93, 67], self.B)
 
-    def run(self, txns, iters=0):
-        """txns: Payment records (TpccBatch.TXN_DTYPE) of one batch, TID = index.
-        Returns the flags (and, with iters > 0, the mean milliseconds of the
-        three kernels over `iters` batches, each after the per-batch clears)."""
-        L, B = self.L, self.B
+    def run(self, txns, lines=None, iters=0):
+        """txns: one batch of NewOrder / Payment records (TpccBatch.TXN_DTYPE),
+        TID = index, with exactly the compiled NEWORDER_CNT NewOrders and
+        PAYMENT_CNT Payments; lines: the batch's order lines.  Returns the
+        flags (and, with iters > 0, the mean milliseconds of the three kernels
+        over `iters` batches, each after the per-batch clears)."""
+        L = self.L
+        NC, PC = L["neworder_cnt"], L["payment_cnt"]
         ps, pq, lg = L["payment_set"], L["payment_query"], L["log"]
-        assert len(txns) == B
+        kind = txns["kind_info"] & 0xFF
+        no_idx, pay_idx = np.nonzero(kind == 0)[0], np.nonzero(kind == 1)[0]
+        assert len(no_idx) == NC and len(pay_idx) == PC and len(txns) == NC + PC
         query = np.zeros(pq["size"], dtype=np.uint8)
         qv = query.view(np.uint32)
 
         def put(field, values):
-            qv[pq[field] // 4:pq[field] // 4 + B] = np.asarray(values, dtype=np.uint32)
+            qv[pq[field] // 4:pq[field] // 4 + PC] = np.asarray(values, dtype=np.uint32)
 
-        ki = txns["kind_info"]
-        put("W_ID", txns["w"])
+        x = txns[pay_idx]
+        ki = x["kind_info"]
+        put("W_ID", x["w"])
         put("D_ID", (ki >> 16) & 0xFF)
-        put("C_ID", txns["c_id"])
-        put("C_LAST", np.zeros(B))
-        put("isName", np.zeros(B))
+        put("C_ID", x["c_id"])
+        put("C_LAST", np.zeros(PC))
+        put("isName", np.zeros(PC))
         put("C_D_ID", ki >> 24)
-        put("C_W_ID", txns["c_w"])
-        put("H_AMOUNT", txns["b"])
-        put("H_ID", txns["a"])
-        put("TID", np.arange(B))
+        put("C_W_ID", x["c_w"])
+        put("H_AMOUNT", x["b"])
+        put("H_ID", x["a"])
+        put("TID", pay_idx)
         pset = np.zeros(ps["size"], dtype=np.uint8)
         nset = np.zeros(max(16, L["neworder_set"]), dtype=np.uint8)
         nquery = np.zeros(max(16, L["neworder_query"]), dtype=np.uint8)
+        if NC:
+            nf, nv = L["neworder_fields"], nquery.view(np.uint32)
+            y = txns[no_idx]
+            cnt = (y["kind_info"] >> 8) & 0xFF
+
+            def putn(field, values, at=0, n=NC):
+                o = nf[field] // 4 + at
+                nv[o:o + n] = np.asarray(values, dtype=np.uint32)
+
+            putn("W_ID", y["w"])
+            putn("D_ID", (y["kind_info"] >> 16) & 0xFF)
+            putn("C_ID", y["c_id"])
+            putn("O_ID", y["a"])
+            putn("N_O_ID", y["b"])
+            putn("O_OL_CNT", cnt)
+            putn("O_OL_ID", y["c"])
+            putn("TID", no_idx)
+            # line ID of NewOrder j at [NEWORDER_CNT * ID + j] (TF/Execute_neworder.h:177)
+            for i in range(15):
+                has = cnt > i
+                ln = lines[y["line_off"][has] + i]
+                for field, col in [("OL_I_ID", "i_id"), ("OL_SUPPLY_W_ID", "supply_w"), ("OL_QUANTITY", "qty")]:
+                    v = np.zeros(NC, dtype=np.uint32)
+                    v[has] = ln[col]
+                    putn(field, v, at=NC * i)
         log = np.zeros(lg["size"], dtype=np.uint8)
         log[:lg["w_ytd"]] = 0xFF  # clear_LOG (TF/Database.h:78-102)
         snap = np.zeros(L["snapshot"], dtype=np.uint8)
         index = np.zeros(max(16, L["index"]), dtype=np.uint8)
         # argument order of KERNEL_EXECUTE / CHECK / WRITEBACK (TF/tp.cu:24-30)
         resets = [(4, 0, lg["w_ytd"], 0xFF), (1, ps["war"], ps["size"] - ps["war"], 0)]
-        ms = _launch("tf", L, [nset, pset, nquery, query, log, snap, index], [0, 1, 0, 0, 0, 0, 0], resets, iters)
+        if NC:
+            nc = L["neworder_counters"]
+            resets.append((0, nc["war"], L["neworder_set"] - nc["war"], 0))
+        ms = _launch(self.prog, L, [nset, pset, nquery, query, log, snap, index], [1 if NC else 0, 1, 0, 0, 0, 0, 0],
+                     resets, iters)
+        flags = np.zeros(len(txns), dtype=np.uint8)
         sv = pset.view(np.uint32)
-        raw = sv[ps["raw"] // 4:ps["raw"] // 4 + B]
-        war = sv[ps["war"] // 4:ps["war"] // 4 + B]
-        waw = sv[ps["waw"] // 4:ps["waw"] // 4 + B]
+        flags[pay_idx] = _flags(sv[ps["raw"] // 4:ps["raw"] // 4 + PC], sv[ps["war"] // 4:ps["war"] // 4 + PC],
+                                sv[ps["waw"] // 4:ps["waw"] // 4 + PC])
+        if NC:
+            nc, nsv = L["neworder_counters"], nset.view(np.uint32)
+            flags[no_idx] = _flags(nsv[nc["raw"] // 4:nc["raw"] // 4 + NC], nsv[nc["war"] // 4:nc["war"] // 4 + NC],
+                                   nsv[nc["waw"] // 4:nc["waw"] // 4 + NC])
         if iters:
-            return _flags(raw, war, waw), ms
-        return _flags(raw, war, waw)
+            return flags, ms
+        return flags
 
     def cid(self, txns, c_last, c_id):
         """The reference's KERNEL_CID on one batch of Payments: the C_ID it

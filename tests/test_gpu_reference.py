@@ -94,6 +94,58 @@ def test_reference_payment_flags_match(ref):
         eng.close()
 
 
+def _mixed_batch(g, nc, pc):
+    """The first nc NewOrders and pc Payments of the generator's next batch, in
+    their order (TID = position), order lines repacked."""
+    from ltpg_gb300 import TpccBatch
+    b = g.next()
+    kind = b.txns["kind_info"] & 0xFF
+    no, pay = kind == abi.TPCC_NEWORDER, kind == abi.TPCC_PAYMENT
+    sel = (no & (np.cumsum(no) <= nc)) | (pay & (np.cumsum(pay) <= pc))
+    assert no[sel].sum() == nc and pay[sel].sum() == pc
+    x = b.txns[sel].copy()
+    cnt = np.where((x["kind_info"] & 0xFF) == abi.TPCC_NEWORDER, (x["kind_info"] >> 8) & 0xFF, 0).astype(np.int64)
+    new_off = np.cumsum(cnt) - cnt
+    total = int(cnt.sum())
+    src = np.repeat(x["line_off"].astype(np.int64), cnt) + (np.arange(total) - np.repeat(new_off, cnt))
+    lines = b.lines[src]
+    x["line_off"] = new_off.astype(np.uint32)
+    return TpccBatch(x, lines)
+
+
+def test_reference_neworder_flags_match(ref):
+    """NewOrders and Payments together, pinned by the reference's own TF
+    kernels compiled with NEWORDER_PERCENT = 50: per-transaction RAW / WAR /
+    WAW and commit equal the oracle's (default insert mode, which follows the
+    reference's NEW-ORDER registration) and the engine's."""
+    if not reference.available("tf50"):
+        pytest.skip("tf50 not built (oracle/ref_build.py where the reference sources are)")
+    r = reference.RefTF("tf50")
+    nc, pc, W = r.L["neworder_cnt"], r.L["payment_cnt"], r.W
+    assert (nc, pc, W) == (32768, 32768, 64)
+    g = TpccGenerator(13, W, 70000, neworder_pct=50)  # about 35,000 of each kind per batch
+    o = oracle.TpccOracle(13, W)
+    eng = Engine(device=0, n_slots=1, max_txn=nc + pc, max_ops_per_txn=16, max_lines=15 * nc)
+    try:
+        eng.load_tpcc(13, W)
+        for _ in range(2):
+            b = _mixed_batch(g, nc, pc)
+            assert b.txns["c"].max() + 15 < 450000  # ORDER-LINE keys stay inside each warehouse's range
+            ref_flags = r.run(b.txns, b.lines)
+            want = o.run(b)[0]
+            assert r.covered >= max(nc, pc)
+            bad = np.nonzero(ref_flags != want)[0]
+            assert len(bad) == 0, (bad[:10], ref_flags[bad[:5]], want[bad[:5]], b.txns["kind_info"][bad[:5]] & 0xFF)
+            eng.upload(0, b)
+            eng.run_batch(0, "graph")
+            eng.sync()
+            assert np.array_equal(eng.txn_flags(0, b.n_txn), want)
+            no = (b.txns["kind_info"] & 0xFF) == abi.TPCC_NEWORDER
+            assert (want[no] & abi.FLAG_COMMIT).any() and (want[no] & abi.FLAG_WAW).any()
+    finally:
+        eng.close()
+
+
 @pytest.mark.parametrize("data", ["generated", "reference"])
 def test_reference_name_lookup_matches(ref, data):
     """The reference's KERNEL_CID (TF/tp.cu:11-23) on our Payments by last name
