@@ -489,7 +489,26 @@ def ref_shape_batches():
     ops[:, 9] = np.uint32(0x80000000) | keys[:, 9]
     yb = YcsbBatch(ops.ravel(), np.arange(B + 1, dtype=np.uint32), np.arange(B, dtype=np.uint64) + 7, B, 10)
     tb = TpccGenerator(SEED, REF_TF["warehouses"], REF_TF["n_txn"], neworder_pct=0).next()
-    return keys, yb, tb
+    mb = mixed_tpcc_batch(TpccGenerator(SEED, REF_TF["warehouses"], 70000, neworder_pct=50), REF_TF["n_txn"] // 2,
+                          REF_TF["n_txn"] // 2)
+    return keys, yb, tb, mb
+
+
+def mixed_tpcc_batch(g, nc, pc):
+    """The first nc NewOrders and pc Payments of the generator's next batch, in
+    their order (TID = position), order lines repacked: the reference's TF
+    build with NEWORDER_PERCENT = 50 takes exactly that many of each."""
+    from ltpg_gb300 import TpccBatch, abi
+    b = g.next()
+    kind = b.txns["kind_info"] & 0xFF
+    no, pay = kind == abi.TPCC_NEWORDER, kind == abi.TPCC_PAYMENT
+    sel = (no & (np.cumsum(no) <= nc)) | (pay & (np.cumsum(pay) <= pc))
+    x = b.txns[sel].copy()
+    cnt = np.where((x["kind_info"] & 0xFF) == abi.TPCC_NEWORDER, (x["kind_info"] >> 8) & 0xFF, 0).astype(np.int64)
+    new_off = np.cumsum(cnt) - cnt
+    src = np.repeat(x["line_off"].astype(np.int64), cnt) + (np.arange(int(cnt.sum())) - np.repeat(new_off, cnt))
+    x["line_off"] = new_off.astype(np.uint32)
+    return TpccBatch(x, b.lines[src])
 
 
 def reference_gpu(iters):
@@ -499,7 +518,7 @@ def reference_gpu(iters):
     from oracle import reference
     if not reference.available():
         return {"unavailable": "reference cubins not built (oracle/_ref is made where the reference sources are)"}
-    keys, _, tb = ref_shape_batches()
+    keys, _, tb, mb = ref_shape_batches()
     out = {}
     r = reference.RefY1()
     flags, mark, ms = r.run(keys[:, :9], keys[:, 9], iters=iters)
@@ -512,6 +531,13 @@ def reference_gpu(iters):
     commits = int((flags & 8 != 0).sum())
     out["payment_65536"] = {"batch_txn": t.B, "ms_per_batch": sum(ms), "kernel_ms": ms, "commits": commits,
                             "committed_per_s": commits / (sum(ms) * 1e-3), "iters": iters}
+    if reference.available("tf50"):  # the same sources with NEWORDER_PERCENT = 50
+        t = reference.RefTF("tf50")
+        flags, ms = t.run(mb.txns, mb.lines, iters=iters)
+        commits = int((flags & 8 != 0).sum())
+        out["neworder_payment_65536"] = {"batch_txn": t.B, "ms_per_batch": sum(ms), "kernel_ms": ms,
+                                         "commits": commits, "committed_per_s": commits / (sum(ms) * 1e-3),
+                                         "iters": iters}
     return out
 
 
@@ -521,12 +547,14 @@ def engine_on_ref_shapes(iters):
     import torch
 
     import ltpg_gb300 as L
-    _, yb, tb = ref_shape_batches()
+    _, yb, tb, mb = ref_shape_batches()
     out = {}
     for name, load, b, kw in [("ycsb_10k_x10", lambda e: e.load_ycsb(SEED, REF_Y1["n_records"]), yb,
                                dict(max_ops_per_txn=10)),
                               ("payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), tb,
-                               dict(max_ops_per_txn=16, max_lines=16))]:
+                               dict(max_ops_per_txn=16, max_lines=16)),
+                              ("neworder_payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), mb,
+                               dict(max_ops_per_txn=16, max_lines=max(16, mb.n_lines)))]:
         n_slots = 8
         e = L.Engine(device=0, n_slots=n_slots, max_txn=b.n_txn, **kw)
         try:
