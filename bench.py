@@ -542,8 +542,9 @@ def reference_gpu(iters):
 
 
 def engine_on_ref_shapes(iters):
-    """The engine on the batches reference_gpu() times, plain and graph mode,
-    the same batch in every slot, CUDA events around `iters` batches."""
+    """The engine on the batches reference_gpu() times, in each launch mode
+    (plain, fused, persistent, graph), the same batch in every slot, CUDA
+    events around `iters` batches; `best_mode` names the fastest."""
     import torch
 
     import ltpg_gb300 as L
@@ -562,11 +563,12 @@ def engine_on_ref_shapes(iters):
             for s in range(n_slots):
                 e.upload(s, b)
             res = {}
-            for mode in ["plain", "graph"]:
+            for mode in ["plain", "fused", "persistent", "graph"]:
                 nxt = run_steps(e, n_slots, 16, mode)
                 secs, commits, launches, _ = timed(e, torch, n_slots, iters, mode, nxt, None)
                 res[mode] = {"ms_per_batch": secs * 1e3 / iters, "committed_per_s": commits / secs,
                              "launches_per_batch": launches / iters}
+            res["best_mode"] = min(("plain", "fused", "persistent", "graph"), key=lambda m: res[m]["ms_per_batch"])
             res["commits"] = commits // iters
             res["batch_txn"] = b.n_txn
             out[name] = res
