@@ -78,6 +78,9 @@ def parse():
                     help="steps of the end-to-end leg (host wall clock; long enough to average out host stalls)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-device-gen", action="store_true", help="skip the device-generator section")
+    ap.add_argument("--late-reads", type=int, choices=[0, 1, 2], default=None,
+                    help="YCSB: override the launch setting late_reads (0 rows read at execute, 1 after the check "
+                         "in the check kernel, 2 in a kernel of their own)")
     ap.add_argument("--no-tune", action="store_true",
                     help="the engine's default launch shape, no autotuning (profiling runs)")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
@@ -182,17 +185,28 @@ class Clocks:
 
 
 # ---- byte model (algorithmic bytes, logical, no sector rounding) --------------------
-def ycsb_bytes_per_txn(k, u, commit_rate, scan=1):
+def ycsb_bytes_per_txn(k, u, commit_rate, scan=1, late=False):
     """Per transaction: op words 4k, value offset 4, update values 8uk, registration
     (8-byte slot word read+written) 16 per update and 16 per key a read covers,
     check loads 8 per key a read covers / 16 per update, row reads 80 per key a
     read covers, committed update stores 8 per update of a committed
     transaction, result 8, flags 1+1, bitmap 1/8.  A read covers `scan` keys
-    (1: point reads)."""
-    exec_b = 4 * k + 16 * u * k + (16 + 80) * (1 - u) * k * scan + 8
-    check_b = (4 * k + 4 + 8 * (1 - u) * k * scan + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1
-               + 1 / 8)
-    return exec_b, check_b
+    (1: point reads).  Returns (execute, check + write-back, 0).
+
+    late: execute registers only; check + reads reads the rows of committed
+    transactions' reads (80 per covered key times the commit rate) and writes
+    the result; the write-back kernel reads flags 1 and, for a committed
+    transaction, its value offset 4, op words 4k and update values 8uk, and
+    stores 8uk.  Returns (execute, check + reads, write-back)."""
+    if not late:
+        exec_b = 4 * k + 16 * u * k + (16 + 80) * (1 - u) * k * scan + 8
+        check_b = (4 * k + 4 + 8 * (1 - u) * k * scan + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1
+                   + 1 / 8)
+        return exec_b, check_b, 0.0
+    exec_b = 4 * k + 16 * u * k + 16 * (1 - u) * k * scan
+    check_b = 4 * k + 8 * (1 - u) * k * scan + 16 * u * k + 80 * (1 - u) * k * scan * commit_rate + 8 + 1 + 1 / 8
+    wb_b = 1 + commit_rate * (4 + 4 * k + 16 * u * k)
+    return exec_b, check_b, wb_b
 
 
 def profile_traffic(workload, kernel):
@@ -211,7 +225,7 @@ def profile_traffic(workload, kernel):
 def ycsb_exec_kernel_name(launch, stride):
     """Name of the execute kernel the tuned path launches for this shape."""
     opt = (launch or {}).get("ops_per_thread", 1)
-    if opt == 1 and stride <= 32:
+    if (opt == 1 or (launch or {}).get("late_reads")) and stride <= 32:
         return "ycsb_exec_coop"
     if opt in (2, 4) and stride % opt == 0 and ((stride // opt) & (stride // opt - 1)) == 0:
         return "ycsb_exec_fast"
@@ -270,7 +284,7 @@ def kernel_split(eng, n_slots, mode, start):
     the events that split a batch into its kernels are recorded only here, so
     the timed region carries no instrumentation (on 40-us batches it cost a
     quarter of the time).  Rows: slots; columns: execute, check+write-back,
-    (unused)."""
+    predictor (YCSB late reads: execute, check+reads, write-back)."""
     eng.set_profiling(True)
     run_steps(eng, n_slots, n_slots, mode, start)
     eng.sync()
@@ -345,6 +359,10 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                 cfg, how = tune.apply_cached_or_tune(eng, "ycsb", wkey, list(range(min(8, n_slots))),
                                                      lambda: eng.load_ycsb(SEED, w["n_records"]))
                 res["launch"] = dict(cfg, source=how)
+            if mode != "plain" and args.late_reads is not None:
+                eng.set_launch("ycsb", late_reads=args.late_reads)
+                res["launch"] = dict(res["launch"], late_reads=args.late_reads, source=res["launch"]["source"] +
+                                     " + --late-reads")
             eng.load_ycsb(SEED, w["n_records"])
             eng.sync()
             nxt = run_steps(eng, n_slots, args.warmup, mode)
@@ -377,6 +395,10 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                     eng.run_batch(0, mode if mode != "graph" else "graph")
                     eng.sync()
                     outs.append(eng.commit_bitmap(0, w["n_txn"]))
+                    # results of the committed transactions (with late reads an
+                    # aborted transaction's result is 0 by definition)
+                    com = (eng.txn_flags(0, w["n_txn"]) & L.FLAG_COMMIT) != 0
+                    outs.append(eng.txn_results(0, w["n_txn"])[com])
                 img = eng.download_table(L.TABLE_YCSB)
                 ref[mode] = (outs, int(np.bitwise_xor.reduce(img)), int(img.sum()))
             a, b = ref["plain"], ref[args.mode]
@@ -667,11 +689,21 @@ def main():
     B = w["n_txn"]
     commit_rate = tuned["commits"] / (args.steps * B)
     kt = tuned["kt"]
-    exec_ms, cwb_ms = float(np.mean(kt[:, 0])), float(np.mean(kt[:, 1]))
+    exec_ms, cwb_ms, third_ms = (float(np.mean(kt[:, i])) for i in range(3))
+    late = w["kind"] == "ycsb" and bool((launch or {}).get("late_reads")) and ((w["ops"] + 3) & ~3) <= 32
+    kernel_ms = {"execute": exec_ms, "check_reads": cwb_ms, "write_back": third_ms} if late else \
+        {"execute": exec_ms, "check_writeback": cwb_ms}
+    prof_kernel = None
     if w["kind"] == "ycsb":
-        eb, cb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate, max(1, w.get("scan_len", 0)))
+        eb, cb, wb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate, max(1, w.get("scan_len", 0)),
+                                        late)
         ek = ycsb_exec_kernel_name(launch, (w["ops"] + 3) & ~3)
-        kernel, kbytes, kms = (ek, eb, exec_ms) if exec_ms >= cwb_ms else ("ycsb_checkwb_tuned", cb, cwb_ms)
+        cands = [(ek, eb, exec_ms), ("ycsb_checkwb_tuned", cb, cwb_ms)]
+        if late:
+            cands.append(("ycsb_writeback_late", wb, third_ms))
+        kernel, kbytes, kms = max(cands, key=lambda c: c[2])
+        # the late-read kernels have their own profile summaries
+        prof_kernel = kernel + "_late" if late and kernel != "ycsb_writeback_late" else kernel
     else:
         # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
         eb, cb = tpcc_bytes_per_txn(w.get("mix"), commit_rate)
@@ -679,7 +711,7 @@ def main():
             ("tpcc_checkwb_tuned", cb, cwb_ms)
     achieved = kbytes * B / (kms / 1e3) / 1e9 if kms > 0 else None
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = profile_traffic(args.workload, kernel)
+    traffic = profile_traffic(args.workload, prof_kernel or kernel)
     line = {
         "metric": "committed txns/s", "value": value, "unit": "txn/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
@@ -697,7 +729,7 @@ def main():
                      "traffic": traffic * B if traffic else None,
                      "traffic_note": "ncu dram bytes per transaction of a 262,144-transaction capture "
                                      "scaled to the batch" if traffic else None,
-                     "kernel_ms": {"execute": exec_ms, "check_writeback": cwb_ms},
+                     "kernel_ms": kernel_ms,
                      "pattern_ceilings": ceilings},
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],

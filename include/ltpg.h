@@ -368,7 +368,13 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
  * Launch shape of the tuned kernels of one workload; the autotuner writes it.
  * None of these settings can change a commit decision or the table image.
  * Defaults: 256 threads (TPC-C 128), 1 op per thread, occupancy, 4 ways,
- * filter 1, dedupe 0. */
+ * filter 1, dedupe 0, late_reads 0.
+ * late_reads (YCSB, strides <= 32): the execute kernel only registers; the
+ * check kernel reads the rows of committed transactions once their commit
+ * decision is made, and a third kernel stores the updates.  Commit decisions,
+ * the table image and the results of committed transactions are unchanged;
+ * an aborted transaction's result is 0 (its reads are void: it runs again in
+ * a later batch).  It saves the row reads of aborted transactions. */
 typedef struct {
     uint32_t block_threads;   /* threads per block, multiple of 32, <= 512 (YCSB;
                                  the tuned TPC-C kernels use 128)               */
@@ -377,6 +383,8 @@ typedef struct {
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
     uint32_t filter;          /* 1 = read the slot before its atomicMin         */
     uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any; TPC-C: header ops) */
+    uint32_t late_reads;      /* YCSB: 1 = rows read after the check, in the check
+                                 kernel; 2 = in a kernel of their own (see above) */
 } ltpg_launch;
 int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
 int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);
@@ -477,7 +485,9 @@ int ltpg_counters(ltpg_ctx *ctx, uint64_t *commits_total, uint64_t *kernel_launc
 /* When on, every batch run records CUDA events around each of its kernels
  * (also inside captured graphs); ltpg_kernel_times returns the durations in
  * milliseconds of the last run of a slot: [execute, check, write-back] for the
- * plain mode, [execute, check+write-back, 0] for the tuned modes. */
+ * plain mode, [execute, check+write-back, predictor] for the tuned modes
+ * ([execute, check+reads, write-back+predictor] with YCSB late reads; the
+ * predictor's share is 0 when it is off). */
 int ltpg_set_profiling(ltpg_ctx *ctx, int on);
 int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms3);
 

@@ -402,7 +402,9 @@ class Engine:
 
     def set_launch(self, workload, **kw):
         """Sets fields of the tuned launch shape (block_threads, ops_per_thread,
-        blocks_per_sm, stage_ways, filter, dedupe) of workload 'ycsb' or 'tpcc'."""
+        blocks_per_sm, stage_ways, filter, dedupe, late_reads) of workload
+        'ycsb' or 'tpcc'.  late_reads = 1: YCSB rows are read after the check,
+        by committed transactions only (an aborted transaction's result is 0)."""
         wl = abi.WORKLOAD_YCSB if workload == "ycsb" else abi.WORKLOAD_TPCC
         cur = abi.LaunchC()
         self._ck(lib().ltpg_get_launch(self._h, wl, C.byref(cur)))

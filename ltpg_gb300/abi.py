@@ -56,7 +56,8 @@ class ConfigC(C.Structure):
 
 class LaunchC(C.Structure):
     _fields_ = [("block_threads", C.c_uint32), ("ops_per_thread", C.c_uint32), ("blocks_per_sm", C.c_uint32),
-                ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("dedupe", C.c_uint32)]
+                ("stage_ways", C.c_uint32), ("filter", C.c_uint32), ("dedupe", C.c_uint32),
+                ("late_reads", C.c_uint32)]
 
 
 class PredictorC(C.Structure):

@@ -720,6 +720,7 @@ int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
     const uint32_t opt = cfg->ops_per_thread;
     if (opt != 1 && opt != 2 && opt != 4 && opt != 8) return fail(c, LTPG_ERR_INVALID, "ops_per_thread in {1, 2, 4, 8}");
     if (cfg->stage_ways < 1 || cfg->stage_ways > 8) return fail(c, LTPG_ERR_INVALID, "stage_ways in [1, 8]");
+    if (cfg->late_reads > 2) return fail(c, LTPG_ERR_INVALID, "late_reads in {0, 1, 2}");
     LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
     l.block = cfg->block_threads;
     l.per_thread = cfg->ops_per_thread;
@@ -727,6 +728,7 @@ int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
     l.ways = cfg->stage_ways;
     l.filter = cfg->filter ? 1u : 0u;
     l.dedupe = cfg->dedupe ? 1u : 0u;
+    l.late_reads = cfg->late_reads;
     drop_graphs(c);
     return LTPG_OK;
 }
@@ -742,6 +744,7 @@ int ltpg_get_launch(ltpg_ctx *c, int workload, ltpg_launch *cfg) {
     cfg->stage_ways = l.ways;
     cfg->filter = l.filter;
     cfg->dedupe = l.dedupe;
+    cfg->late_reads = l.late_reads;
     return LTPG_OK;
 }
 

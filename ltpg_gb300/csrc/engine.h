@@ -98,6 +98,7 @@ struct LaunchCfg {
     uint32_t ways = 4;           // shared-memory staging entries per hot bucket
     uint32_t filter = 1;         // read the slot before its atomicMin
     uint32_t dedupe = 0;         // one atomic per key per warp (measured slower on GB300 for both workloads)
+    uint32_t late_reads = 0;     // YCSB: rows read after the check, by committed transactions only
 };
 
 }  // namespace ltpg

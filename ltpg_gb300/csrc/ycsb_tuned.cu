@@ -13,7 +13,11 @@
 //     observed, stale or not, is >= the current one: the skip is exact;
 //   * check and write-back run in one kernel: the commit decision of a tile is
 //     made in shared memory, then each committed transaction's thread stores
-//     its updates in op order.
+//     its updates in op order;
+//   * late reads (a launch setting): execute only registers, the check kernel
+//     reads the rows of the committed transactions after the tile's commit
+//     decision, and a third kernel stores the updates, so that no aborted
+//     transaction's rows are read.
 #include "stage.cuh"
 
 namespace ltpg {
@@ -38,6 +42,7 @@ struct YcsbTunedArgs {
     uint32_t ways, stage_entries;
     uint32_t filter;
     uint32_t lpt;  // lanes per transaction of the one-op-per-lane kernels: stride rounded up to a power of two (0: > 32)
+    uint32_t late; // late reads: 0 off, 1 in the check kernel, 2 in a kernel of their own
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
@@ -124,8 +129,146 @@ __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long
     (void)counted;
 }
 
+// Stores the updates of committed transaction t in op order: a transaction
+// that updates a field twice leaves its later value (as a sequential replay
+// does), and no two committed transactions write one row (WAW).
+__device__ __forceinline__ void write_txn_updates(const YcsbTunedArgs &a, uint32_t t) {
+    uint32_t v = a.val_off[t];
+    if (v == a.val_off[t + 1]) return;
+    const uint4 *tw = reinterpret_cast<const uint4 *>(a.ops + (uint64_t)t * a.stride);
+    for (uint32_t q4 = 0; q4 < a.stride / 4u; ++q4) {
+        const uint4 w4 = ld_nc_u4(tw + q4);
+        const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t x = words[q];
+            if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
+            const uint32_t key = ycsb_key(x), fld = ycsb_field(x);
+            if (key < a.n && fld < LTPG_YCSB_FIELDS) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = a.vals[v];
+            ++v;
+        }
+    }
+}
+
+// Late reads of one tile whose commit flags are in fl: the lpt lanes of a
+// transaction (a power of two, aligned in the warp) take one op each; the
+// point reads of committed transactions are gathered five lanes to a row (one
+// 16-byte chunk each, six rows per round), a range scan by the whole warp over
+// its contiguous rows.  results[t] = sum over reads of xor(row) * (2j + 1), as
+// at execute; 0 for an aborted transaction.  No row is written before the
+// next kernel, so every read sees the batch-start image.
+// Per-warp shared scratch of the late reads: the keys of the warp's point
+// reads by rank, and the xor of each one's row.
+struct LateScratch {
+    uint32_t key[32];
+    unsigned long long x[32];
+};
+
+// One step of the lanes of a warp (all 32 call it): lane j of transaction t
+// (own: the lane holds an op slot of a transaction; com: t committed).
+__device__ __forceinline__ void late_read_step(const YcsbTunedArgs &a, LateScratch *ws, uint32_t t, uint32_t j,
+                                               bool own, bool com) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lpt = a.lpt;
+    const uint32_t grp = lane / 5, chunk = lane % 5;
+    {
+        const uint32_t w = com && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
+        const uint32_t key = ycsb_key(w);
+        const bool rd = !ycsb_is_pad(w) && !ycsb_is_update(w) && key < a.n;
+        const bool scan = rd && ycsb_span(w) != 0u;
+        const unsigned need = __ballot_sync(FULL, rd && !scan);
+        const uint32_t n_need = __popc(need);
+        unsigned long long x = 0;
+        if (n_need) {  // warp-uniform
+            // round r: lane group g (five lanes, one 16-byte chunk each) reads
+            // the row of the (6r + g)-th point read; its first lane folds the
+            // chunks and leaves the row's xor under that rank
+            const uint32_t my_rank = __popc(need & ((1u << lane) - 1u));
+            const bool mine = (need >> lane) & 1u;
+            if (mine) ws->key[my_rank] = key;
+            __syncwarp();
+            ulonglong2 ch[6];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                const uint32_t idx = (uint32_t)r * 6u + grp;
+                const bool go = grp < 6 && idx < n_need;
+                const uint32_t k_src = go ? ws->key[idx] : 0u;
+                ch[r] = go ? ld_nc16_issue(reinterpret_cast<const char *>(a.rows + (uint64_t)k_src * LTPG_YCSB_FIELDS) +
+                                           16u * chunk)
+                           : make_ulonglong2(0ull, 0ull);
+            }
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                if ((uint32_t)r * 6u >= n_need) break;  // warp-uniform
+                const unsigned long long c0 = ch[r].x ^ ch[r].y;
+                unsigned long long c = c0 ^ __shfl_down_sync(FULL, c0, 1);
+                c ^= __shfl_down_sync(FULL, c, 2);
+                const unsigned long long rowx = c ^ __shfl_down_sync(FULL, c0, 4);
+                const uint32_t idx = (uint32_t)r * 6u + grp;
+                if (chunk == 0u && grp < 6 && idx < n_need) ws->x[idx] = rowx;
+            }
+            __syncwarp();
+            if (mine) x = ws->x[my_rank];
+            __syncwarp();  // the next step reuses the scratch
+        }
+        const uint32_t last = scan ? (uint32_t)scan_last(w, a.n) : 0u;
+        for (unsigned m = __ballot_sync(FULL, scan); m; m &= m - 1u) {
+            const uint32_t src = (uint32_t)__ffs(m) - 1u;
+            const uint32_t k0 = __shfl_sync(FULL, key, src), k1 = __shfl_sync(FULL, last, src);
+            const uint32_t chunks = (k1 - k0 + 1u) * 5u;
+            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(a.rows + (uint64_t)k0 * LTPG_YCSB_FIELDS);
+            unsigned long long c_all = 0;
+            for (uint32_t c = lane; c < chunks; c += 32u) {
+                const ulonglong2 q = ld_nc16(p + c);
+                c_all ^= q.x ^ q.y;
+            }
+            for (uint32_t o = 16; o >= 1u; o >>= 1) c_all ^= __shfl_xor_sync(FULL, c_all, o);
+            if (lane == src) x = c_all;
+        }
+        unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
+        for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
+        if (own && j == 0u) a.results[t] = (int64_t)part;
+    }
+}
+
+__device__ __forceinline__ void late_read_tile(const YcsbTunedArgs &a, const uint32_t *fl, uint32_t t0,
+                                               uint32_t nt) {
+    __shared__ LateScratch scratch[16];  // blocks of up to 512 threads
+    LateScratch *ws = scratch + (threadIdx.x >> 5);
+    const uint32_t lsh = (uint32_t)__ffs(a.lpt) - 1u;
+    const uint32_t nl = a.tile << lsh;
+    for (uint32_t base = 0; base < nl; base += blockDim.x) {
+        const uint32_t v = base + threadIdx.x;
+        const uint32_t lt = v >> lsh, j = v & (a.lpt - 1u);
+        const bool own = v < nl && lt < nt;
+        late_read_step(a, ws, t0 + lt, j, own, own && (fl[lt] & LTPG_FLAG_COMMIT) != 0u);
+    }
+}
+
+// Late reads as a kernel of their own (late_reads = 2), after the check: the
+// lanes of the whole batch, lpt per transaction, commit flags from global memory.
+__device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
+    __shared__ LateScratch scratch[16];  // blocks of up to 512 threads
+    LateScratch *ws = scratch + (threadIdx.x >> 5);
+    const uint32_t lsh = (uint32_t)__ffs(a.lpt) - 1u;
+    const uint64_t nw = (uint64_t)a.B << lsh;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
+        const uint64_t v = base + threadIdx.x;
+        const bool own = v < nw;
+        const uint32_t t = (uint32_t)(v >> lsh), j = (uint32_t)v & (a.lpt - 1u);
+        late_read_step(a, ws, t, j, own, own && (a.flags[t] & LTPG_FLAG_COMMIT) != 0u);
+    }
+}
+
+__global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop(a); }
+
 // ---- check + write-back over all tiles assigned to this block ------------------
-// fl: tile flags.
+// fl: tile flags.  kLate = 0: the third pass stores the committed updates;
+// 1: it reads the committed transactions' rows (late_read_tile); 2: there is
+// no third pass (the reads have a kernel of their own).  With late reads the
+// updates are stored by a later kernel.
+template <int kLate>
 __device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *fl,
                                               uint32_t epoch) {
     const uint32_t lane = threadIdx.x & 31;
@@ -186,28 +329,13 @@ __device__ __forceinline__ void checkwb_tiles(const YcsbTunedArgs &a, uint32_t *
             }
         }
         __syncthreads();
-        // pass 3: committed updates, one thread per transaction in op order:
-        // a transaction that updates a field twice leaves its later value (as a
-        // sequential replay does), and no two committed transactions write one
-        // row (WAW)
-        for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
-            if (!(fl[i] & LTPG_FLAG_COMMIT)) continue;
-            const uint32_t t = t0 + i;
-            uint32_t v = a.val_off[t];
-            if (v == a.val_off[t + 1]) continue;
-            const uint4 *tw = reinterpret_cast<const uint4 *>(a.ops + (uint64_t)t * a.stride);
-            for (uint32_t q4 = 0; q4 < a.stride / 4u; ++q4) {
-                const uint4 w4 = ld_nc_u4(tw + q4);
-                const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t x = words[q];
-                    if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
-                    const uint32_t key = ycsb_key(x), fld = ycsb_field(x);
-                    if (key < a.n && fld < LTPG_YCSB_FIELDS) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = a.vals[v];
-                    ++v;
-                }
-            }
+        // pass 3: committed updates, one thread per transaction in op order
+        // (or, with late reads, the committed transactions' row reads)
+        if (kLate == 1) {
+            late_read_tile(a, fl, t0, nt);
+        } else if (kLate == 0) {
+            for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x)
+                if (fl[i] & LTPG_FLAG_COMMIT) write_txn_updates(a, t0 + i);
         }
         __syncthreads();
     }
@@ -355,7 +483,9 @@ __global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t 
 // contiguous 16-byte chunk, so a row costs one or two cache-line requests
 // instead of five.  The five chunks are xor-folded within their lane group and
 // handed back to the lane that owns the op.
-template <bool kStage, bool kFilter, bool kDedupe>
+// kReads = false (late reads): registration only; the rows are read after the
+// check, by the committed transactions alone (late_read_tile).
+template <bool kStage, bool kFilter, bool kDedupe, bool kReads>
 __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt *tab, const uint32_t *sbits,
                                                const uint32_t *srank, uint64_t tag) {
     const uint32_t lane = threadIdx.x & 31;
@@ -389,7 +519,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             const uint32_t g = stage_group(sbits, srank, b);
             if (g < groups) e = stage_find(tab, g, a.ways, key);
             if (!e && (t % COUNT_SAMPLE) == 0u) atomicAdd(a.bucket_counts + b, COUNT_SAMPLE);
-            if (e && rd && *reinterpret_cast<volatile uint32_t *>(&e->dig_ok)) {
+            if (kReads && e && rd && *reinterpret_cast<volatile uint32_t *>(&e->dig_ok)) {
                 __threadfence_block();
                 x = *reinterpret_cast<volatile unsigned long long *>(&e->dig);
                 have_dig = true;
@@ -401,13 +531,13 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
         const uint32_t leader_lane = (uint32_t)__ffs(peers) - 1u;
         const bool leader = valid && leader_lane == lane;
         // rows still to read, compacted: round r reads the (6r + g)-th of them
-        const unsigned need = __ballot_sync(FULL, rd && !have_dig && leader);
+        const unsigned need = kReads ? __ballot_sync(FULL, rd && !have_dig && leader) : 0u;
         const uint32_t n_need = __popc(need);
         ulonglong2 ch[6];
 #pragma unroll
         for (int r = 0; r < 6; ++r) {
             const uint32_t idx = (uint32_t)r * 6u + grp;
-            const bool go = grp < 6 && idx < n_need;
+            const bool go = kReads && grp < 6 && idx < n_need;
             const uint32_t src = go ? __fns(need, 0, (int)idx + 1) : 0u;
             const uint32_t k_src = __shfl_sync(FULL, key, src & 31u);
             ch[r] = go ? ld_nc16_issue(reinterpret_cast<const char *>(a.rows + (uint64_t)k_src * LTPG_YCSB_FIELDS) +
@@ -426,6 +556,8 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
         }
         const unsigned long long mine = tag | t;
         if (need_global && (kDedupe ? leader : true) && cur > mine) red_min_exec(slot, mine);
+        scans |= rd && ycsb_span(w) != 0u;
+        if (!kReads) continue;
         // fold the five chunks of each row onto its group's first lane (5g),
         // then hand the row's xor to the lane that owns the op
         const uint32_t my_rank = __popc(need & lanes_below);
@@ -449,7 +581,6 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
             __threadfence_block();
             *reinterpret_cast<volatile uint32_t *>(&e->dig_ok) = 1u;
         }
-        scans |= rd && ycsb_span(w) != 0u;
         unsigned long long part = rd ? x * (2ull * j + 1ull) : 0ull;
         for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
         if (act && j == 0u) a.results[t] = (int64_t)part;
@@ -477,7 +608,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
                 const uint32_t src = (uint32_t)__ffs(m) - 1u;
                 const uint32_t k0 = __shfl_sync(FULL, key, src), k1 = __shfl_sync(FULL, last, src);
                 const uint32_t ts = __shfl_sync(FULL, t, src);
-                const uint32_t chunks = (k1 - k0 + 1u) * 5u;
+                const uint32_t chunks = kReads ? (k1 - k0 + 1u) * 5u : 0u;
                 const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(a.rows + (uint64_t)k0 * LTPG_YCSB_FIELDS);
                 unsigned long long c_all = 0, c_first = 0;
                 for (uint32_t c = lane; c < chunks; c += 32u) {
@@ -490,6 +621,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
                     const unsigned long long mine = tag | ts;
                     if (!kFilter || ld_ca_u64(slot) > mine) red_min(slot, mine);
                 }
+                if (!kReads) continue;
                 for (uint32_t o = 16; o >= 1u; o >>= 1) {
                     c_all ^= __shfl_xor_sync(FULL, c_all, o);
                     c_first ^= __shfl_xor_sync(FULL, c_first, o);
@@ -499,6 +631,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
                     xf = c_first;
                 }
             }
+            if (!kReads) continue;
             // the first pass added x_first * (2j + 1); the read's term is
             // x_all * (2j + 1): add the difference (mod 2^64)
             unsigned long long part = rd ? (xa - xf) * (2ull * j + 1ull) : 0ull;
@@ -508,7 +641,7 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
     }
 }
 
-template <bool kStage, bool kFilter, bool kDedupe>
+template <bool kStage, bool kFilter, bool kDedupe, bool kReads>
 __global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     uint32_t *sbits = reinterpret_cast<uint32_t *>(smem);
@@ -523,7 +656,7 @@ __global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
         stage_init(tab, a.stage_entries);
         __syncthreads();
     }
-    coop_exec_loop<kStage, kFilter, kDedupe>(a, tab, sbits, srank, tag);
+    coop_exec_loop<kStage, kFilter, kDedupe, kReads>(a, tab, sbits, srank, tag);
     if (kStage) {
         __syncthreads();
         const uint32_t ops = stage_flush(tab, a.stage_entries, a.reg, tag, a.bucket_counts);
@@ -571,16 +704,31 @@ __global__ void __launch_bounds__(512) ycsb_exec_tuned(YcsbTunedArgs a) {
     }
 }
 
+template <int kLate>
 __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     const SmemPtrs p = carve(smem, a.tile);
-    checkwb_tiles(a, p.fl, a.ctl->epoch);
+    checkwb_tiles<kLate>(a, p.fl, a.ctl->epoch);
+    if (!kLate) finish_batch(a.ctl);
+}
+
+// Write-back after late reads: one thread per committed transaction.
+__device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < a.B; t += step)
+        if (a.flags[t] & LTPG_FLAG_COMMIT) write_txn_updates(a, t);
+}
+
+__global__ void __launch_bounds__(256) ycsb_writeback_late(YcsbTunedArgs a) {
+    writeback_late_loop(a);
     finish_batch(a.ctl);
 }
 
 // One cooperative kernel per batch: execute+register, grid barrier, check +
 // write-back.  The barrier wait is bounded (2 s).
-template <bool kStage>
+// With late reads (kLate, which needs a.lpt != 0): execute registers only,
+// then check + reads, a second grid barrier, and the write-back.
+template <bool kStage, bool kLate>
 __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     const SmemPtrs p = carve(smem, a.tile);
@@ -591,9 +739,9 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         __syncthreads();
     }
     if (a.lpt) {
-        if (a.filter) coop_exec_loop<kStage, true, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
-        else coop_exec_loop<kStage, false, true>(a, p.tab, a.stage_bits, a.stage_rank, tag);
-    } else {
+        if (a.filter) coop_exec_loop<kStage, true, true, !kLate>(a, p.tab, a.stage_bits, a.stage_rank, tag);
+        else coop_exec_loop<kStage, false, true, !kLate>(a, p.tab, a.stage_bits, a.stage_rank, tag);
+    } else if (!kLate) {
         exec_tiles<kStage>(a, p.dig, p.tab, tag);
     }
     if (kStage) {
@@ -601,7 +749,20 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         const uint32_t ops = stage_flush(p.tab, a.stage_entries, a.reg, tag, a.bucket_counts);
         if (ops) red_add_u64(&a.st->staged_ops, ops);
     }
-    if (grid_barrier(a.ctl, 2000000000ull)) checkwb_tiles(a, p.fl, epoch);
+    bool ok = grid_barrier(a.ctl, 2000000000ull);
+    if (ok) {
+        if (!kLate) checkwb_tiles<0>(a, p.fl, epoch);
+        else if (a.late == 2u) checkwb_tiles<2>(a, p.fl, epoch);
+        else checkwb_tiles<1>(a, p.fl, epoch);
+    }
+    if (kLate) {
+        if (a.late == 2u) {
+            ok = grid_barrier(a.ctl, 2000000000ull) && ok;
+            if (ok) late_read_loop(a);
+        }
+        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
+        if (ok) writeback_late_loop(a);
+    }
     finish_batch(a.ctl);
 }
 
@@ -641,21 +802,26 @@ static void launch_fast_t(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, uint3
     k<<<grid, 256, smem, c->stream>>>(a, lpt);
 }
 
-static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
+template <bool kReads>
+static void (*coop_kernel(int sel))(YcsbTunedArgs) {
+    switch (sel) {
+    case 0: return ycsb_exec_coop<false, false, false, kReads>;
+    case 1: return ycsb_exec_coop<false, false, true, kReads>;
+    case 2: return ycsb_exec_coop<false, true, false, kReads>;
+    case 3: return ycsb_exec_coop<false, true, true, kReads>;
+    case 4: return ycsb_exec_coop<true, false, false, kReads>;
+    case 5: return ycsb_exec_coop<true, false, true, kReads>;
+    case 6: return ycsb_exec_coop<true, true, false, kReads>;
+    default: return ycsb_exec_coop<true, true, true, kReads>;
+    }
+}
+
+// reads = false: registration only (late reads)
+static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, bool reads) {
     const LaunchCfg &L = c->launch_y;
     const size_t smem = stage ? 2 * STAGE_WORDS * sizeof(uint32_t) + (size_t)a.stage_entries * sizeof(StageEnt) : 0;
-    void (*k)(YcsbTunedArgs);
     const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
-    switch (sel) {
-    case 0: k = ycsb_exec_coop<false, false, false>; break;
-    case 1: k = ycsb_exec_coop<false, false, true>; break;
-    case 2: k = ycsb_exec_coop<false, true, false>; break;
-    case 3: k = ycsb_exec_coop<false, true, true>; break;
-    case 4: k = ycsb_exec_coop<true, false, false>; break;
-    case 5: k = ycsb_exec_coop<true, false, true>; break;
-    case 6: k = ycsb_exec_coop<true, true, false>; break;
-    default: k = ycsb_exec_coop<true, true, true>; break;
-    }
+    void (*k)(YcsbTunedArgs) = reads ? coop_kernel<true>(sel) : coop_kernel<false>(sel);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
@@ -674,7 +840,7 @@ static bool launch_fast_exec(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
     const uint32_t opt = c->launch_y.per_thread ? c->launch_y.per_thread : 4u;
     if (opt >= 8) return false;
     if (opt == 1 && a.lpt) {
-        launch_coop(c, a, stage);
+        launch_coop(c, a, stage, true);
         return true;
     }
     const uint32_t ops = std::max<uint32_t>(2u, std::min<uint32_t>(opt, 4u));
@@ -721,16 +887,21 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.ways = L.ways ? L.ways : 4u;
     // with the predictor counting but staging off, the staging table is empty
     a.stage_entries = (stage && c->stage_on) ? STAGE_MAX_ENTRIES / a.ways * a.ways : 0u;
+    // late reads need the one-op-per-lane layout (stride <= 32)
+    const bool late = L.late_reads && a.lpt;
     a.filter = L.filter;
+    a.late = late ? L.late_reads : 0u;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
     const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
     if (e != cudaSuccess) return e;
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
-    auto pers_k = stage ? ycsb_persistent<true> : ycsb_persistent<false>;
+    auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
+                        : (late ? ycsb_persistent<false, true> : ycsb_persistent<false, false>);
+    auto cwb_k = !late ? ycsb_checkwb_tuned<0> : L.late_reads == 2u ? ycsb_checkwb_tuned<2> : ycsb_checkwb_tuned<1>;
     if (smem > 48 * 1024) {
         cudaFuncSetAttribute(exec_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(ycsb_checkwb_tuned, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(cwb_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(pers_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
     int per_sm = 0;
@@ -755,20 +926,41 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     }
     prof_mark(c, 0);
     count_launch(c);
-    if (!launch_fast_exec(c, a, stage)) {
-        exec_k<<<grid, threads, smem, c->stream>>>(a);
-    }
+    if (late) launch_coop(c, a, stage, false);
+    else if (!launch_fast_exec(c, a, stage)) exec_k<<<grid, threads, smem, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 1);
     count_launch(c);
     int per_sm_cwb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cwb, ycsb_checkwb_tuned, (int)threads, smem_cwb);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_cwb, cwb_k, (int)threads, smem_cwb);
     if (e != cudaSuccess) return e;
     if (per_sm_cwb < 1) per_sm_cwb = 1;
     const uint32_t grid_cwb = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm_cwb * c->sm_count));
-    ycsb_checkwb_tuned<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
+    cwb_k<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (late && L.late_reads == 2u) {
+        count_launch(c);
+        int per_sm_rd = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rd, ycsb_read_late, 256, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm_rd < 1) per_sm_rd = 1;
+        const uint64_t nw = (uint64_t)a.B * a.lpt;
+        const uint32_t grid_rd = (uint32_t)std::min<uint64_t>((nw + 255) / 256, (uint64_t)per_sm_rd * c->sm_count);
+        ycsb_read_late<<<grid_rd, 256, 0, c->stream>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     prof_mark(c, 2);
+    if (late) {  // the write-back waits for every read of the batch
+        count_launch(c);
+        int per_sm_wb = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_wb, ycsb_writeback_late, 256, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm_wb < 1) per_sm_wb = 1;
+        const uint32_t grid_wb = (uint32_t)std::min<uint64_t>(((uint64_t)a.B + 255) / 256,
+                                                              (uint64_t)per_sm_wb * c->sm_count);
+        ycsb_writeback_late<<<grid_wb, 256, 0, c->stream>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if ((e = predictor_after_batch(c)) != cudaSuccess) return e;
     prof_mark(c, 3);
     return cudaSuccess;

@@ -1,7 +1,9 @@
 """Autotuner for the tuned kernels' launch shape.
 
-Searches ops per thread, blocks per SM, the slot-read filter and the staging
-ways on the batches already uploaded to an engine, times each candidate with
+Searches ops per thread, blocks per SM, the slot-read filter, the warp dedupe,
+the staging ways and (YCSB) where the rows are read (at execute, or after the
+check for committed transactions only) on the batches already uploaded to an
+engine, times each candidate with
 CUDA events on the engine's stream, and keeps the fastest.  Every candidate's
 commit bitmaps are compared with the plain path's on the same batch before it
 may win: a launch shape can change speed, never a commit decision.  Results are
@@ -55,10 +57,15 @@ def save_cached(workload_key, cfg):
 def candidates(workload, staging=False):
     if workload == "ycsb":
         grid = itertools.product([1, 2, 4], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
-        return [dict(block_threads=256, ops_per_thread=o, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w)
-                for o, b, f, d, w in grid]
+        out = [dict(block_threads=256, ops_per_thread=o, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w,
+                    late_reads=0) for o, b, f, d, w in grid]
+        # late reads (in the check kernel, or a kernel of their own) run the
+        # one-op-per-lane registration kernel whatever ops_per_thread says
+        grid = itertools.product([1, 2], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
+        return out + [dict(block_threads=256, ops_per_thread=1, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w,
+                           late_reads=r) for r, b, f, d, w in grid]
     # TPC-C: 128-thread blocks (fixed), up to 16 resident per SM
-    return [dict(block_threads=128, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4)
+    return [dict(block_threads=128, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4, late_reads=0)
             for b, f, d in itertools.product([0, 4, 8, 12], [0, 1], [0, 1])]
 
 

@@ -58,3 +58,32 @@ def test_invalid_arguments_rejected(built_lib):
     assert L.ltpg_gen_create_ycsb(C.byref(p), C.byref(h)) == abi.ERR_INVALID
     q = abi.TpccParamsC(1, 0, 10, 50, 1, 15)  # no warehouses
     assert L.ltpg_gen_create_tpcc(C.byref(q), C.byref(h)) == abi.ERR_INVALID
+
+
+STRUCTS = {"YcsbBatchC": "ltpg_ycsb_batch", "YcsbParamsC": "ltpg_ycsb_params", "TpccBatchC": "ltpg_tpcc_batch",
+           "TpccParamsC": "ltpg_tpcc_params", "ConfigC": "ltpg_config", "LaunchC": "ltpg_launch",
+           "PredictorC": "ltpg_predictor_cfg", "ServeCfgC": "ltpg_serve_cfg", "ServeStatsC": "ltpg_serve_stats",
+           "StatsC": "ltpg_batch_stats", "BatchInfoC": "ltpg_batch_info"}
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror of an ABI struct has the C struct's size and field
+    offsets (gcc compiles the header and prints them)."""
+    import subprocess
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "ltpg.h"', "int main(void) {"]
+    for py, c in STRUCTS.items():
+        lines.append(f'printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(abi, py)._fields_:
+            lines.append(f'printf("{py} {name} %zu\\n", offsetof({c}, {name}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line}
+    for py in STRUCTS:
+        cls = getattr(abi, py)
+        assert got[(py, "size")] == C.sizeof(cls), py
+        for name, _ in cls._fields_:
+            assert got[(py, name)] == getattr(cls, name).offset, (py, name)

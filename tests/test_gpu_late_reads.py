@@ -1,0 +1,171 @@
+"""Late reads (launch setting `late_reads`, YCSB): the execute kernel only
+registers, the check kernel reads the rows of committed transactions, and a
+third kernel stores the updates.  Against the oracle: flags, bitmap and the
+table image bit-exact; results bit-exact for every committed transaction and
+0 for every aborted one.  Every mode of the tuned path, filter on and off,
+strides that are and are not a power of two, staging, range scans, ragged
+transactions and keys at the table's end.  Both placements of the reads:
+late_reads = 1 (in the check kernel, per tile) and 2 (a kernel of their own)."""
+import numpy as np
+import pytest
+
+import oracle
+from ltpg_gb300 import Engine, YcsbBatch, YcsbGenerator, abi, key_bucket
+
+pytestmark = pytest.mark.gpu
+TUNED = ["fused", "persistent", "graph"]
+
+
+@pytest.fixture(scope="module")
+def eng(gpu):
+    e = Engine(device=0, n_slots=2, max_txn=1 << 15, max_ops_per_txn=32)
+    yield e
+    e.close()
+
+
+def _late_same(e, o, b, slot, mode):
+    """Runs b; checks flags / bitmap equal, results equal where committed and 0 elsewhere."""
+    e.upload(slot, b)
+    e.run_batch(slot, mode)
+    e.sync()
+    wf, wb, wr = o.run(b)[:3]
+    gf, gb, gr = e.txn_flags(slot, b.n_txn), e.commit_bitmap(slot, b.n_txn), e.txn_results(slot, b.n_txn)
+    assert np.array_equal(gf, wf), ("flags", np.nonzero(gf != wf)[0][:10])
+    assert np.array_equal(gb, wb)
+    com = (wf & abi.FLAG_COMMIT) != 0
+    assert np.array_equal(gr[com], wr[com]), ("results", np.nonzero(com & (gr != wr))[0][:10])
+    assert not gr[~com].any(), "an aborted transaction has a result"
+    return wf
+
+
+@pytest.fixture(params=[1, 2])
+def late(request):
+    return request.param
+
+
+class _late:
+    def __init__(self, e, late, **kw):
+        self.e, self.late, self.kw = e, late, kw
+
+    def __enter__(self):
+        self.saved = self.e.get_launch("ycsb")
+        self.e.set_launch("ycsb", late_reads=self.late, **self.kw)
+        return self
+
+    def __exit__(self, *exc):
+        self.e.stage_set([])
+        self.e.set_launch("ycsb", **self.saved)
+
+
+def test_setting_round_trips(eng, late):
+    with _late(eng, late):
+        assert eng.get_launch("ycsb")["late_reads"] == late
+    assert eng.get_launch("ycsb")["late_reads"] == 0
+    with pytest.raises(Exception):
+        eng.set_launch("ycsb", late_reads=3)
+
+
+@pytest.mark.parametrize("filt", [0, 1])
+@pytest.mark.parametrize("k,upd,theta", [(1, 50, 0.99), (3, 30, 0.99), (7, 20, 0.9), (10, 50, 0.6), (16, 5, 0.99),
+                                         (20, 10, 0.99), (32, 5, 0.8)])
+def test_late_reads_match_oracle(eng, late, k, upd, theta, filt):
+    n = 40000
+    eng.load_ycsb(51, n)
+    o = oracle.YcsbOracle(51, n)
+    g = YcsbGenerator(51, n, 9000, k, upd, theta)
+    with _late(eng, late, filter=filt):
+        aborted = 0
+        for bid, mode in enumerate(TUNED + TUNED):
+            flags = _late_same(eng, o, g.batch(bid), bid % 2, mode)
+            aborted += int(((flags & abi.FLAG_COMMIT) == 0).sum())
+        if k > 1:
+            assert aborted > 0  # the masked case is exercised
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+@pytest.mark.parametrize("B", [1, 31, 32, 33, 4097])
+def test_late_reads_partial_tiles(eng, late, B):
+    n = 3000
+    eng.load_ycsb(52, n)
+    o = oracle.YcsbOracle(52, n)
+    g = YcsbGenerator(52, n, B, 16, 20, 0.99)
+    with _late(eng, late):
+        for bid, mode in enumerate(TUNED):
+            _late_same(eng, o, g.batch(bid), bid % 2, mode)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+def test_late_reads_with_staging(eng, late):
+    n = 100000
+    eng.load_ycsb(53, n)
+    o = oracle.YcsbOracle(53, n)
+    g = YcsbGenerator(53, n, 30000, 16, 5, 0.99, rotate_every=2)
+    with _late(eng, late, stage_ways=2):
+        for bid in range(6):
+            b = g.batch(bid)
+            keys = (b.ops.reshape(b.n_txn, -1)[:, :16] & ((1 << 27) - 1)).ravel()
+            cnt = np.bincount(key_bucket(keys), minlength=abi.STAGE_BUCKETS)
+            eng.stage_set(np.argsort(-cnt, kind="stable")[:abi.STAGE_ENTRIES // 2])
+            _late_same(eng, o, b, bid % 2, TUNED[bid % 3])
+            assert eng.stats(bid % 2)["staged_ops"] > 0
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+@pytest.mark.parametrize("k,scan,n", [(4, 10, 30000), (10, 3, 30000), (16, 16, 30000), (8, 12, 2000)])
+def test_late_reads_with_scans(eng, late, k, scan, n):
+    """Range scans, including scans that run past the table's last key."""
+    eng.load_ycsb(54, n)
+    o = oracle.YcsbOracle(54, n)
+    g = YcsbGenerator(54, n, 6000, k, 20, 0.9, scan_len=scan)
+    with _late(eng, late):
+        for bid, mode in enumerate(TUNED):
+            _late_same(eng, o, g.batch(bid), bid % 2, mode)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+def _ragged(rng, n, B, k):
+    ops, vals = [], []
+    for t in range(B):
+        m = int(rng.integers(0, k + 1))
+        lst, vs = [], []
+        for j in range(m):
+            key = lst[int(rng.integers(0, j))][0] if j > 0 and rng.random() < 0.3 else int(rng.integers(0, n))
+            upd = bool(rng.random() < 0.5)
+            lst.append((key, upd, int(rng.integers(0, 2)) if upd else 0))
+            if upd:
+                vs.append(int(rng.integers(0, 2**63)))
+        ops.append(lst)
+        vals.append(vs)
+    ops[0], vals[0] = [], []
+    return YcsbBatch.from_ops(ops, vals)
+
+
+@pytest.mark.parametrize("k", [7, 16, 32])
+def test_late_reads_ragged_and_table_end(eng, late, k):
+    n = 5000
+    eng.load_ycsb(55, n)
+    o = oracle.YcsbOracle(55, n)
+    rng = np.random.default_rng(k)
+    with _late(eng, late):
+        for bid, mode in enumerate(TUNED):
+            _late_same(eng, o, _ragged(rng, n, 3000, k), bid % 2, mode)
+        ops = [[(n - 1, True, 9), (n - 2, False, 0)], [(n - 1, False, 0)], [(0, True, 0), (n - 1, True, 3)]]
+        _late_same(eng, o, YcsbBatch.from_ops(ops, [[11], [], [12, 13]]), 0, "fused")
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+def test_late_reads_kernel_count(eng, late):
+    n = 20000
+    eng.load_ycsb(56, n)
+    g = YcsbGenerator(56, n, 4000, 16, 5, 0.99)
+    eng.upload(0, g.batch(0))
+    with _late(eng, late):
+        _, k0 = eng.counters()
+        eng.run_batch(0, "fused")
+        eng.sync()
+        _, k1 = eng.counters()
+        assert k1 - k0 == 2 + late
+        eng.run_batch(0, "persistent")
+        eng.sync()
+        _, k2 = eng.counters()
+        assert k2 - k1 == 1
