@@ -191,22 +191,29 @@ def ycsb_bytes_per_txn(k, u, commit_rate, scan=1, late=False):
     check loads 8 per key a read covers / 16 per update, row reads 80 per key a
     read covers, committed update stores 8 per update of a committed
     transaction, result 8, flags 1+1, bitmap 1/8.  A read covers `scan` keys
-    (1: point reads).  Returns (execute, check + write-back, 0).
+    (1: point reads).  Returns bytes of (execute, check + write-back, 0, 0).
 
-    late: execute registers only; check + reads reads the rows of committed
-    transactions' reads (80 per covered key times the commit rate) and writes
-    the result; the write-back kernel reads flags 1 and, for a committed
-    transaction, its value offset 4, op words 4k and update values 8uk, and
-    stores 8uk.  Returns (execute, check + reads, write-back)."""
+    late (1: reads in the check kernel, 2: a read kernel of their own):
+    execute registers only; the check reads op words, slots and writes flags
+    and bitmap; the reads read the committed transactions' op words (4k times
+    the commit rate) and rows (80 per covered key of a read times the commit
+    rate) and write the result 8 (late 2 also reads the flag 1); the
+    write-back reads the flag 1 and, for a committed transaction, its value
+    offset 4, op words 4k and update values 8uk, and stores 8uk.  Returns
+    bytes of (execute, check + reads, 0, write-back) for late 1 and
+    (execute, check, reads, write-back) for late 2."""
     if not late:
         exec_b = 4 * k + 16 * u * k + (16 + 80) * (1 - u) * k * scan + 8
         check_b = (4 * k + 4 + 8 * (1 - u) * k * scan + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1
                    + 1 / 8)
-        return exec_b, check_b, 0.0
+        return exec_b, check_b, 0.0, 0.0
     exec_b = 4 * k + 16 * u * k + 16 * (1 - u) * k * scan
-    check_b = 4 * k + 8 * (1 - u) * k * scan + 16 * u * k + 80 * (1 - u) * k * scan * commit_rate + 8 + 1 + 1 / 8
+    check_b = 4 * k + 8 * (1 - u) * k * scan + 16 * u * k + 1 + 1 / 8
+    read_b = commit_rate * (4 * k + 80 * (1 - u) * k * scan) + 8
     wb_b = 1 + commit_rate * (4 + 4 * k + 16 * u * k)
-    return exec_b, check_b, wb_b
+    if late == 1:
+        return exec_b, check_b + read_b, 0.0, wb_b
+    return exec_b, check_b, read_b + 1, wb_b
 
 
 def profile_traffic(workload, kernel):
@@ -283,8 +290,9 @@ def kernel_split(eng, n_slots, mode, start):
     """Per-kernel times of one more pass over the slots, after the timed region:
     the events that split a batch into its kernels are recorded only here, so
     the timed region carries no instrumentation (on 40-us batches it cost a
-    quarter of the time).  Rows: slots; columns: execute, check+write-back,
-    predictor (YCSB late reads: execute, check+reads, write-back)."""
+    quarter of the time).  Rows: slots; columns: execute, check, reads,
+    write-back (a phase inside another kernel reads 0: the tuned check kernel
+    also writes back unless YCSB reads late)."""
     eng.set_profiling(True)
     run_steps(eng, n_slots, n_slots, mode, start)
     eng.sync()
@@ -689,21 +697,30 @@ def main():
     B = w["n_txn"]
     commit_rate = tuned["commits"] / (args.steps * B)
     kt = tuned["kt"]
-    exec_ms, cwb_ms, third_ms = (float(np.mean(kt[:, i])) for i in range(3))
-    late = w["kind"] == "ycsb" and bool((launch or {}).get("late_reads")) and ((w["ops"] + 3) & ~3) <= 32
-    kernel_ms = {"execute": exec_ms, "check_reads": cwb_ms, "write_back": third_ms} if late else \
-        {"execute": exec_ms, "check_writeback": cwb_ms}
+    exec_ms, cwb_ms, read_ms, wb_ms = (float(np.mean(kt[:, i])) for i in range(4))
+    late = int((launch or {}).get("late_reads") or 0) if w["kind"] == "ycsb" and ((w["ops"] + 3) & ~3) <= 32 else 0
+    if late == 2:
+        kernel_ms = {"execute": exec_ms, "check": cwb_ms, "reads": read_ms, "write_back": wb_ms}
+    elif late == 1:
+        kernel_ms = {"execute": exec_ms, "check_reads": cwb_ms, "write_back": wb_ms}
+    else:
+        kernel_ms = {"execute": exec_ms, "check_writeback": cwb_ms}
     prof_kernel = None
     if w["kind"] == "ycsb":
-        eb, cb, wb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate, max(1, w.get("scan_len", 0)),
-                                        late)
+        eb, cb, rb, wb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate,
+                                            max(1, w.get("scan_len", 0)), late)
         ek = ycsb_exec_kernel_name(launch, (w["ops"] + 3) & ~3)
         cands = [(ek, eb, exec_ms), ("ycsb_checkwb_tuned", cb, cwb_ms)]
         if late:
-            cands.append(("ycsb_writeback_late", wb, third_ms))
+            cands += [("ycsb_read_late", rb, read_ms), ("ycsb_writeback_late", wb, wb_ms)]
         kernel, kbytes, kms = max(cands, key=lambda c: c[2])
-        # the late-read kernels have their own profile summaries
-        prof_kernel = kernel + "_late" if late and kernel != "ycsb_writeback_late" else kernel
+        # the late-read variants of the execute and check kernels have profile
+        # summaries of their own (one execute kernel for both; two check kernels)
+        prof_kernel = kernel
+        if late and kernel == ek:
+            prof_kernel = kernel + "_late"
+        elif late and kernel == "ycsb_checkwb_tuned":
+            prof_kernel = kernel + f"_late{late}"
     else:
         # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
         eb, cb = tpcc_bytes_per_txn(w.get("mix"), commit_rate)

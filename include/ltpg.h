@@ -483,13 +483,14 @@ int ltpg_serve_record_free(ltpg_serve_record *r);
  * counts its kernels). */
 int ltpg_counters(ltpg_ctx *ctx, uint64_t *commits_total, uint64_t *kernel_launches);
 /* When on, every batch run records CUDA events around each of its kernels
- * (also inside captured graphs); ltpg_kernel_times returns the durations in
- * milliseconds of the last run of a slot: [execute, check, write-back] for the
- * plain mode, [execute, check+write-back, predictor] for the tuned modes
- * ([execute, check+reads, write-back+predictor] with YCSB late reads; the
- * predictor's share is 0 when it is off). */
+ * (also inside captured graphs); ltpg_kernel_times writes the durations in
+ * milliseconds of the last run of a slot into ms4 = [execute, check, reads,
+ * write-back].  A phase that runs inside another kernel reads 0: the tuned
+ * modes' check kernel also writes back ([execute, check+write-back, 0, 0]),
+ * YCSB late reads in the check kernel give [execute, check+reads, 0,
+ * write-back], and a persistent launch puts the whole batch under execute. */
 int ltpg_set_profiling(ltpg_ctx *ctx, int on);
-int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms3);
+int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms4);
 
 /* ---- no-allocation batch -------------------------------------------------------
  * This entry point has no counterpart in the reference.  It runs one whole YCSB

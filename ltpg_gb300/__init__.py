@@ -478,7 +478,8 @@ class Engine:
         self._ck(lib().ltpg_set_profiling(self._h, int(bool(on))))
 
     def kernel_times(self, slot):
-        out = (C.c_float * 3)()
+        """[execute, check, reads, write-back] ms of the slot's last run (profiling on)."""
+        out = (C.c_float * 4)()
         self._ck(lib().ltpg_kernel_times(self._h, slot, out))
         return list(out)
 

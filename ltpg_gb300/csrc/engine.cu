@@ -95,7 +95,7 @@ int check_device_error(ltpg_ctx *c) {
 }
 
 int ensure_prof_events(ltpg_ctx *c) {
-    const size_t need = c->slots.size() * 4;
+    const size_t need = c->slots.size() * PROF_MARKS;
     while (c->prof_events.size() < need) {
         cudaEvent_t ev;
         CK(cudaEventCreate(&ev), "event create");
@@ -115,7 +115,7 @@ namespace ltpg {
 void drop_graphs_ctx(ltpg_ctx *c) { drop_graphs(c); }
 void prof_mark(ltpg_ctx *c, int i) {
     if (!c->profiling) return;
-    const size_t k = (size_t)c->cur_slot * 4 + (size_t)i;
+    const size_t k = (size_t)c->cur_slot * PROF_MARKS + (size_t)i;
     if (k >= c->prof_events.size()) return;
     if (c->capturing) cudaEventRecordWithFlags(c->prof_events[k], c->stream, cudaEventRecordExternal);
     else cudaEventRecord(c->prof_events[k], c->stream);
@@ -442,12 +442,14 @@ int run_one(ltpg_ctx *c, uint32_t slot, int mode) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     c->cur_slot = slot;
-    if (mode == LTPG_MODE_PLAIN) {
+    if (mode == LTPG_MODE_PLAIN) {  // intervals: execute, check, (no reads), write-back
+        static const int after[3][2] = {{1, 1}, {2, 3}, {4, 4}};
         prof_mark(c, 0);
         for (int p = 0; p < 3; ++p) {
             int r = run_phase(c, slot, p);
             if (r) return r;
-            prof_mark(c, p + 1);
+            prof_mark(c, after[p][0]);
+            if (after[p][1] != after[p][0]) prof_mark(c, after[p][1]);
         }
         return LTPG_OK;
     }
@@ -770,16 +772,16 @@ int ltpg_set_profiling(ltpg_ctx *c, int on) {
     return LTPG_OK;
 }
 
-int ltpg_kernel_times(ltpg_ctx *c, uint32_t slot, float *ms3) {
+int ltpg_kernel_times(ltpg_ctx *c, uint32_t slot, float *ms4) {
     Slot *s = get_slot(c, slot);
-    if (!s || !ms3) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
+    if (!s || !ms4) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     if (!c->profiling) return fail(c, LTPG_ERR_STATE, "profiling is off");
     CK(cudaStreamSynchronize(c->stream), "sync");
-    cudaEvent_t *ev = &c->prof_events[(size_t)slot * 4];
-    for (int i = 0; i < 3; ++i) {
+    cudaEvent_t *ev = &c->prof_events[(size_t)slot * PROF_MARKS];
+    for (int i = 0; i < PROF_MARKS - 1; ++i) {
         float ms = 0.f;
         cudaError_t e = cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
-        ms3[i] = e == cudaSuccess ? ms : 0.f;
+        ms4[i] = e == cudaSuccess ? ms : 0.f;
         if (e != cudaSuccess) cudaGetLastError();
     }
     return LTPG_OK;

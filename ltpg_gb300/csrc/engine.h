@@ -135,7 +135,7 @@ struct ltpg_ctx {
     bool profiling = false;
     bool capturing = false;
     uint32_t cur_slot = 0;
-    std::vector<cudaEvent_t> prof_events;  // 4 per slot
+    std::vector<cudaEvent_t> prof_events;  // PROF_MARKS per slot
     // cached CUDA graphs keyed by (first, count, workload)
     struct GraphEntry {
         uint32_t first, count;
@@ -149,6 +149,11 @@ struct ltpg_ctx {
 // Kernel launchers implemented in ycsb.cu / tpcc.cu.
 namespace ltpg {
 // Records profiling event i (0..3) of the slot being run, if profiling is on.
+// Profiling marks of a batch: 0 before the first kernel, then after the
+// execute (1), check (2), read (3) and write-back (4) kernels; a phase a mode
+// does not have (or runs inside another kernel) gets its mark at the same
+// place as the one before, so its interval is 0.
+constexpr int PROF_MARKS = 5;
 void prof_mark(ltpg_ctx *c, int i);
 // Drops the cached CUDA graphs (launch settings changed).
 void drop_graphs_ctx(ltpg_ctx *c);

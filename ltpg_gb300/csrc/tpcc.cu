@@ -926,9 +926,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         count_launch(c);
         e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent, dim3(grid), dim3(TBS), args, smem, c->stream);
         if (e != cudaSuccess) return e;
-        prof_mark(c, 1);
-        prof_mark(c, 2);
-        prof_mark(c, 3);
+        for (int m = 1; m < PROF_MARKS; ++m) prof_mark(c, m);
         return cudaSuccess;
     }
     prof_mark(c, 0);
@@ -939,8 +937,7 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     count_launch(c);
     tpcc_checkwb_tuned<<<grid, TBS, smem, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_mark(c, 2);
-    prof_mark(c, 3);
+    for (int m = 2; m < PROF_MARKS; ++m) prof_mark(c, m);
     return cudaSuccess;
 }
 

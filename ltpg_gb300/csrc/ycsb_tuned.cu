@@ -918,11 +918,8 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         count_launch(c);
         e = cudaLaunchCooperativeKernel((const void *)pers_k, dim3(grid), dim3(threads), args, smem, c->stream);
         if (e != cudaSuccess) return e;
-        prof_mark(c, 1);
-        prof_mark(c, 2);
-        if ((e = predictor_after_batch(c)) != cudaSuccess) return e;
-        prof_mark(c, 3);
-        return cudaSuccess;
+        for (int m = 1; m < PROF_MARKS; ++m) prof_mark(c, m);
+        return predictor_after_batch(c);
     }
     prof_mark(c, 0);
     count_launch(c);
@@ -938,6 +935,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     const uint32_t grid_cwb = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm_cwb * c->sm_count));
     cwb_k<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 2);
     if (late && L.late_reads == 2u) {
         count_launch(c);
         int per_sm_rd = 0;
@@ -949,7 +947,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         ycsb_read_late<<<grid_rd, 256, 0, c->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    prof_mark(c, 2);
+    prof_mark(c, 3);
     if (late) {  // the write-back waits for every read of the batch
         count_launch(c);
         int per_sm_wb = 0;
@@ -961,9 +959,8 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         ycsb_writeback_late<<<grid_wb, 256, 0, c->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    if ((e = predictor_after_batch(c)) != cudaSuccess) return e;
-    prof_mark(c, 3);
-    return cudaSuccess;
+    prof_mark(c, 4);
+    return predictor_after_batch(c);
 }
 
 }  // namespace ltpg
