@@ -383,8 +383,9 @@ typedef struct {
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
     uint32_t filter;          /* 1 = read the slot before its atomicMin         */
     uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any; TPC-C: header ops) */
-    uint32_t late_reads;      /* YCSB: 1 = rows read after the check, in the check
-                                 kernel; 2 = in a kernel of their own (see above) */
+    uint32_t late_reads;      /* YCSB: rows read after the check (see above):
+                                 1 = in the check kernel's tiles, 2 = in a kernel
+                                 of their own */
 } ltpg_launch;
 int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
 int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);

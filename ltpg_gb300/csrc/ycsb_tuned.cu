@@ -18,6 +18,9 @@
 //     reads the rows of the committed transactions after the tile's commit
 //     decision, and a third kernel stores the updates, so that no aborted
 //     transaction's rows are read.
+#include <mutex>
+#include <unordered_map>
+
 #include "stage.cuh"
 
 namespace ltpg {
@@ -42,7 +45,7 @@ struct YcsbTunedArgs {
     uint32_t ways, stage_entries;
     uint32_t filter;
     uint32_t lpt;  // lanes per transaction of the one-op-per-lane kernels: stride rounded up to a power of two (0: > 32)
-    uint32_t late; // late reads: 0 off, 1 in the check kernel, 2 in a kernel of their own
+    uint32_t late; // late reads: 0 off, 1 in the check kernel's tiles, 2 in a kernel of their own
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
@@ -164,6 +167,12 @@ struct LateScratch {
     unsigned long long x[32];
 };
 
+// This warp's scratch; one array per kernel, whichever late-read loops it runs.
+__device__ __forceinline__ LateScratch *late_scratch() {
+    __shared__ LateScratch scratch[16];  // blocks of up to 512 threads
+    return scratch + (threadIdx.x >> 5);
+}
+
 // One step of the lanes of a warp (all 32 call it): lane j of transaction t
 // (own: the lane holds an op slot of a transaction; com: t committed).
 __device__ __forceinline__ void late_read_step(const YcsbTunedArgs &a, LateScratch *ws, uint32_t t, uint32_t j,
@@ -233,8 +242,7 @@ __device__ __forceinline__ void late_read_step(const YcsbTunedArgs &a, LateScrat
 
 __device__ __forceinline__ void late_read_tile(const YcsbTunedArgs &a, const uint32_t *fl, uint32_t t0,
                                                uint32_t nt) {
-    __shared__ LateScratch scratch[16];  // blocks of up to 512 threads
-    LateScratch *ws = scratch + (threadIdx.x >> 5);
+    LateScratch *ws = late_scratch();
     const uint32_t lsh = (uint32_t)__ffs(a.lpt) - 1u;
     const uint32_t nl = a.tile << lsh;
     for (uint32_t base = 0; base < nl; base += blockDim.x) {
@@ -248,8 +256,7 @@ __device__ __forceinline__ void late_read_tile(const YcsbTunedArgs &a, const uin
 // Late reads as a kernel of their own (late_reads = 2), after the check: the
 // lanes of the whole batch, lpt per transaction, commit flags from global memory.
 __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
-    __shared__ LateScratch scratch[16];  // blocks of up to 512 threads
-    LateScratch *ws = scratch + (threadIdx.x >> 5);
+    LateScratch *ws = late_scratch();
     const uint32_t lsh = (uint32_t)__ffs(a.lpt) - 1u;
     const uint64_t nw = (uint64_t)a.B << lsh;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
@@ -766,6 +773,19 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     finish_batch(a.ctl);
 }
 
+// Static shared memory of a kernel, queried once per kernel.
+static size_t static_smem(const void *k) {
+    static std::mutex mu;
+    static std::unordered_map<const void *, size_t> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(k);
+    if (it != cache.end()) return it->second;
+    cudaFuncAttributes fa{};
+    const size_t v = cudaFuncGetAttributes(&fa, k) == cudaSuccess ? fa.sharedSizeBytes : 48 * 1024;
+    cache.emplace(k, v);
+    return v;
+}
+
 // Transactions per tile: as many whole transactions as the block reads with
 // `per_thread` 16-byte vectors per thread, rounded down to a multiple of 32.
 static uint32_t tuned_tile(uint32_t stride, uint32_t threads, uint32_t per_thread) {
@@ -792,7 +812,8 @@ static void launch_fast_t(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, uint3
     case 6: k = ycsb_exec_fast<OPS, true, true, false>; break;
     default: k = ycsb_exec_fast<OPS, true, true, true>; break;
     }
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem + static_smem((const void *)k) > 48 * 1024)
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
     if (per_sm < 1) per_sm = 1;
@@ -822,7 +843,8 @@ static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, bool re
     const size_t smem = stage ? 2 * STAGE_WORDS * sizeof(uint32_t) + (size_t)a.stage_entries * sizeof(StageEnt) : 0;
     const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
     void (*k)(YcsbTunedArgs) = reads ? coop_kernel<true>(sel) : coop_kernel<false>(sel);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem + static_smem((const void *)k) > 48 * 1024)
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
     if (per_sm < 1) per_sm = 1;
@@ -899,11 +921,10 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
                         : (late ? ycsb_persistent<false, true> : ycsb_persistent<false, false>);
     auto cwb_k = !late ? ycsb_checkwb_tuned<0> : L.late_reads == 2u ? ycsb_checkwb_tuned<2> : ycsb_checkwb_tuned<1>;
-    if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(exec_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(cwb_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(pers_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
+    // above 48 KB of static + dynamic shared memory a kernel must opt in
+    for (const void *k : {(const void *)exec_k, (const void *)cwb_k, (const void *)pers_k})
+        if (smem + static_smem(k) > 48 * 1024)
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mode == LTPG_MODE_PERSISTENT ? pers_k : exec_k,
                                                       (int)threads, smem);
