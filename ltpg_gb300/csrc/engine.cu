@@ -64,7 +64,9 @@ int ensure_outputs(ltpg_ctx *c, Slot &s, uint64_t n) {
     dev_free(s.results);
     dev_free(s.stats);
     const uint64_t cap = std::max<uint64_t>(n, c->cfg.max_txn);
-    CK(dev_alloc(&s.flags, cap), "alloc flags");
+    // a multiple of 4 bytes: write-first registration ORs conflict bits into
+    // the flag bytes with 32-bit atomics
+    CK(dev_alloc(&s.flags, (cap + 3) / 4 * 4), "alloc flags");
     CK(dev_alloc(&s.bitmap, (cap + 31) / 32 + 1), "alloc bitmap");
     CK(dev_alloc(&s.results, cap), "alloc results");
     CK(dev_alloc(&s.stats, 1), "alloc stats");
@@ -722,7 +724,7 @@ int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
     const uint32_t opt = cfg->ops_per_thread;
     if (opt != 1 && opt != 2 && opt != 4 && opt != 8) return fail(c, LTPG_ERR_INVALID, "ops_per_thread in {1, 2, 4, 8}");
     if (cfg->stage_ways < 1 || cfg->stage_ways > 8) return fail(c, LTPG_ERR_INVALID, "stage_ways in [1, 8]");
-    if (cfg->late_reads > 2) return fail(c, LTPG_ERR_INVALID, "late_reads in {0, 1, 2}");
+    if (cfg->late_reads > 3) return fail(c, LTPG_ERR_INVALID, "late_reads in {0, 1, 2, 3}");
     LaunchCfg &l = workload == LTPG_WORKLOAD_YCSB ? c->launch_y : c->launch_c;
     l.block = cfg->block_threads;
     l.per_thread = cfg->ops_per_thread;

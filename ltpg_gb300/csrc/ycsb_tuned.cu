@@ -45,7 +45,8 @@ struct YcsbTunedArgs {
     uint32_t ways, stage_entries;
     uint32_t filter;
     uint32_t lpt;  // lanes per transaction of the one-op-per-lane kernels: stride rounded up to a power of two (0: > 32)
-    uint32_t late; // late reads: 0 off, 1 in the check kernel's tiles, 2 in a kernel of their own
+    uint32_t late; // late reads: 0 off, 1 in the check kernel's tiles, 2 in a kernel of their own,
+                   // 3 write-first registration
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
@@ -264,11 +265,138 @@ __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
         const uint64_t v = base + threadIdx.x;
         const bool own = v < nw;
         const uint32_t t = (uint32_t)(v >> lsh), j = (uint32_t)v & (a.lpt - 1u);
-        late_read_step(a, ws, t, j, own, own && (a.flags[t] & LTPG_FLAG_COMMIT) != 0u);
+        // the commit decision from the conflict bits (the check kernel of late
+        // reads 2 also set COMMIT; write-first leaves it to the write-back)
+        late_read_step(a, ws, t, j, own,
+                       own && commits(a.flags[t] & (LTPG_FLAG_RAW | LTPG_FLAG_WAR | LTPG_FLAG_WAW)));
     }
 }
 
 __global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop(a); }
+
+// ---- write-first registration (late_reads = 3) ---------------------------------
+// The same RAW / WAR / WAW outcome with one random slot access per op instead
+// of two.  (1) The updates register (write word).  (2) Each read loads its
+// key's slot once: the write word is final, so RAW = (smallest writer < t);
+// the read registers in the read word only when the key has a writer in this
+// batch, since a key without one has no WAR to detect.  A key with a writer
+// thus gets every one of its reads registered, as in the protocol.  (3) The
+// updates load their slot for WAR and WAW, the transaction's bits are OR-ed
+// with its RAW bit and the commit decided; (4) the committed reads gather
+// their rows (late_read_loop); (5) the write-back.  Flags hold the RAW bit
+// between (2) and (3).  Deciding in a kernel of its own keeps the update's
+// slot load out of the path of the row reads: 81 % of the warps of a
+// 16-op, 5 %-update batch hold an update.
+
+// 16-byte slot load through L1: the write words are final after (1), and L1
+// is invalidated between dependent kernels; a read word seen stale is never
+// below the current one, so skipping a red.min on it stays exact.
+__device__ __forceinline__ ulonglong2 ld_slot_ca(const RegSlot *p) {
+    ulonglong2 v;
+    asm volatile("ld.global.ca.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+
+// (1) the updates' registrations: four op words per thread (transactions are
+// 4-word aligned); every op's key is bounds-checked here.
+__device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint64_t tag) {
+    const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops);
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += step) {
+        const uint4 w4 = ld_nc_u4(vp + v);
+        const uint32_t t = (uint32_t)(v * 4u / a.stride);
+        const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = words[q];
+            if (ycsb_is_pad(w)) continue;
+            const uint32_t key = ycsb_key(w);
+            if (key >= a.n) {
+                report_error(a.ctl, DERR_BOUNDS, t);
+                continue;
+            }
+            if (!ycsb_is_update(w)) continue;
+            unsigned long long *slot = &a.reg[key].w;
+            const unsigned long long mine = tag | t;
+            if (!a.filter || ld_ca_u64(slot) > mine) red_min(slot, mine);
+        }
+    }
+}
+
+// One key of a read: RAW against the final write word, registration when the
+// key has a writer.  Returns the RAW bit.
+__device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key, uint32_t t, uint32_t epoch,
+                                            unsigned long long mine) {
+    const ulonglong2 s = ld_slot_ca(a.reg + key);
+    const uint32_t wmin = slot_min(s.y, epoch);
+    if (wmin != 0xFFFFFFFFu && s.x > mine) red_min(&a.reg[key].r, mine);
+    return wmin < t;
+}
+
+// (2) reads: one op per lane, lpt lanes per transaction; the transaction's RAW
+// bit goes to its flag byte.
+__device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32_t epoch) {
+    const uint64_t tag = slot_tag(epoch);
+    const uint32_t lpt = a.lpt;
+    const uint32_t lsh = (uint32_t)__ffs(lpt) - 1u;
+    const uint64_t nw = (uint64_t)a.B << lsh;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
+        const uint64_t v = base + threadIdx.x;
+        const bool own = v < nw;
+        const uint32_t t = (uint32_t)(v >> lsh), j = (uint32_t)v & (lpt - 1u);
+        const uint32_t w = own && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
+        const uint32_t key = ycsb_key(w);
+        uint32_t f = 0;
+        if (!ycsb_is_pad(w) && !ycsb_is_update(w) && key < a.n) {
+            const unsigned long long mine = tag | t;
+            bool raw = wf_read_key(a, key, t, epoch, mine);
+            if (ycsb_span(w)) {
+                const uint64_t last = scan_last(w, a.n);
+                for (uint64_t q = (uint64_t)key + 1; q <= last; ++q) raw |= wf_read_key(a, q, t, epoch, mine);
+            }
+            f = raw ? LTPG_FLAG_RAW : 0u;
+        }
+        for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) f |= __shfl_xor_sync(FULL, f, o);
+        if (own && j == 0u) a.flags[t] = (uint8_t)f;
+    }
+}
+
+// (3) the updates' WAR / WAW, OR-ed into the transaction's flag byte (32-bit
+// atomics on the padded flag array); four op words per thread, the slot loads
+// of a thread's updates all issued before the first is used.  The commit
+// decision is made where it is needed: by the read kernel and by the
+// write-back, which also writes the final flags, bitmap and counters.
+__device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch) {
+    const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops);
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += step) {
+        const uint4 w4 = ld_nc_u4(vp + v);
+        const uint32_t t = (uint32_t)(v * 4u / a.stride);
+        const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
+        bool upd[4];
+        ulonglong2 s[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = words[q];
+            upd[q] = !ycsb_is_pad(w) && ycsb_is_update(w) && ycsb_key(w) < a.n;
+            s[q] = upd[q] ? ld_slot(a.reg + ycsb_key(w)) : make_ulonglong2(~0ull, ~0ull);
+        }
+        uint32_t f = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (slot_min(s[q].x, epoch) < t) f |= LTPG_FLAG_WAR;
+            if (slot_min(s[q].y, epoch) < t) f |= LTPG_FLAG_WAW;
+        }
+        if (f) atomicOr(reinterpret_cast<unsigned *>(a.flags) + (t >> 2), f << (8u * (t & 3u)));
+    }
+}
+
+__global__ void __launch_bounds__(256) ycsb_wf_writes(YcsbTunedArgs a) { wf_register_writes(a, slot_tag(a.ctl->epoch)); }
+__global__ void __launch_bounds__(256) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads(a, a.ctl->epoch); }
+__global__ void __launch_bounds__(256) ycsb_wf_check(YcsbTunedArgs a) { wf_check(a, a.ctl->epoch); }
 
 // ---- check + write-back over all tiles assigned to this block ------------------
 // fl: tile flags.  kLate = 0: the third pass stores the committed updates;
@@ -719,15 +847,54 @@ __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
     if (!kLate) finish_batch(a.ctl);
 }
 
-// Write-back after late reads: one thread per committed transaction.
+// Write-back after late reads: one thread per transaction; a committed one
+// stores its updates.  kDecide (write-first registration): the flags hold the
+// conflict bits only, and this pass makes the commit decision and writes the
+// final flags, the bitmap (a warp's ballot over 32 consecutive transactions is
+// one bitmap word) and the counters.
+template <bool kDecide>
 __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     const uint32_t step = gridDim.x * blockDim.x;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < a.B; t += step)
-        if (a.flags[t] & LTPG_FLAG_COMMIT) write_txn_updates(a, t);
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long c_com = 0, c_raw = 0, c_war = 0, c_waw = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < a.B; base += step) {
+        const uint32_t t = base + threadIdx.x;
+        const bool act = t < a.B;
+        const uint32_t f = act ? a.flags[t] : 0u;
+        bool com;
+        if (kDecide) {
+            com = act && commits(f);
+            if (act) a.flags[t] = (uint8_t)(f | (com ? LTPG_FLAG_COMMIT : 0u));
+            const unsigned bc = __ballot_sync(FULL, com);
+            const unsigned br = __ballot_sync(FULL, (f & LTPG_FLAG_RAW) != 0u);
+            const unsigned bwr = __ballot_sync(FULL, (f & LTPG_FLAG_WAR) != 0u);
+            const unsigned bww = __ballot_sync(FULL, (f & LTPG_FLAG_WAW) != 0u);
+            if (lane == 0u && act) {
+                a.bitmap[t >> 5] = bc;
+                c_com += __popc(bc);
+                c_raw += __popc(br);
+                c_war += __popc(bwr);
+                c_waw += __popc(bww);
+            }
+        } else {
+            com = (f & LTPG_FLAG_COMMIT) != 0u;
+        }
+        if (com) write_txn_updates(a, t);
+    }
+    if (kDecide && lane == 0u) {
+        if (c_com) {
+            red_add_u64(&a.st->commits, c_com);
+            red_add_u64(&a.ctl->total_commits, c_com);
+        }
+        if (c_raw) red_add_u64(&a.st->raw, c_raw);
+        if (c_war) red_add_u64(&a.st->war, c_war);
+        if (c_waw) red_add_u64(&a.st->waw, c_waw);
+    }
 }
 
+template <bool kDecide>
 __global__ void __launch_bounds__(256) ycsb_writeback_late(YcsbTunedArgs a) {
-    writeback_late_loop(a);
+    writeback_late_loop<kDecide>(a);
     finish_batch(a.ctl);
 }
 
@@ -741,6 +908,19 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     const SmemPtrs p = carve(smem, a.tile);
     const uint32_t epoch = a.ctl->epoch;
     const uint64_t tag = slot_tag(epoch);
+    if (kLate && !kStage && a.late == 3u) {  // write-first: five phases, four grid barriers
+        wf_register_writes(a, tag);
+        bool ok = grid_barrier(a.ctl, 2000000000ull);
+        if (ok) wf_register_reads(a, epoch);
+        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
+        if (ok) wf_check(a, epoch);
+        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
+        if (ok) late_read_loop(a);
+        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
+        if (ok) writeback_late_loop<true>(a);
+        finish_batch(a.ctl);
+        return;
+    }
     if (kStage) {
         stage_init(p.tab, a.stage_entries);
         __syncthreads();
@@ -768,7 +948,7 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
             if (ok) late_read_loop(a);
         }
         ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-        if (ok) writeback_late_loop(a);
+        if (ok) writeback_late_loop<false>(a);
     }
     finish_batch(a.ctl);
 }
@@ -854,6 +1034,45 @@ static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, bool re
     k<<<grid, 256, smem, c->stream>>>(a);
 }
 
+// Grid of a 256-thread grid-stride kernel over `items` lanes: at most the
+// blocks that fit on the GPU at once (blocks_per_sm caps them when set).
+static uint32_t stride_grid(ltpg_ctx *c, const void *k, uint64_t items) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (c->launch_y.blocks_per_sm && (int)c->launch_y.blocks_per_sm < per_sm) per_sm = (int)c->launch_y.blocks_per_sm;
+    const uint64_t g = std::min<uint64_t>((items + 255) / 256, (uint64_t)per_sm * c->sm_count);
+    return (uint32_t)std::max<uint64_t>(g, 1);
+}
+
+// Write-first registration (late_reads = 3): write registration, read
+// registration + RAW, WAR / WAW, committed reads, commit decision +
+// write-back.  Profiled as [registration (both), check, reads, write-back].
+static cudaError_t launch_write_first(ltpg_ctx *c, const YcsbTunedArgs &a) {
+    const uint64_t lanes = (uint64_t)a.B * a.lpt;
+    prof_mark(c, 0);
+    count_launch(c, 2);
+    ycsb_wf_writes<<<stride_grid(c, (const void *)ycsb_wf_writes, (uint64_t)a.B * a.stride / 4), 256, 0,
+                     c->stream>>>(a);
+    ycsb_wf_reads<<<stride_grid(c, (const void *)ycsb_wf_reads, lanes), 256, 0, c->stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    prof_mark(c, 1);
+    count_launch(c, 2);
+    ycsb_wf_check<<<stride_grid(c, (const void *)ycsb_wf_check, (uint64_t)a.B * a.stride / 4), 256, 0,
+                    c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 2);
+    ycsb_read_late<<<stride_grid(c, (const void *)ycsb_read_late, lanes), 256, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 3);
+    count_launch(c);
+    ycsb_writeback_late<true>
+        <<<stride_grid(c, (const void *)ycsb_writeback_late<true>, a.B), 256, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 4);
+    return predictor_after_batch(c);
+}
+
 // Launch shapes of the execute phase, by ops_per_thread: 1 = cooperative row
 // reads (ycsb_exec_coop, any stride <= 32), 2 / 4 = per-thread row reads
 // (ycsb_exec_fast, stride / ops a power of two); 8 = block tiles
@@ -909,10 +1128,14 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.ways = L.ways ? L.ways : 4u;
     // with the predictor counting but staging off, the staging table is empty
     a.stage_entries = (stage && c->stage_on) ? STAGE_MAX_ENTRIES / a.ways * a.ways : 0u;
-    // late reads need the one-op-per-lane layout (stride <= 32)
-    const bool late = L.late_reads && a.lpt;
+    // late reads need the one-op-per-lane layout (stride <= 32); write-first
+    // registration has no staging path (with staging it reads late in a
+    // kernel of their own)
+    uint32_t late_mode = a.lpt ? L.late_reads : 0u;
+    if (late_mode == 3u && stage) late_mode = 2u;
+    const bool late = late_mode != 0u;
     a.filter = L.filter;
-    a.late = late ? L.late_reads : 0u;
+    a.late = late_mode;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
     const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
@@ -920,7 +1143,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
     auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
                         : (late ? ycsb_persistent<false, true> : ycsb_persistent<false, false>);
-    auto cwb_k = !late ? ycsb_checkwb_tuned<0> : L.late_reads == 2u ? ycsb_checkwb_tuned<2> : ycsb_checkwb_tuned<1>;
+    auto cwb_k = !late ? ycsb_checkwb_tuned<0> : late_mode == 1u ? ycsb_checkwb_tuned<1> : ycsb_checkwb_tuned<2>;
     // above 48 KB of static + dynamic shared memory a kernel must opt in
     for (const void *k : {(const void *)exec_k, (const void *)cwb_k, (const void *)pers_k})
         if (smem + static_smem(k) > 48 * 1024)
@@ -942,6 +1165,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         for (int m = 1; m < PROF_MARKS; ++m) prof_mark(c, m);
         return predictor_after_batch(c);
     }
+    if (late_mode == 3u) return launch_write_first(c, a);
     prof_mark(c, 0);
     count_launch(c);
     if (late) launch_coop(c, a, stage, false);
@@ -957,7 +1181,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     cwb_k<<<grid_cwb, threads, smem_cwb, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 2);
-    if (late && L.late_reads == 2u) {
+    if (late_mode == 2u) {
         count_launch(c);
         int per_sm_rd = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rd, ycsb_read_late, 256, 0);
@@ -972,12 +1196,12 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     if (late) {  // the write-back waits for every read of the batch
         count_launch(c);
         int per_sm_wb = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_wb, ycsb_writeback_late, 256, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_wb, ycsb_writeback_late<false>, 256, 0);
         if (e != cudaSuccess) return e;
         if (per_sm_wb < 1) per_sm_wb = 1;
         const uint32_t grid_wb = (uint32_t)std::min<uint64_t>(((uint64_t)a.B + 255) / 256,
                                                               (uint64_t)per_sm_wb * c->sm_count);
-        ycsb_writeback_late<<<grid_wb, 256, 0, c->stream>>>(a);
+        ycsb_writeback_late<false><<<grid_wb, 256, 0, c->stream>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     prof_mark(c, 4);

@@ -62,8 +62,11 @@ def candidates(workload, staging=False):
         # late reads (in the check kernel, or a kernel of their own) run the
         # one-op-per-lane registration kernel whatever ops_per_thread says
         grid = itertools.product([1, 2], [0, 2, 4], [0, 1], [0, 1], [2, 4] if staging else [4])
-        return out + [dict(block_threads=256, ops_per_thread=1, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w,
-                           late_reads=r) for r, b, f, d, w in grid]
+        out += [dict(block_threads=256, ops_per_thread=1, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=w,
+                     late_reads=r) for r, b, f, d, w in grid]
+        # write-first registration: no warp dedupe; the filter applies to the updates
+        return out + [dict(block_threads=256, ops_per_thread=1, blocks_per_sm=b, filter=f, dedupe=0, stage_ways=4,
+                           late_reads=3) for b, f in itertools.product([0, 2, 4], [0, 1])]
     # TPC-C: 128-thread blocks (fixed), up to 16 resident per SM
     return [dict(block_threads=128, ops_per_thread=4, blocks_per_sm=b, filter=f, dedupe=d, stage_ways=4, late_reads=0)
             for b, f, d in itertools.product([0, 4, 8, 12], [0, 1], [0, 1])]

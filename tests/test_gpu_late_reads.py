@@ -4,8 +4,11 @@ third kernel stores the updates.  Against the oracle: flags, bitmap and the
 table image bit-exact; results bit-exact for every committed transaction and
 0 for every aborted one.  Every mode of the tuned path, filter on and off,
 strides that are and are not a power of two, staging, range scans, ragged
-transactions and keys at the table's end.  Both placements of the reads:
-late_reads = 1 (in the check kernel, per tile) and 2 (a kernel of their own)."""
+transactions and keys at the table's end.  Every placement of the reads:
+late_reads = 1 (in the check kernel, per tile), 2 (a kernel of their own) and
+3 (write-first registration: updates register first, each read loads its
+slot once, registering only on keys with a writer; with staging it falls back
+to 2)."""
 import numpy as np
 import pytest
 
@@ -38,7 +41,7 @@ def _late_same(e, o, b, slot, mode):
     return wf
 
 
-@pytest.fixture(params=[1, 2])
+@pytest.fixture(params=[1, 2, 3])
 def late(request):
     return request.param
 
@@ -62,7 +65,7 @@ def test_setting_round_trips(eng, late):
         assert eng.get_launch("ycsb")["late_reads"] == late
     assert eng.get_launch("ycsb")["late_reads"] == 0
     with pytest.raises(Exception):
-        eng.set_launch("ycsb", late_reads=3)
+        eng.set_launch("ycsb", late_reads=4)
 
 
 @pytest.mark.parametrize("filt", [0, 1])
@@ -164,7 +167,7 @@ def test_late_reads_kernel_count(eng, late):
         eng.run_batch(0, "fused")
         eng.sync()
         _, k1 = eng.counters()
-        assert k1 - k0 == 2 + late
+        assert k1 - k0 == {1: 3, 2: 4, 3: 5}[late]
         eng.run_batch(0, "persistent")
         eng.sync()
         _, k2 = eng.counters()
