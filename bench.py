@@ -78,9 +78,9 @@ def parse():
                     help="steps of the end-to-end leg (host wall clock; long enough to average out host stalls)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop section")
     ap.add_argument("--no-device-gen", action="store_true", help="skip the device-generator section")
-    ap.add_argument("--late-reads", type=int, choices=[0, 1, 2], default=None,
+    ap.add_argument("--late-reads", type=int, choices=[0, 1, 2, 3], default=None,
                     help="YCSB: override the launch setting late_reads (0 rows read at execute, 1 after the check "
-                         "in the check kernel, 2 in a kernel of their own)")
+                         "in the check kernel, 2 in a kernel of their own, 3 write-first registration)")
     ap.add_argument("--no-tune", action="store_true",
                     help="the engine's default launch shape, no autotuning (profiling runs)")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
@@ -201,7 +201,14 @@ def ycsb_bytes_per_txn(k, u, commit_rate, scan=1, late=False):
     write-back reads the flag 1 and, for a committed transaction, its value
     offset 4, op words 4k and update values 8uk, and stores 8uk.  Returns
     bytes of (execute, check + reads, 0, write-back) for late 1 and
-    (execute, check, reads, write-back) for late 2."""
+    (execute, check, reads, write-back) for late 2.
+
+    late 3 (write-first registration): "execute" is the write registration
+    (op words 4k, slot RMW 16 per update) and the read registration (op words
+    4k, one 16-byte slot load per covered key of a read, which also carries
+    the conditional registration, RAW flag 1); the check reads op words 4k and
+    16 per update and ORs the flag 1; the reads as above; the write-back also
+    reads and writes the flag (1 + 1) and writes the bitmap 1/8."""
     if not late:
         exec_b = 4 * k + 16 * u * k + (16 + 80) * (1 - u) * k * scan + 8
         check_b = (4 * k + 4 + 8 * (1 - u) * k * scan + 16 * u * k + 8 * u * k + 8 * u * k * commit_rate + 1
@@ -213,6 +220,9 @@ def ycsb_bytes_per_txn(k, u, commit_rate, scan=1, late=False):
     wb_b = 1 + commit_rate * (4 + 4 * k + 16 * u * k)
     if late == 1:
         return exec_b, check_b + read_b, 0.0, wb_b
+    if late == 3:
+        return (8 * k + 16 * u * k + 16 * (1 - u) * k * scan + 1, 4 * k + 16 * u * k + 1, read_b + 1,
+                wb_b + 1 + 1 / 8)
     return exec_b, check_b, read_b + 1, wb_b
 
 
@@ -699,7 +709,9 @@ def main():
     kt = tuned["kt"]
     exec_ms, cwb_ms, read_ms, wb_ms = (float(np.mean(kt[:, i])) for i in range(4))
     late = int((launch or {}).get("late_reads") or 0) if w["kind"] == "ycsb" and ((w["ops"] + 3) & ~3) <= 32 else 0
-    if late == 2:
+    if late == 3:
+        kernel_ms = {"registration": exec_ms, "check": cwb_ms, "reads": read_ms, "decide_write_back": wb_ms}
+    elif late == 2:
         kernel_ms = {"execute": exec_ms, "check": cwb_ms, "reads": read_ms, "write_back": wb_ms}
     elif late == 1:
         kernel_ms = {"execute": exec_ms, "check_reads": cwb_ms, "write_back": wb_ms}
@@ -710,16 +722,19 @@ def main():
         eb, cb, rb, wb = ycsb_bytes_per_txn(w["ops"], w["update_pct"] / 100, commit_rate,
                                             max(1, w.get("scan_len", 0)), late)
         ek = ycsb_exec_kernel_name(launch, (w["ops"] + 3) & ~3)
-        cands = [(ek, eb, exec_ms), ("ycsb_checkwb_tuned", cb, cwb_ms)]
+        ck = "ycsb_checkwb_tuned"
+        if late == 3:  # the registration interval is two kernels; the reads' dominates
+            ek, ck = "ycsb_wf_reads", "ycsb_wf_check"
+        cands = [(ek, eb, exec_ms), (ck, cb, cwb_ms)]
         if late:
             cands += [("ycsb_read_late", rb, read_ms), ("ycsb_writeback_late", wb, wb_ms)]
         kernel, kbytes, kms = max(cands, key=lambda c: c[2])
         # the late-read variants of the execute and check kernels have profile
         # summaries of their own (one execute kernel for both; two check kernels)
         prof_kernel = kernel
-        if late and kernel == ek:
+        if late in (1, 2) and kernel == ek:
             prof_kernel = kernel + "_late"
-        elif late and kernel == "ycsb_checkwb_tuned":
+        elif late in (1, 2) and kernel == ck:
             prof_kernel = kernel + f"_late{late}"
     else:
         # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
