@@ -170,6 +170,7 @@ int ltpg_destroy(ltpg_ctx *c) {
     for (auto &s : c->slots) free_slot(s);
     dev_free(c->ycsb.rows);
     dev_free(c->ycsb.reg);
+    dev_free(c->ycsb.wbits);
     for (auto &t : c->tpcc.tab) dev_free(t);
     dev_free(c->tpcc.reg);
     dev_free(c->tpcc.name_idx);
@@ -217,9 +218,11 @@ int ltpg_db_load_ycsb(ltpg_ctx *c, uint64_t seed, uint64_t n) {
     drop_graphs(c);
     dev_free(c->ycsb.rows);
     dev_free(c->ycsb.reg);
+    dev_free(c->ycsb.wbits);
     c->ycsb.n = 0;
     CK(dev_alloc(&c->ycsb.rows, n * LTPG_YCSB_FIELDS), "alloc YCSB table");
     CK(dev_alloc(&c->ycsb.reg, n), "alloc YCSB registration table");
+    CK(dev_alloc(&c->ycsb.wbits, (n + 31) / 32), "alloc YCSB writer bitmap");
     c->ycsb.n = n;
     c->ycsb_seed = seed;
     CK(ycsb_init_table(c), "init YCSB table");

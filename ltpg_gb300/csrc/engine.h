@@ -45,6 +45,7 @@ struct YcsbDb {
     uint64_t n = 0;
     uint64_t *rows = nullptr;  // n * 10 u64
     RegSlot *reg = nullptr;    // n
+    uint32_t *wbits = nullptr; // ceil(n / 32): keys with a writer in the batch (write-first registration)
 };
 
 struct TpccDb {

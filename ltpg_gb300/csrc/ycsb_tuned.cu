@@ -47,11 +47,17 @@ struct YcsbTunedArgs {
     uint32_t lpt;  // lanes per transaction of the one-op-per-lane kernels: stride rounded up to a power of two (0: > 32)
     uint32_t late; // late reads: 0 off, 1 in the check kernel's tiles, 2 in a kernel of their own,
                    // 3 write-first registration
+    uint32_t *wbits;  // write-first: one bit per key, set for keys an update of the batch writes
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
     uint64_t v;
     asm volatile("ld.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_ca_u32(const unsigned *p) {
+    uint32_t v;
+    asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
     return v;
 }
 
@@ -275,18 +281,19 @@ __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
 __global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop(a); }
 
 // ---- write-first registration (late_reads = 3) ---------------------------------
-// The same RAW / WAR / WAW outcome with one random slot access per op instead
-// of two.  (1) The updates register (write word).  (2) Each read loads its
-// key's slot once: the write word is final, so RAW = (smallest writer < t);
-// the read registers in the read word only when the key has a writer in this
-// batch, since a key without one has no WAR to detect.  A key with a writer
-// thus gets every one of its reads registered, as in the protocol.  (3) The
-// updates load their slot for WAR and WAW, the transaction's bits are OR-ed
-// with its RAW bit and the commit decided; (4) the committed reads gather
-// their rows (late_read_loop); (5) the write-back.  Flags hold the RAW bit
-// between (2) and (3).  Deciding in a kernel of its own keeps the update's
-// slot load out of the path of the row reads: 81 % of the warps of a
-// 16-op, 5 %-update batch hold an update.
+// The same RAW / WAR / WAW outcome with at most one random slot access per op
+// instead of two.  (1) The updates register (write word) and set their key's
+// bit in a writer bitmap.  (2) A read whose key has no writer in the batch has
+// no RAW and no WAR to cause, and touches no slot; any other read loads its
+// key's slot once: the write word is final, so RAW = (smallest writer < t),
+// and the read registers in the read word.  A key with a writer thus gets
+// every one of its reads registered, as in the protocol.  (3) The updates load
+// their slot for WAR and WAW.  The flag bytes collect the conflict bits of (2)
+// and (3).  (4) The committed reads gather their rows (late_read_loop; commit
+// from the conflict bits); (5) the write-back decides the commits, writes the
+// final flags, bitmap and counters, and stores.  Checking the updates in a
+// kernel of their own keeps their slot loads out of the path of the row
+// reads: 81 % of the warps of a 16-op, 5 %-update batch hold an update.
 
 // 16-byte slot load through L1: the write words are final after (1), and L1
 // is invalidated between dependent kernels; a read word seen stale is never
@@ -297,11 +304,14 @@ __device__ __forceinline__ ulonglong2 ld_slot_ca(const RegSlot *p) {
     return v;
 }
 
-// (1) the updates' registrations: four op words per thread (transactions are
-// 4-word aligned); every op's key is bounds-checked here.
+// (1) the updates' registrations and writer bits: four op words per thread
+// (transactions are 4-word aligned); every op's key is bounds-checked here.
+// Also zeroes the flag bytes, which (2) and (3) OR the conflict bits into.
 __device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint64_t tag) {
     const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ((uint64_t)a.B + 3) / 4; i += step)
+        reinterpret_cast<unsigned *>(a.flags)[i] = 0u;
     const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops);
     for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += step) {
         const uint4 w4 = ld_nc_u4(vp + v);
@@ -320,46 +330,77 @@ __device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint6
             unsigned long long *slot = &a.reg[key].w;
             const unsigned long long mine = tag | t;
             if (!a.filter || ld_ca_u64(slot) > mine) red_min(slot, mine);
+            // bits are only set within a batch: a bit seen set needs no atomic
+            // (hot keys' updates would otherwise all hit one word)
+            unsigned *bw = a.wbits + (key >> 5);
+            if (!((ld_ca_u32(bw) >> (key & 31u)) & 1u)) atomicOr(bw, 1u << (key & 31u));
         }
     }
 }
 
 // One key of a read: RAW against the final write word, registration when the
-// key has a writer.  Returns the RAW bit.
+// key has a writer.  Returns the RAW bit.  A key outside the writer bitmap has
+// no writer in the batch: no RAW, nothing to register, and no slot load (the
+// bitmap, 1/128 of the slot table, stays in L2).
 __device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key, uint32_t t, uint32_t epoch,
                                             unsigned long long mine) {
+    if (!((__ldg(a.wbits + (key >> 5)) >> (key & 31u)) & 1u)) return false;
     const ulonglong2 s = ld_slot_ca(a.reg + key);
     const uint32_t wmin = slot_min(s.y, epoch);
     if (wmin != 0xFFFFFFFFu && s.x > mine) red_min(&a.reg[key].r, mine);
     return wmin < t;
 }
 
-// (2) reads: one op per lane, lpt lanes per transaction; the transaction's RAW
-// bit goes to its flag byte.
+// (2) reads: four op words per thread (one 16-byte load); the writer-bitmap
+// words of the thread's reads are loaded together, then the slots of those
+// with a writer; the RAW bit is OR-ed into the transaction's flag byte
+// (zeroed by (1)) with a 32-bit atomic.
 __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32_t epoch) {
     const uint64_t tag = slot_tag(epoch);
-    const uint32_t lpt = a.lpt;
-    const uint32_t lsh = (uint32_t)__ffs(lpt) - 1u;
-    const uint64_t nw = (uint64_t)a.B << lsh;
+    const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nw; base += step) {
+    const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops);
+    // a block-uniform loop, so that whole warps reach the warp-wide calls below
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < nvec; base += step) {
         const uint64_t v = base + threadIdx.x;
-        const bool own = v < nw;
-        const uint32_t t = (uint32_t)(v >> lsh), j = (uint32_t)v & (lpt - 1u);
-        const uint32_t w = own && j < a.stride ? __ldg(a.ops + (uint64_t)t * a.stride + j) : LTPG_YCSB_OP_PAD;
-        const uint32_t key = ycsb_key(w);
-        uint32_t f = 0;
-        if (!ycsb_is_pad(w) && !ycsb_is_update(w) && key < a.n) {
-            const unsigned long long mine = tag | t;
-            bool raw = wf_read_key(a, key, t, epoch, mine);
-            if (ycsb_span(w)) {
-                const uint64_t last = scan_last(w, a.n);
-                for (uint64_t q = (uint64_t)key + 1; q <= last; ++q) raw |= wf_read_key(a, q, t, epoch, mine);
-            }
-            f = raw ? LTPG_FLAG_RAW : 0u;
+        const bool act = v < nvec;
+        const uint4 w4 = act ? ld_nc_u4(vp + v)
+                             : make_uint4(LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD, LTPG_YCSB_OP_PAD);
+        const uint32_t t = act ? (uint32_t)(v * 4u / a.stride) : 0xFFFFFFFFu;
+        const unsigned long long mine = tag | t;
+        const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
+        bool rd[4];
+        uint32_t bits[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = words[q], key = ycsb_key(w);
+            rd[q] = !ycsb_is_pad(w) && !ycsb_is_update(w) && key < a.n;
+            bits[q] = rd[q] ? __ldg(a.wbits + (key >> 5)) : 0u;
         }
-        for (uint32_t o = lpt >> 1; o >= 1; o >>= 1) f |= __shfl_xor_sync(FULL, f, o);
-        if (own && j == 0u) a.flags[t] = (uint8_t)f;
+        ulonglong2 s[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t key = ycsb_key(words[q]);
+            s[q] = (bits[q] >> (key & 31u)) & 1u ? ld_slot_ca(a.reg + key) : make_ulonglong2(~0ull, ~0ull);
+        }
+        bool raw = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = words[q], key = ycsb_key(w);
+            const uint32_t wmin = slot_min(s[q].y, epoch);
+            if (wmin != 0xFFFFFFFFu && s[q].x > mine) red_min(&a.reg[key].r, mine);
+            raw |= wmin < t;
+            if (rd[q] && ycsb_span(w)) {  // a range scan: the keys after the first
+                const uint64_t last = scan_last(w, a.n);
+                for (uint64_t k2 = (uint64_t)key + 1; k2 <= last; ++k2) raw |= wf_read_key(a, k2, t, epoch, mine);
+            }
+        }
+        // one atomic per transaction: the lowest of its threads in the warp
+        // ORs the bit when any of them saw RAW
+        const unsigned peers = __match_any_sync(FULL, t);
+        const bool any = (__ballot_sync(FULL, raw) & peers) != 0u;
+        if (act && any && (threadIdx.x & 31u) == (uint32_t)__ffs(peers) - 1u)
+            atomicOr(reinterpret_cast<unsigned *>(a.flags) + (t >> 2), LTPG_FLAG_RAW << (8u * (t & 3u)));
     }
 }
 
@@ -1053,7 +1094,8 @@ static cudaError_t launch_write_first(ltpg_ctx *c, const YcsbTunedArgs &a) {
     count_launch(c, 2);
     ycsb_wf_writes<<<stride_grid(c, (const void *)ycsb_wf_writes, (uint64_t)a.B * a.stride / 4), 256, 0,
                      c->stream>>>(a);
-    ycsb_wf_reads<<<stride_grid(c, (const void *)ycsb_wf_reads, lanes), 256, 0, c->stream>>>(a);
+    ycsb_wf_reads<<<stride_grid(c, (const void *)ycsb_wf_reads, (uint64_t)a.B * a.stride / 4), 256, 0,
+                    c->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     prof_mark(c, 1);
@@ -1136,10 +1178,15 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     const bool late = late_mode != 0u;
     a.filter = L.filter;
     a.late = late_mode;
+    a.wbits = c->ycsb.wbits;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
     const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
     if (e != cudaSuccess) return e;
+    // write-first: the writer bitmap starts empty for every batch
+    if (late_mode == 3u &&
+        (e = cudaMemsetAsync(a.wbits, 0, (a.n + 31) / 32 * sizeof(uint32_t), c->stream)) != cudaSuccess)
+        return e;
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
     auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
                         : (late ? ycsb_persistent<false, true> : ycsb_persistent<false, false>);
