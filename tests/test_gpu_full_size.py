@@ -1,6 +1,7 @@
 """Parity at the benchmark sizes: the tuned engine against the oracle on
 full batches — YCSB high contention (10M records, 1,048,576 transactions x 16
-ops, 95/5, theta = 0.99, hot set rotating every 8 batches, across a rotation),
+ops, 95/5, theta = 0.99, hot set rotating every 8 batches, across a rotation;
+rows read at execute, and write-first registration with late reads),
 and TPC-C at W = 64 with 1,048,576 transactions (NewOrder / Payment 50/50 and
 the five-kind mix with names).  Every flag, bitmap word, result and table row
 bit-exact; plus the size-independent properties: commit bits = commit flags,
@@ -26,12 +27,16 @@ def _properties(e, slot, flags, bitmap):
     assert st["waw"] == int(((flags & abi.FLAG_WAW) != 0).sum())
 
 
-def test_ycsb_high_contention_full_size(gpu):
+@pytest.mark.parametrize("late", [0, 3], ids=["reads-at-execute", "write-first"])
+def test_ycsb_high_contention_full_size(gpu, late):
+    """late = 3 is the benchmark's launch setting (write-first registration,
+    rows read by committed transactions only: an aborted one's result is 0)."""
     n = 10_000_000
     g = YcsbGenerator(20261203, n, B, 16, 5, 0.99, 8)
     o = oracle.YcsbOracle(20261203, n)
     e = Engine(device=0, n_slots=2, max_txn=B, max_ops_per_txn=16)
     try:
+        e.set_launch("ycsb", late_reads=late)
         e.load_ycsb(20261203, n)
         for i, (bid, mode) in enumerate([(6, "graph"), (7, "fused"), (8, "graph"), (9, "persistent")]):
             b = g.batch(bid)
@@ -42,7 +47,9 @@ def test_ycsb_high_contention_full_size(gpu):
             got = e.txn_flags(i % 2, B)
             assert np.array_equal(got, flags), np.nonzero(got != flags)[0][:10]
             assert np.array_equal(e.commit_bitmap(i % 2, B), bitmap)
-            assert np.array_equal(e.txn_results(i % 2, B), results)
+            res = e.txn_results(i % 2, B)
+            com = (flags & abi.FLAG_COMMIT) != 0
+            assert np.array_equal(res, results if late == 0 else np.where(com, results, 0))
             _properties(e, i % 2, got, e.commit_bitmap(i % 2, B))
             assert 0.2 < commits / B < 0.9
         assert np.array_equal(e.download_table(abi.TABLE_YCSB), o.rows)
