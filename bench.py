@@ -737,7 +737,7 @@ def main():
         elif late in (1, 2) and kernel == ck:
             prof_kernel = kernel + f"_late{late}"
     else:
-        # NewOrder avg 10 lines, Payment; see the design doc for the per-op byte model
+        # NewOrder avg 10 lines, Payment; per-op byte model in tpcc_bytes_per_txn
         eb, cb = tpcc_bytes_per_txn(w.get("mix"), commit_rate)
         kernel, kbytes, kms = ("tpcc_exec_tuned", eb, exec_ms) if exec_ms >= cwb_ms else \
             ("tpcc_checkwb_tuned", cb, cwb_ms)

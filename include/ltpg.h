@@ -415,7 +415,7 @@ int ltpg_bucket_counts(ltpg_ctx *ctx, uint32_t *host_counts, int reset);
  * trained online on the GPU (one Adam step per batch on 4,096 buckets, label =
  * the latest batch's counts).  When enabled it runs after every tuned YCSB
  * batch (inside CUDA graphs too).  It changes which keys are staged, never a
- * commit decision.  No counterpart in the reference (SURVEY n3). */
+ * commit decision.  No counterpart in the reference. */
 typedef struct {
     uint32_t enable;       /* 0 turns the predictor and staging off            */
     uint32_t train;        /* 1 = train online, 0 = frozen weights            */
@@ -446,7 +446,7 @@ int ltpg_predictor_gradients(ltpg_ctx *ctx, const float *host_x, const float *ho
  * The TPC-C and YCSB parts of a batch run concurrently on two streams and the
  * next batch's upload overlaps the current kernels.  Latency = arrival to the
  * commit bitmap in host memory, over committed requests.  No counterpart in
- * the reference (SURVEY n4).  With `record` non-null, the batch boundaries and
+ * the reference.  With `record` non-null, the batch boundaries and
  * every request's flags and result are kept for replay (free with
  * ltpg_serve_record_free). */
 typedef struct {
