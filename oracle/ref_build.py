@@ -1,9 +1,9 @@
 """Builds the reference's own CUDA kernels for the GPU parity harness.
 
-TEST INFRASTRUCTURE ONLY.  Run in the container that has the reference
-sources at /root/reference; outputs go to oracle/_ref/ (git-ignored), which
-travels to the GPU machine with the repository.  Nothing here is copied from the
-reference: its sources are compiled where they lie.
+TEST INFRASTRUCTURE ONLY.  Run where the reference sources are, at
+/root/reference; outputs go to oracle/_ref/ (git-ignored), which travels with
+a copy of the repository to a machine without them.  Nothing here is copied
+from the reference: its sources are compiled where they lie.
 
   * <prog>.cubin  — the reference program compiled for sm_103a with
                     `nvcc -cubin` (device code only; its host main is ignored).
