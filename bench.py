@@ -762,7 +762,14 @@ def main():
                      "traffic_note": "ncu dram bytes per transaction of a 262,144-transaction capture "
                                      "scaled to the batch" if traffic else None,
                      "kernel_ms": kernel_ms,
-                     "pattern_ceilings": ceilings},
+                     "pattern_ceilings": ceilings,
+                     # the dominant kernel against the measured ceiling of its
+                     # own access pattern (random 80-byte rows read by 5-lane
+                     # groups), where that is the binding pattern
+                     "pattern": ({"ceiling": "row_gather_5lane_GBs", "GBs": ceilings["row_gather_5lane_GBs"],
+                                  "frac": achieved / ceilings["row_gather_5lane_GBs"]}
+                                 if ceilings and achieved and kernel in ("ycsb_read_late", "ycsb_exec_coop")
+                                 else None)},
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],
                 "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)"},
