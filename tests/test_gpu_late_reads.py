@@ -172,3 +172,24 @@ def test_late_reads_kernel_count(eng, late):
         eng.sync()
         _, k2 = eng.counters()
         assert k2 - k1 == 1
+
+
+@pytest.mark.parametrize("mode", TUNED)
+def test_late_reads_out_of_range_key_reports_error(eng, late, mode):
+    """A key past the table's end is reported as LTPG_ERR_BOUNDS (no fault); the
+    context stays usable and the table is untouched."""
+    from ltpg_gb300 import LtpgError
+    eng.load_ycsb(1, 100)
+    with _late(eng, late):
+        bad = YcsbBatch.from_ops([[(3, False, 0)], [(100, True, 0)], [(99, False, 0), (150, False, 0)]],
+                                 [[], [7], []])
+        eng.upload(0, bad)
+        eng.run_batch(0, mode)
+        with pytest.raises(LtpgError) as ei:
+            eng.sync()
+        assert ei.value.code == abi.ERR_BOUNDS
+        o = oracle.YcsbOracle(1, 100)
+        assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+        ok = YcsbBatch.from_ops([[(3, True, 2)], [(4, False, 0)]], [[9], []])
+        _late_same(eng, o, ok, 0, mode)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
