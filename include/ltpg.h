@@ -509,15 +509,40 @@ int ltpg_kernel_times(ltpg_ctx *ctx, uint32_t slot, float *ms4);
  * first call on a device sets that device up (it resolves the array's device
  * address and initialises it), so make that first call before any stream
  * capture.  All calls share the one scratch array, which keeps the previous
- * call's contents (calls are told apart by an epoch tag, and the batch counters
- * are cleared by each call): calls that overlap on the GPU race and give wrong
- * results, so issue them one at a time.  Returns after the batch has finished;
- * LTPG_ERR_BOUNDS if a key was out of range. */
+ * call's contents (calls are told apart by an epoch tag; when the epoch would
+ * pass its last value, a call first sets the array back to its cleared state):
+ * calls that overlap on the GPU race and give wrong results, so issue them one
+ * at a time.  The call blocks: it synchronises `stream` and reads the device
+ * error word before it returns, so the batch has finished on the GPU when it
+ * returns.  LTPG_ERR_BOUNDS if a key was out of range (the batch's other
+ * operations still run, as in ltpg_run_batch). */
 #define LTPG_NOALLOC_MAX_RECORDS (1u << 20)
 int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_records, const uint32_t *ops,
                             const uint32_t *val_off, const uint64_t *vals, uint32_t n_txn,
                             uint32_t ops_per_txn, uint8_t *flags, uint32_t *bitmap, int64_t *results,
                             void *stream);
+
+/* ---- test hooks ---------------------------------------------------------------
+ * For tests of rare states; no counterpart in the reference.
+ * Batch epochs: each batch runs at the next epoch (1 .. 0xFFFFFFFF), which tags
+ * its registration slots so that the tables never need clearing.  Before a
+ * launch would run a batch past the last epoch, the engine sets every slot back
+ * to the cleared state and the epoch to 1 (the reference clears its 18 tables
+ * every batch instead, TF/Database.h:78-102).  ltpg_debug_set_epoch makes the
+ * next batch run at `epoch` (1 .. 0xFFFFFFFF), so a test can cross that point
+ * in a few batches; ltpg_debug_get_epoch reads the device's current epoch.  The
+ * _noalloc_ pair does the same for the no-allocation path of `device`.
+ * ltpg_debug_barrier bounds every grid-barrier wait of the persistent kernels
+ * by limit_ns (0 = the default, 2 s) and makes block `skip_block` of the next
+ * persistent launches never arrive at a barrier (UINT32_MAX = none), so that
+ * the other blocks' waits run out: the launch then ends with LTPG_ERR_TIMEOUT
+ * at the next synchronising call, no table row written, and the context stays
+ * usable (the reference's epoch loop only prints and stops, TF/tp.cu:159-164). */
+int ltpg_debug_set_epoch(ltpg_ctx *ctx, uint32_t epoch);
+int ltpg_debug_get_epoch(ltpg_ctx *ctx, uint32_t *epoch);
+int ltpg_debug_noalloc_set_epoch(int device, uint32_t epoch);
+int ltpg_debug_noalloc_get_epoch(int device, uint32_t *epoch);
+int ltpg_debug_barrier(ltpg_ctx *ctx, uint64_t limit_ns, uint32_t skip_block);
 
 /* ---- access-pattern ceilings --------------------------------------------------
  * Runs one access pattern of the engine's kernels alone and reports its rate:

@@ -483,6 +483,22 @@ class Engine:
         self._ck(lib().ltpg_kernel_times(self._h, slot, out))
         return list(out)
 
+    # test hooks (ltpg_debug_* in include/ltpg.h)
+    def debug_set_epoch(self, epoch):
+        """Makes the next batch run at batch epoch `epoch` (1 .. 2^32 - 1)."""
+        self._ck(lib().ltpg_debug_set_epoch(self._h, epoch))
+
+    def debug_epoch(self):
+        """The device's current batch epoch."""
+        out = C.c_uint32()
+        self._ck(lib().ltpg_debug_get_epoch(self._h, C.byref(out)))
+        return out.value
+
+    def debug_barrier(self, limit_ns=0, skip_block=None):
+        """Bounds the persistent kernels' grid-barrier waits by limit_ns (0: default)
+        and makes block `skip_block` never arrive (None: every block arrives)."""
+        self._ck(lib().ltpg_debug_barrier(self._h, limit_ns, 0xFFFFFFFF if skip_block is None else skip_block))
+
 
 def serve(tpcc_engine, ycsb_engine, rate, duration_s, tpcc_params, ycsb_params, deadline_ms=2.0,
           max_batch=262144, tpcc_pct=70, mode="fused", budget_bytes=40 << 30, slots=4, seed=1, record=False):

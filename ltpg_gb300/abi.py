@@ -157,6 +157,11 @@ SIGNATURES = {
     "ltpg_set_profiling": (C.c_int, [P, C.c_int]),
     "ltpg_kernel_times": (C.c_int, [P, U32, C.POINTER(C.c_float)]),
     "ltpg_ycsb_batch_noalloc": (C.c_int, [C.c_int, P, U64, P, P, P, U32, U32, P, P, P, P]),
+    "ltpg_debug_set_epoch": (C.c_int, [P, U32]),
+    "ltpg_debug_get_epoch": (C.c_int, [P, C.POINTER(U32)]),
+    "ltpg_debug_noalloc_set_epoch": (C.c_int, [C.c_int, U32]),
+    "ltpg_debug_noalloc_get_epoch": (C.c_int, [C.c_int, C.POINTER(U32)]),
+    "ltpg_debug_barrier": (C.c_int, [P, U64, U32]),
     "ltpg_microbench": (C.c_int, [P, C.c_int, U64, U32, C.POINTER(C.c_double)]),
     "ltpg_splitmix64": (U64, [U64]),
     "ltpg_hash3": (U64, [U64, U64, U64]),

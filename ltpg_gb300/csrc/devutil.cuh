@@ -36,6 +36,30 @@ __device__ __forceinline__ uint4 ld_nc_u4(const void *p) {
         : "l"(p));
     return v;
 }
+// Loads of words that other blocks of the same launch wrote before a grid
+// barrier (the persistent kernels' later phases): relaxed at GPU scope, so
+// they are served coherently by L2 and never by a stale L1 line or the
+// read-only path, and the "memory" clobber keeps them after the barrier.
+__device__ __forceinline__ uint32_t ld_gpu_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint64_t ld_gpu_u64(const unsigned long long *p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_gpu_u8(const uint8_t *p) {
+    uint16_t v;
+    asm volatile("ld.relaxed.gpu.global.u8 %0, [%1];" : "=h"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ ulonglong2 ld_gpu_slot(const RegSlot *p) {
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+    return v;
+}
 // Fire-and-forget atomic minimum (no return value, so it issues as a
 // reduction at L2).
 __device__ __forceinline__ void red_min(unsigned long long *p, unsigned long long v) {

@@ -81,6 +81,7 @@ int check_device_error(ltpg_ctx *c) {
     DevCtl h;
     CK(cudaMemcpy(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost), "read control block");
     if (h.error == 0) return LTPG_OK;
+    const uint32_t error = h.error, index = h.err_index;
     // clear the error and any barrier / completion state a failed kernel left
     h.error = 0;
     h.err_index = 0;
@@ -88,11 +89,11 @@ int check_device_error(ltpg_ctx *c) {
     h.barrier_count = 0;
     CK(cudaMemcpy(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice), "clear error");
     char buf[160];
-    if (h.error & DERR_TIMEOUT) {
-        snprintf(buf, sizeof buf, "device wait timed out (index %u)", h.err_index);
+    if (error & DERR_TIMEOUT) {
+        snprintf(buf, sizeof buf, "device wait timed out (block %u)", index);
         return fail(c, LTPG_ERR_TIMEOUT, buf);
     }
-    snprintf(buf, sizeof buf, "key or index out of range in batch (transaction %u)", h.err_index);
+    snprintf(buf, sizeof buf, "key or index out of range in batch (transaction %u)", index);
     return fail(c, LTPG_ERR_BOUNDS, buf);
 }
 
@@ -114,6 +115,36 @@ Slot *get_slot(ltpg_ctx *c, uint32_t slot) {
 }  // namespace
 
 namespace ltpg {
+
+__global__ void ctl_set_epoch_kernel(DevCtl *ctl, uint32_t epoch) {
+    ctl->epoch = epoch;
+    ctl->done = 0u;
+}
+
+cudaError_t ctl_set_epoch(DevCtl *ctl, uint32_t epoch, cudaStream_t st) {
+    ctl_set_epoch_kernel<<<1, 1, 0, st>>>(ctl, epoch);
+    return cudaGetLastError();
+}
+
+int epoch_reserve(ltpg_ctx *c, uint64_t batches) {
+    if (c->epoch_next + batches - 1 <= kEpochLast) {
+        c->epoch_next += batches;
+        return LTPG_OK;
+    }
+    // The batches would pass the last epoch: every slot back to the cleared
+    // state (all ones: tag 0xFFFFFFFF, which no epoch from 1 on carries) and
+    // the epoch to 1, on the context stream ahead of the batches.  The kernels
+    // read the epoch from device memory, so captured graphs stay valid.
+    if (batches > kEpochLast) return fail(c, LTPG_ERR_INVALID, "too many batches in one launch");
+    if (c->ycsb.reg)
+        CK(cudaMemsetAsync(c->ycsb.reg, 0xFF, c->ycsb.n * sizeof(RegSlot), c->stream), "clear YCSB slots");
+    if (c->tpcc.reg)
+        CK(cudaMemsetAsync(c->tpcc.reg, 0xFF, c->tpcc.n_slots * sizeof(RegSlot), c->stream), "clear TPC-C slots");
+    CK(ctl_set_epoch(c->ctl, 1u, c->stream), "reset epoch");
+    c->epoch_next = 1 + batches;
+    return LTPG_OK;
+}
+
 void drop_graphs_ctx(ltpg_ctx *c) { drop_graphs(c); }
 void prof_mark(ltpg_ctx *c, int i) {
     if (!c->profiling) return;
@@ -434,6 +465,13 @@ int run_phase(ltpg_ctx *c, uint32_t slot, int phase) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     c->cur_slot = slot;
+    if (s->workload != LTPG_WORKLOAD_YCSB && s->workload != LTPG_WORKLOAD_TPCC)
+        return fail(c, LTPG_ERR_STATE, "slot holds no batch");
+    // a batch's epoch is taken at its first phase and advanced by its last
+    if (phase == 0 && !c->capturing) {
+        int r = epoch_reserve(c, 1);
+        if (r) return r;
+    }
     count_launch(c);
     cudaError_t e;
     if (s->workload == LTPG_WORKLOAD_YCSB) e = ycsb_phase(c, *s, phase);
@@ -447,6 +485,8 @@ int run_one(ltpg_ctx *c, uint32_t slot, int mode) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     c->cur_slot = slot;
+    if (s->workload != LTPG_WORKLOAD_YCSB && s->workload != LTPG_WORKLOAD_TPCC)
+        return fail(c, LTPG_ERR_STATE, "slot holds no batch");
     if (mode == LTPG_MODE_PLAIN) {  // intervals: execute, check, (no reads), write-back
         static const int after[3][2] = {{1, 1}, {2, 3}, {4, 4}};
         prof_mark(c, 0);
@@ -478,6 +518,10 @@ int ltpg_run_batch(ltpg_ctx *c, uint32_t slot, int mode) {
     if (!c) return LTPG_ERR_INVALID;
     if (mode == LTPG_MODE_GRAPH) return ltpg_run_batches(c, slot, 1, mode);
     if (mode < LTPG_MODE_PLAIN || mode > LTPG_MODE_GRAPH) return fail(c, LTPG_ERR_INVALID, "bad mode");
+    if (mode != LTPG_MODE_PLAIN) {  // the plain mode reserves in its execute phase
+        int r = epoch_reserve(c, 1);
+        if (r) return r;
+    }
     return run_one(c, slot, mode);
 }
 
@@ -493,6 +537,12 @@ int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
         return LTPG_OK;
     }
     const int wl = c->slots[first].workload;
+    for (uint32_t i = 0; i < count; ++i) {
+        const int w = c->slots[first + i].workload;
+        if (w != LTPG_WORKLOAD_YCSB && w != LTPG_WORKLOAD_TPCC) return fail(c, LTPG_ERR_STATE, "slot holds no batch");
+    }
+    int r = epoch_reserve(c, count);
+    if (r) return r;
     for (auto &g : c->graphs)
         if (g.first == first && g.count == count && g.workload == wl) {
             CK(cudaGraphLaunch(g.exec, c->stream), "graph launch");
@@ -506,7 +556,6 @@ int ltpg_run_batches(ltpg_ctx *c, uint32_t first, uint32_t count, int mode) {
     CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
     const uint64_t launches0 = c->launches;
     c->capturing = true;
-    int r = LTPG_OK;
     for (uint32_t i = 0; i < count && r == LTPG_OK; ++i) r = run_one(c, first + i, LTPG_MODE_FUSED);
     c->capturing = false;
     const uint64_t kernels = c->launches - launches0;
@@ -789,6 +838,34 @@ int ltpg_kernel_times(ltpg_ctx *c, uint32_t slot, float *ms4) {
         ms4[i] = e == cudaSuccess ? ms : 0.f;
         if (e != cudaSuccess) cudaGetLastError();
     }
+    return LTPG_OK;
+}
+
+// ---- test hooks ------------------------------------------------------------------
+int ltpg_debug_set_epoch(ltpg_ctx *c, uint32_t epoch) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (epoch == 0u) return fail(c, LTPG_ERR_INVALID, "epoch 0 carries the cleared slots' tag");
+    CK(cudaSetDevice(c->device), "set device");
+    CK(ctl_set_epoch(c->ctl, epoch, c->stream), "set epoch");
+    c->epoch_next = epoch;
+    return ltpg_sync(c);
+}
+
+int ltpg_debug_get_epoch(ltpg_ctx *c, uint32_t *epoch) {
+    if (!c || !epoch) return LTPG_ERR_INVALID;
+    CK(cudaMemcpyAsync(epoch, &c->ctl->epoch, sizeof *epoch, cudaMemcpyDeviceToHost, c->stream), "read epoch");
+    return ltpg_sync(c);
+}
+
+int ltpg_debug_barrier(ltpg_ctx *c, uint64_t limit_ns, uint32_t skip_block) {
+    if (!c) return LTPG_ERR_INVALID;
+    CK(cudaSetDevice(c->device), "set device");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    DevCtl h;
+    CK(cudaMemcpy(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost), "read control block");
+    h.barrier_limit_ns = limit_ns;
+    h.barrier_skip = skip_block == UINT32_MAX ? 0u : skip_block + 1u;
+    CK(cudaMemcpy(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice), "write control block");
     return LTPG_OK;
 }
 

@@ -16,7 +16,12 @@ namespace ltpg {
 //  done         completion counter of that final kernel.
 //  error        OR of LTPG device error bits (bounds, timeouts).
 //  err_index    first offending index, for the error message.
-//  barrier      generation counter of the persistent kernel's grid barrier.
+//  barrier      arrival count and generation of the persistent kernels' grid
+//               barrier.
+//  barrier_skip test hook: block index + 1 of a block that never arrives at a
+//               grid barrier, so that the other blocks' bounded waits run out
+//               (0 = none).
+//  barrier_limit_ns  bound of one grid-barrier wait (0 = kBarrierLimitNs).
 struct DevCtl {
     uint32_t epoch;
     uint32_t done;
@@ -24,12 +29,20 @@ struct DevCtl {
     uint32_t err_index;
     uint32_t barrier_count;
     uint32_t barrier_gen;
-    uint32_t pad[2];
+    uint32_t barrier_skip;
+    uint32_t pad;
     unsigned long long total_commits;
-    unsigned long long pad2;
+    unsigned long long barrier_limit_ns;
 };
 constexpr uint32_t DERR_BOUNDS = 1u;
 constexpr uint32_t DERR_TIMEOUT = 2u;
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
+// Batch epochs 1 .. kEpochLast tag the registration slots (slot_tag in
+// proto.h: tag = 0xFFFFFFFF - epoch).  Epoch 0 would carry the tag of a
+// cleared slot, and a wrapped epoch a tag larger than stale ones, so before a
+// launch would run a batch past kEpochLast the host sets every slot back to
+// the cleared state and the epoch to 1 (epoch_reserve in engine.cu).
+constexpr uint32_t kEpochLast = 0xFFFFFFFFu;
 
 // Per-batch counters accumulated on the device (ltpg_batch_stats).
 struct DevStats {
@@ -131,6 +144,10 @@ struct ltpg_ctx {
     // contention predictor (predictor.cu)
     ltpg_predictor_state *pred = nullptr;
     uint32_t pred_on = 0, pred_train = 0;
+    // Epoch the next batch runs at, or more: every launch adds its batches
+    // before it is enqueued, and the device adds one per batch it finishes,
+    // so the device's epoch never passes this mirror.
+    uint64_t epoch_next = 1;
     // measurement
     uint64_t launches = 0;
     bool profiling = false;
@@ -164,6 +181,11 @@ int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, ui
 int slot_prepare_tpcc(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint64_t n_lines, uint64_t txn_base, Slot **out);
 // Makes generator g's batch batch_id in slot `slot` on stream st (gen_dev.cu).
 int gen_device_batch(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, cudaStream_t st);
+// Makes room for `batches` more batch epochs before a launch (resets the
+// registration slots and the epoch when the last epoch would be passed).
+int epoch_reserve(ltpg_ctx *c, uint64_t batches);
+// Sets the device epoch to `epoch`, in the order of stream `st`.
+cudaError_t ctl_set_epoch(DevCtl *ctl, uint32_t epoch, cudaStream_t st);
 // Record an error message on the context and return its code.
 int ctx_fail(ltpg_ctx *c, int code, const char *msg);
 int ctx_cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what);

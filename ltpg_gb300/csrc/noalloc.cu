@@ -35,10 +35,12 @@ __global__ void ycsb_writeback_plain(const uint8_t *__restrict__ flags, uint32_t
 
 using namespace ltpg;
 
-// Registration slots of the no-allocation path (epoch-tagged, never cleared
-// between calls: each call runs with a newer epoch, see slot_tag in proto.h).
+// Registration slots of the no-allocation path (epoch-tagged: each call runs
+// with a newer epoch, see slot_tag in proto.h; they are set back to the
+// cleared state only when the epoch would pass its last value).
 static __device__ __align__(256) RegSlot g_noalloc_reg[LTPG_NOALLOC_MAX_RECORDS];
-// Control block (epoch, error word, completion counter) and batch counters.
+// Control block (epoch, error word, completion counter), and the batch
+// counters the write-back kernel accumulates (not reported by this path).
 static __device__ __align__(256) DevCtl g_noalloc_ctl;
 static __device__ __align__(256) DevStats g_noalloc_stats;
 
@@ -49,6 +51,7 @@ struct NoallocDevice {
     RegSlot *reg = nullptr;
     DevCtl *ctl = nullptr;
     DevStats *stats = nullptr;
+    uint64_t epoch_next = 1;  // epoch of the next call (the device's never passes it)
 };
 NoallocDevice g_dev[kMaxDevices];
 std::mutex g_mu;
@@ -77,6 +80,20 @@ int setup_device(int device, NoallocDevice **out) {
     *out = &d;
     return LTPG_OK;
 }
+
+// Takes the epoch of one call; when it would pass the last epoch, enqueues on
+// s the reset of the slots and of the epoch ahead of the call's kernels.
+int reserve_epoch(NoallocDevice *d, cudaStream_t s) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (d->epoch_next <= kEpochLast) {
+        ++d->epoch_next;
+        return LTPG_OK;
+    }
+    if (cudaMemsetAsync(d->reg, 0xFF, sizeof(g_noalloc_reg), s) != cudaSuccess) return LTPG_ERR_CUDA;
+    if (ctl_set_epoch(d->ctl, 1u, s) != cudaSuccess) return LTPG_ERR_CUDA;
+    d->epoch_next = 2;
+    return LTPG_OK;
+}
 }  // namespace
 
 extern "C" int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_records, const uint32_t *ops,
@@ -95,9 +112,12 @@ extern "C" int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_re
     const uint32_t k = ops_per_txn, stride = ycsb_stride(k);
     const uint32_t tile = k >= 256 ? 1u : 256u / k;
     const uint32_t grid = (n_txn + tile - 1) / tile;
-    // Counters of this call start at zero; the registration slots need no
-    // clearing (older epochs never match).
-    if (cudaMemsetAsync(d->stats, 0, sizeof(DevStats), s) != cudaSuccess) return LTPG_ERR_CUDA;
+    // an earlier, unrelated launch error of this thread must not be taken
+    // for one of this call's launches
+    (void)cudaGetLastError();
+    // the registration slots need no clearing between calls (older epochs
+    // never match) except when the epoch would pass its last value
+    if ((r = reserve_epoch(d, s)) != LTPG_OK) return r;
     ycsb_exec_plain<<<grid, tile * k, 0, s>>>(ops, n_txn, k, stride, tile, rows, n_records, d->reg, results, d->ctl);
     ycsb_check_plain<<<grid, tile * k, 0, s>>>(ops, n_txn, k, stride, tile, d->reg, n_records, flags, d->ctl);
     ycsb_writeback_plain<<<(n_txn + 255) / 256, 256, 0, s>>>(flags, n_txn, ops, k, stride, val_off, vals, rows,
@@ -114,5 +134,30 @@ extern "C" int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_re
         if (cudaMemcpy(d->ctl, &h, sizeof h, cudaMemcpyHostToDevice) != cudaSuccess) return LTPG_ERR_CUDA;
         return LTPG_ERR_BOUNDS;
     }
+    return LTPG_OK;
+}
+
+extern "C" int ltpg_debug_noalloc_set_epoch(int device, uint32_t epoch) {
+    if (device < 0 || device >= kMaxDevices || epoch == 0u) return LTPG_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return LTPG_ERR_CUDA;
+    NoallocDevice *d = nullptr;
+    int r = setup_device(device, &d);
+    if (r) return r;
+    if (cudaDeviceSynchronize() != cudaSuccess) return LTPG_ERR_CUDA;
+    if (ctl_set_epoch(d->ctl, epoch, nullptr) != cudaSuccess) return LTPG_ERR_CUDA;
+    if (cudaDeviceSynchronize() != cudaSuccess) return LTPG_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_mu);
+    d->epoch_next = epoch;
+    return LTPG_OK;
+}
+
+extern "C" int ltpg_debug_noalloc_get_epoch(int device, uint32_t *epoch) {
+    if (device < 0 || device >= kMaxDevices || !epoch) return LTPG_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return LTPG_ERR_CUDA;
+    NoallocDevice *d = nullptr;
+    int r = setup_device(device, &d);
+    if (r) return r;
+    if (cudaDeviceSynchronize() != cudaSuccess) return LTPG_ERR_CUDA;
+    if (cudaMemcpy(epoch, &d->ctl->epoch, sizeof *epoch, cudaMemcpyDeviceToHost) != cudaSuccess) return LTPG_ERR_CUDA;
     return LTPG_OK;
 }

@@ -74,33 +74,47 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
-// wait is bounded: after `limit_ns` a block records DERR_TIMEOUT and returns
-// false, so a broken launch ends with an error status instead of a hang.
-__device__ __forceinline__ bool grid_barrier(DevCtl *ctl, uint64_t limit_ns) {
+// wait is bounded: after ctl->barrier_limit_ns (0: kBarrierLimitNs) a block
+// records DERR_TIMEOUT and returns false, so a broken launch ends with an
+// error status instead of a hang.  A wait that ran out anywhere in the grid
+// makes every later arrival return false as well, so that no block runs a
+// phase whose inputs some block did not finish.  Callers stop calling it
+// once it has returned false.  Test hook: the block named by
+// ctl->barrier_skip (index + 1) returns false without arriving, so the
+// others' waits run out.
+__device__ __forceinline__ bool grid_barrier(DevCtl *ctl) {
     __shared__ uint32_t ok;
     __syncthreads();
     if (threadIdx.x == 0) {
+        volatile DevCtl *vc = ctl;
+        const unsigned long long lim = vc->barrier_limit_ns;
+        const uint64_t limit_ns = lim ? lim : kBarrierLimitNs;
         ok = 1u;
-        volatile uint32_t *gen = &ctl->barrier_gen;
-        const uint32_t g0 = *gen;
-        __threadfence();
-        const uint32_t arrived = atomicAdd(&ctl->barrier_count, 1u) + 1u;
-        if (arrived == gridDim.x) {
-            ctl->barrier_count = 0u;
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
+        if (vc->barrier_skip == blockIdx.x + 1u) {
+            ok = 0u;
         } else {
-            const uint64_t t0 = global_ns();
-            while (*gen == g0) {
-                __nanosleep(64);
-                if (global_ns() - t0 > limit_ns) {
-                    report_error(ctl, DERR_TIMEOUT, blockIdx.x);
-                    ok = 0u;
-                    break;
+            volatile uint32_t *gen = &ctl->barrier_gen;
+            const uint32_t g0 = *gen;
+            __threadfence();
+            const uint32_t arrived = atomicAdd(&ctl->barrier_count, 1u) + 1u;
+            if (arrived == gridDim.x) {
+                ctl->barrier_count = 0u;
+                __threadfence();
+                atomicAdd(&ctl->barrier_gen, 1u);
+            } else {
+                const uint64_t t0 = global_ns();
+                while (*gen == g0) {
+                    __nanosleep(64);
+                    if (global_ns() - t0 > limit_ns) {
+                        report_error(ctl, DERR_TIMEOUT, blockIdx.x);
+                        ok = 0u;
+                        break;
+                    }
                 }
             }
+            __threadfence();
+            if (vc->error & DERR_TIMEOUT) ok = 0u;
         }
-        __threadfence();
     }
     __syncthreads();
     return ok != 0u;

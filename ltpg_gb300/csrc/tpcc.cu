@@ -879,6 +879,14 @@ __global__ void __launch_bounds__(TBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
     finish_batch(a.ctl);
 }
 
+// One cooperative kernel per batch: execute+register, a bounded grid barrier,
+// check + write-back.  What the second phase loads that the first wrote:
+// registration slots (ld_slot: ld.global.cg, served by L2) and the tile's
+// results (written by the same block, ordered by __syncthreads).  Table rows
+// are read through the read-only path only in the first phase, before any
+// row is written; the second phase's read-modify-writes (C_BALANCE,
+// S_QUANTITY by atomicCAS) touch rows that one committed transaction writes
+// (WAW), whose batch-start value is what they must see.
 __global__ void __launch_bounds__(TBS) tpcc_persistent(TpccTunedArgs a) {
     __shared__ TileHdrT h;
     extern __shared__ __align__(16) long long hot_dyn[];
@@ -886,7 +894,7 @@ __global__ void __launch_bounds__(TBS) tpcc_persistent(TpccTunedArgs a) {
     const uint32_t epoch = a.ctl->epoch;
     if (hot) hot_init(hot, 11u * a.db.W);
     tpcc_exec_tiles(a, h, slot_tag(epoch));
-    if (grid_barrier(a.ctl, 2000000000ull)) tpcc_checkwb_tiles(a, h, epoch, hot);
+    if (grid_barrier(a.ctl)) tpcc_checkwb_tiles(a, h, epoch, hot);
     if (hot) hot_flush(a.db, hot);
     finish_batch(a.ctl);
 }

@@ -61,6 +61,26 @@ __device__ __forceinline__ uint32_t ld_ca_u32(const unsigned *p) {
     return v;
 }
 
+// kCoh (the persistent kernel, where the phases share one launch): every
+// load of a word that an earlier phase of the launch wrote, or that this
+// phase writes (slots, writer bits, flag bytes), is a GPU-scope relaxed load
+// served by L2 (ld_gpu_*), never an L1 or read-only-path load, which could
+// return a line cached before the grid barrier.  Op words, values and rows
+// (read before the write-back) are written by no phase and keep the
+// read-only path.  In the separate kernels L1 starts empty at every kernel.
+template <bool kCoh>
+__device__ __forceinline__ uint64_t ld_filter_u64(const unsigned long long *p) {
+    return kCoh ? ld_gpu_u64(p) : ld_ca_u64(p);
+}
+template <bool kCoh>
+__device__ __forceinline__ uint32_t ld_wbits(const uint32_t *p) {
+    return kCoh ? ld_gpu_u32(p) : __ldg(p);
+}
+template <bool kCoh>
+__device__ __forceinline__ uint32_t ld_flag(const uint8_t *p) {
+    return kCoh ? ld_gpu_u8(p) : (uint32_t)*p;
+}
+
 // ---- execute + register over all tiles assigned to this block ----------------
 template <bool kStage>
 __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long long *dig, StageEnt *tab,
@@ -262,6 +282,7 @@ __device__ __forceinline__ void late_read_tile(const YcsbTunedArgs &a, const uin
 
 // Late reads as a kernel of their own (late_reads = 2), after the check: the
 // lanes of the whole batch, lpt per transaction, commit flags from global memory.
+template <bool kCoh>
 __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
     LateScratch *ws = late_scratch();
     const uint32_t lsh = (uint32_t)__ffs(a.lpt) - 1u;
@@ -274,11 +295,11 @@ __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
         // the commit decision from the conflict bits (the check kernel of late
         // reads 2 also set COMMIT; write-first leaves it to the write-back)
         late_read_step(a, ws, t, j, own,
-                       own && commits(a.flags[t] & (LTPG_FLAG_RAW | LTPG_FLAG_WAR | LTPG_FLAG_WAW)));
+                       own && commits(ld_flag<kCoh>(a.flags + t) & (LTPG_FLAG_RAW | LTPG_FLAG_WAR | LTPG_FLAG_WAW)));
     }
 }
 
-__global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop(a); }
+__global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop<false>(a); }
 
 // ---- write-first registration (late_reads = 3) ---------------------------------
 // The same RAW / WAR / WAW outcome with at most one random slot access per op
@@ -307,6 +328,7 @@ __device__ __forceinline__ ulonglong2 ld_slot_ca(const RegSlot *p) {
 // (1) the updates' registrations and writer bits: four op words per thread
 // (transactions are 4-word aligned); every op's key is bounds-checked here.
 // Also zeroes the flag bytes, which (2) and (3) OR the conflict bits into.
+template <bool kCoh>
 __device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint64_t tag) {
     const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
@@ -329,11 +351,12 @@ __device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint6
             if (!ycsb_is_update(w)) continue;
             unsigned long long *slot = &a.reg[key].w;
             const unsigned long long mine = tag | t;
-            if (!a.filter || ld_ca_u64(slot) > mine) red_min(slot, mine);
+            if (!a.filter || ld_filter_u64<kCoh>(slot) > mine) red_min(slot, mine);
             // bits are only set within a batch: a bit seen set needs no atomic
             // (hot keys' updates would otherwise all hit one word)
             unsigned *bw = a.wbits + (key >> 5);
-            if (!((ld_ca_u32(bw) >> (key & 31u)) & 1u)) atomicOr(bw, 1u << (key & 31u));
+            const uint32_t seen = kCoh ? ld_gpu_u32(bw) : ld_ca_u32(bw);
+            if (!((seen >> (key & 31u)) & 1u)) atomicOr(bw, 1u << (key & 31u));
         }
     }
 }
@@ -342,10 +365,11 @@ __device__ __forceinline__ void wf_register_writes(const YcsbTunedArgs &a, uint6
 // key has a writer.  Returns the RAW bit.  A key outside the writer bitmap has
 // no writer in the batch: no RAW, nothing to register, and no slot load (the
 // bitmap, 1/128 of the slot table, stays in L2).
+template <bool kCoh>
 __device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key, uint32_t t, uint32_t epoch,
                                             unsigned long long mine) {
-    if (!((__ldg(a.wbits + (key >> 5)) >> (key & 31u)) & 1u)) return false;
-    const ulonglong2 s = ld_slot_ca(a.reg + key);
+    if (!((ld_wbits<kCoh>(a.wbits + (key >> 5)) >> (key & 31u)) & 1u)) return false;
+    const ulonglong2 s = kCoh ? ld_gpu_slot(a.reg + key) : ld_slot_ca(a.reg + key);
     const uint32_t wmin = slot_min(s.y, epoch);
     if (wmin != 0xFFFFFFFFu && s.x > mine) red_min(&a.reg[key].r, mine);
     return wmin < t;
@@ -355,6 +379,7 @@ __device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key
 // words of the thread's reads are loaded together, then the slots of those
 // with a writer; the RAW bit is OR-ed into the transaction's flag byte
 // (zeroed by (1)) with a 32-bit atomic.
+template <bool kCoh>
 __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32_t epoch) {
     const uint64_t tag = slot_tag(epoch);
     const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
@@ -375,13 +400,14 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
         for (int q = 0; q < 4; ++q) {
             const uint32_t w = words[q], key = ycsb_key(w);
             rd[q] = !ycsb_is_pad(w) && !ycsb_is_update(w) && key < a.n;
-            bits[q] = rd[q] ? __ldg(a.wbits + (key >> 5)) : 0u;
+            bits[q] = rd[q] ? ld_wbits<kCoh>(a.wbits + (key >> 5)) : 0u;
         }
         ulonglong2 s[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint32_t key = ycsb_key(words[q]);
-            s[q] = (bits[q] >> (key & 31u)) & 1u ? ld_slot_ca(a.reg + key) : make_ulonglong2(~0ull, ~0ull);
+            s[q] = (bits[q] >> (key & 31u)) & 1u ? (kCoh ? ld_gpu_slot(a.reg + key) : ld_slot_ca(a.reg + key))
+                                                 : make_ulonglong2(~0ull, ~0ull);
         }
         bool raw = false;
 #pragma unroll
@@ -392,7 +418,8 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
             raw |= wmin < t;
             if (rd[q] && ycsb_span(w)) {  // a range scan: the keys after the first
                 const uint64_t last = scan_last(w, a.n);
-                for (uint64_t k2 = (uint64_t)key + 1; k2 <= last; ++k2) raw |= wf_read_key(a, k2, t, epoch, mine);
+                for (uint64_t k2 = (uint64_t)key + 1; k2 <= last; ++k2)
+                    raw |= wf_read_key<kCoh>(a, k2, t, epoch, mine);
             }
         }
         // one atomic per transaction: the lowest of its threads in the warp
@@ -409,6 +436,7 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
 // of a thread's updates all issued before the first is used.  The commit
 // decision is made where it is needed: by the read kernel and by the
 // write-back, which also writes the final flags, bitmap and counters.
+template <bool kCoh>
 __device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch) {
     const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
@@ -423,7 +451,8 @@ __device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch)
         for (int q = 0; q < 4; ++q) {
             const uint32_t w = words[q];
             upd[q] = !ycsb_is_pad(w) && ycsb_is_update(w) && ycsb_key(w) < a.n;
-            s[q] = upd[q] ? ld_slot(a.reg + ycsb_key(w)) : make_ulonglong2(~0ull, ~0ull);
+            s[q] = upd[q] ? (kCoh ? ld_gpu_slot(a.reg + ycsb_key(w)) : ld_slot(a.reg + ycsb_key(w)))
+                          : make_ulonglong2(~0ull, ~0ull);
         }
         uint32_t f = 0;
 #pragma unroll
@@ -435,9 +464,11 @@ __device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch)
     }
 }
 
-__global__ void __launch_bounds__(256) ycsb_wf_writes(YcsbTunedArgs a) { wf_register_writes(a, slot_tag(a.ctl->epoch)); }
-__global__ void __launch_bounds__(256) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads(a, a.ctl->epoch); }
-__global__ void __launch_bounds__(256) ycsb_wf_check(YcsbTunedArgs a) { wf_check(a, a.ctl->epoch); }
+__global__ void __launch_bounds__(256) ycsb_wf_writes(YcsbTunedArgs a) {
+    wf_register_writes<false>(a, slot_tag(a.ctl->epoch));
+}
+__global__ void __launch_bounds__(256) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads<false>(a, a.ctl->epoch); }
+__global__ void __launch_bounds__(256) ycsb_wf_check(YcsbTunedArgs a) { wf_check<false>(a, a.ctl->epoch); }
 
 // ---- check + write-back over all tiles assigned to this block ------------------
 // fl: tile flags.  kLate = 0: the third pass stores the committed updates;
@@ -893,7 +924,7 @@ __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
 // conflict bits only, and this pass makes the commit decision and writes the
 // final flags, the bitmap (a warp's ballot over 32 consecutive transactions is
 // one bitmap word) and the counters.
-template <bool kDecide>
+template <bool kDecide, bool kCoh>
 __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     const uint32_t step = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
@@ -901,7 +932,7 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < a.B; base += step) {
         const uint32_t t = base + threadIdx.x;
         const bool act = t < a.B;
-        const uint32_t f = act ? a.flags[t] : 0u;
+        const uint32_t f = act ? ld_flag<kCoh>(a.flags + t) : 0u;
         bool com;
         if (kDecide) {
             com = act && commits(f);
@@ -935,14 +966,17 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
 
 template <bool kDecide>
 __global__ void __launch_bounds__(256) ycsb_writeback_late(YcsbTunedArgs a) {
-    writeback_late_loop<kDecide>(a);
+    writeback_late_loop<kDecide, false>(a);
     finish_batch(a.ctl);
 }
 
 // One cooperative kernel per batch: execute+register, grid barrier, check +
-// write-back.  The barrier wait is bounded (2 s).
+// write-back.  The barrier wait is bounded (grid_barrier); once a wait has
+// run out, a block runs no further phase and calls no further barrier.
 // With late reads (kLate, which needs a.lpt != 0): execute registers only,
-// then check + reads, a second grid barrier, and the write-back.
+// then check + reads, a second grid barrier, and the write-back.  Phases
+// after the first load what earlier phases wrote with coherent loads
+// (kCoh = true above; checkwb_tiles reads slots with ld.global.cg, at L2).
 template <bool kStage, bool kLate>
 __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
@@ -950,15 +984,15 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     const uint32_t epoch = a.ctl->epoch;
     const uint64_t tag = slot_tag(epoch);
     if (kLate && !kStage && a.late == 3u) {  // write-first: five phases, four grid barriers
-        wf_register_writes(a, tag);
-        bool ok = grid_barrier(a.ctl, 2000000000ull);
-        if (ok) wf_register_reads(a, epoch);
-        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-        if (ok) wf_check(a, epoch);
-        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-        if (ok) late_read_loop(a);
-        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-        if (ok) writeback_late_loop<true>(a);
+        wf_register_writes<true>(a, tag);
+        bool ok = grid_barrier(a.ctl);
+        if (ok) wf_register_reads<true>(a, epoch);
+        ok = ok && grid_barrier(a.ctl);
+        if (ok) wf_check<true>(a, epoch);
+        ok = ok && grid_barrier(a.ctl);
+        if (ok) late_read_loop<true>(a);
+        ok = ok && grid_barrier(a.ctl);
+        if (ok) writeback_late_loop<true, true>(a);
         finish_batch(a.ctl);
         return;
     }
@@ -977,7 +1011,7 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
         const uint32_t ops = stage_flush(p.tab, a.stage_entries, a.reg, tag, a.bucket_counts);
         if (ops) red_add_u64(&a.st->staged_ops, ops);
     }
-    bool ok = grid_barrier(a.ctl, 2000000000ull);
+    bool ok = grid_barrier(a.ctl);
     if (ok) {
         if (!kLate) checkwb_tiles<0>(a, p.fl, epoch);
         else if (a.late == 2u) checkwb_tiles<2>(a, p.fl, epoch);
@@ -985,11 +1019,11 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     }
     if (kLate) {
         if (a.late == 2u) {
-            ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-            if (ok) late_read_loop(a);
+            ok = ok && grid_barrier(a.ctl);
+            if (ok) late_read_loop<true>(a);
         }
-        ok = grid_barrier(a.ctl, 2000000000ull) && ok;
-        if (ok) writeback_late_loop<false>(a);
+        ok = ok && grid_barrier(a.ctl);
+        if (ok) writeback_late_loop<false, true>(a);
     }
     finish_batch(a.ctl);
 }
