@@ -9,7 +9,12 @@ timed on the same batches, and both are checked to give bit-identical commit
 bitmaps and table images.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload ycsb_hc|ycsb_small|tpcc] [--theta T] [--sweep]
+                  [--workload ycsb_hc|ycsb_small|tpcc|...] [--theta T] [--no-sweep] [--no-tpcc]
+
+The default line also carries the TPC-C W=64 NewOrder+Payment workload (key
+"tpcc": tuned and plain, bit-exactness, end to end, HBM and atomic
+rooflines, CPU baseline) and the YCSB theta sweep 0 / 0.6 / 0.8 / 0.99 (key
+"theta_sweep", tuned against plain).
 
 --impl reference times the reference protocol's CPU replay (the oracle port,
 all host threads) on the same workload; the reference has no CPU implementation
@@ -70,7 +75,12 @@ def parse():
     ap.add_argument("--workload", default="ycsb_hc", choices=sorted(WORKLOADS))
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--mode", default="graph", choices=["fused", "graph", "persistent"])
-    ap.add_argument("--sweep", action="store_true", help="also time theta 0/0.6/0.8/0.99 (YCSB)")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the theta 0/0.6/0.8/0.99 sweep (YCSB)")
+    ap.add_argument("--no-tpcc", action="store_true", help="skip the TPC-C W=64 record of the YCSB line")
+    ap.add_argument("--cpu-batches-tpcc", type=int, default=3,
+                    help="whole TPC-C batches replayed by the single-threaded CPU baseline")
+    ap.add_argument("--ref-scale-iters", type=int, default=10,
+                    help="timed batches of the reference's kernels at the headline scale")
     ap.add_argument("--cpu-batches", type=int, default=12,
                     help="batches in the CPU-baseline sample (about 10 s of oracle replay at the default sizes)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -81,6 +91,10 @@ def parse():
     ap.add_argument("--late-reads", type=int, choices=[0, 1, 2, 3], default=None,
                     help="YCSB: override the launch setting late_reads (0 rows read at execute, 1 after the check "
                          "in the check kernel, 2 in a kernel of their own, 3 write-first registration)")
+    ap.add_argument("--retune", action="store_true",
+                    help="tune the launch shape even when one is cached, and cache the result")
+    ap.add_argument("--tune-cache", default=None,
+                    help="cache file the autotuner reads first and writes (default: ltpg_gb300.tune.user_cache_path())")
     ap.add_argument("--no-tune", action="store_true",
                     help="the engine's default launch shape, no autotuning (profiling runs)")
     ap.add_argument("--no-predictor", action="store_true", help="skip the predictor section")
@@ -373,9 +387,10 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                 res["launch"] = dict(eng.get_launch("ycsb"), source="default")
             elif mode != "plain":
                 from ltpg_gb300 import tune
-                wkey = f"{args.workload}|theta={theta}"
+                wkey = f"{w['key']}|theta={theta}"
                 cfg, how = tune.apply_cached_or_tune(eng, "ycsb", wkey, list(range(min(8, n_slots))),
-                                                     lambda: eng.load_ycsb(SEED, w["n_records"]))
+                                                     lambda: eng.load_ycsb(SEED, w["n_records"]),
+                                                     cache_path=args.tune_cache, retune=args.retune)
                 res["launch"] = dict(cfg, source=how)
             if mode != "plain" and args.late_reads is not None:
                 eng.set_launch("ycsb", late_reads=args.late_reads)
@@ -463,8 +478,9 @@ def tpcc_bench(args, w, dist, want_extras=True):
                 res["launch"] = dict(eng.get_launch("tpcc"), source="default")
             elif mode != "plain":
                 from ltpg_gb300 import tune
-                cfg, how = tune.apply_cached_or_tune(eng, "tpcc", args.workload, list(range(min(4, n_slots))),
-                                                     lambda: eng.load_tpcc(SEED, w["warehouses"]))
+                cfg, how = tune.apply_cached_or_tune(eng, "tpcc", w["key"], list(range(min(4, n_slots))),
+                                                     lambda: eng.load_tpcc(SEED, w["warehouses"]),
+                                                     cache_path=args.tune_cache, retune=args.retune)
                 res["launch"] = dict(cfg, source=how)
             eng.load_tpcc(SEED, w["warehouses"])
             eng.sync()
@@ -551,10 +567,32 @@ def mixed_tpcc_batch(g, nc, pc):
     return TpccBatch(x, b.lines[src])
 
 
-def reference_gpu(iters):
+# The same sources compiled at the headline scale (oracle/ref_build.py y1_c2,
+# tf_c3): 1,048,576 YCSB transactions x (15 reads + 1 write) over 10,000,000
+# records at theta 0.99 (uniform mode: every key registers), and 1,048,576
+# TPC-C transactions, 524,288 NewOrders + 524,288 Payments, W = 64.
+REF_Y1_C2 = dict(n_records=10_000_000, n_txn=1 << 20, ops=16, theta=0.99)
+REF_TF_C3 = dict(warehouses=64, n_txn=1 << 20)
+
+
+def ref_scale_batches():
+    from ltpg_gb300 import TpccGenerator, YcsbBatch, YcsbGenerator, abi
+    B, n, k = REF_Y1_C2["n_txn"], REF_Y1_C2["n_records"], REF_Y1_C2["ops"]
+    g = YcsbGenerator(SEED, n, B, k, 0, REF_Y1_C2["theta"], 8)
+    keys = (g.batch(0).ops.reshape(B, k) & ((1 << abi.YCSB_KEY_BITS) - 1)).astype(np.uint32)
+    ops = keys.copy()
+    ops[:, k - 1] |= np.uint32(0x80000000)  # reads first, then the one write
+    yb = YcsbBatch(ops.ravel(), np.arange(B + 1, dtype=np.uint32), np.arange(B, dtype=np.uint64) + 7, B, k)
+    half = REF_TF_C3["n_txn"] // 2
+    mb = mixed_tpcc_batch(TpccGenerator(SEED, REF_TF_C3["warehouses"], 1_100_000, neworder_pct=50), half, half)
+    return keys, yb, mb
+
+
+def reference_gpu(iters, scale_iters=10):
     """The reference's own three kernels (LTPG/YCSB/1, LTPG/TPCC-allopt-final,
-    compiled for sm_103a) on its compiled shapes, CUDA events around each
-    kernel, its per-batch clears outside the timed span."""
+    compiled for sm_103a) on its compiled shapes and at the headline scale,
+    CUDA events around each kernel, its per-batch clears outside the timed
+    span."""
     from oracle import reference
     if not reference.available():
         return {"unavailable": "reference cubins not built (oracle/_ref is made where the reference sources are)"}
@@ -578,25 +616,55 @@ def reference_gpu(iters):
         out["neworder_payment_65536"] = {"batch_txn": t.B, "ms_per_batch": sum(ms), "kernel_ms": ms,
                                          "commits": commits, "committed_per_s": commits / (sum(ms) * 1e-3),
                                          "iters": iters}
+    if scale_iters and reference.available("y1_c2") and reference.available("tf_c3"):
+        keys, _, mb = ref_scale_batches()
+        r = reference.RefY1("y1_c2")
+        flags, mark, ms = r.run(keys[:, :-1], keys[:, -1], iters=scale_iters)
+        commits = int((flags[:r.covered] & 8 != 0).sum())
+        out["ycsb_1m_x16"] = {"batch_txn": r.B, "covered_txn": r.covered, "ms_per_batch": sum(ms),
+                              "kernel_ms": ms, "commits": commits, "committed_per_s": commits / (sum(ms) * 1e-3),
+                              "theta": REF_Y1_C2["theta"], "iters": scale_iters}
+        t = reference.RefTF("tf_c3")
+        flags, ms = t.run(mb.txns, mb.lines, iters=scale_iters)
+        commits = int((flags & 8 != 0).sum())
+        out["neworder_payment_1m"] = {"batch_txn": t.B, "ms_per_batch": sum(ms), "kernel_ms": ms,
+                                      "commits": commits, "committed_per_s": commits / (sum(ms) * 1e-3),
+                                      "iters": scale_iters}
     return out
 
 
-def engine_on_ref_shapes(iters):
+def engine_on_ref_shapes(iters, scale_iters=10):
     """The engine on the batches reference_gpu() times, in each launch mode
     (plain, fused, persistent, graph), the same batch in every slot, CUDA
-    events around `iters` batches; `best_mode` names the fastest."""
+    events around `iters` batches (at the headline scale: max(8, scale_iters)
+    batches, with the tuned launch shape of the high-contention YCSB
+    workload); `best_mode` names the fastest."""
     import torch
 
     import ltpg_gb300 as L
+    from ltpg_gb300 import tune
     _, yb, tb, mb = ref_shape_batches()
+    shapes = [("ycsb_10k_x10", lambda e: e.load_ycsb(SEED, REF_Y1["n_records"]), yb, dict(max_ops_per_txn=10), iters),
+              ("payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), tb,
+               dict(max_ops_per_txn=16, max_lines=16), iters),
+              ("neworder_payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), mb,
+               dict(max_ops_per_txn=16, max_lines=max(16, mb.n_lines)), iters)]
+    if scale_iters:
+        _, yb2, mb2 = ref_scale_batches()
+        hc = tune.load_cached("ycsb_hc|theta=0.99")
+
+        def load_y(e):
+            e.load_ycsb(SEED, REF_Y1_C2["n_records"])
+            if hc:
+                e.set_launch("ycsb", **{k: v for k, v in hc.items() if k in dict(L.abi.LaunchC._fields_)})
+
+        big = max(8, scale_iters)
+        shapes += [("ycsb_1m_x16", load_y, yb2, dict(max_ops_per_txn=16), big),
+                   ("neworder_payment_1m", lambda e: e.load_tpcc(SEED, REF_TF_C3["warehouses"]), mb2,
+                    dict(max_ops_per_txn=16, max_lines=mb2.n_lines), big)]
     out = {}
-    for name, load, b, kw in [("ycsb_10k_x10", lambda e: e.load_ycsb(SEED, REF_Y1["n_records"]), yb,
-                               dict(max_ops_per_txn=10)),
-                              ("payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), tb,
-                               dict(max_ops_per_txn=16, max_lines=16)),
-                              ("neworder_payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), mb,
-                               dict(max_ops_per_txn=16, max_lines=max(16, mb.n_lines)))]:
-        n_slots = 8
+    for name, load, b, kw, n_it in shapes:
+        n_slots = 8 if b.n_txn <= 65536 else 2
         e = L.Engine(device=0, n_slots=n_slots, max_txn=b.n_txn, **kw)
         try:
             load(e)
@@ -604,12 +672,12 @@ def engine_on_ref_shapes(iters):
                 e.upload(s, b)
             res = {}
             for mode in ["plain", "fused", "persistent", "graph"]:
-                nxt = run_steps(e, n_slots, 16, mode)
-                secs, commits, launches, _ = timed(e, torch, n_slots, iters, mode, nxt, None)
-                res[mode] = {"ms_per_batch": secs * 1e3 / iters, "committed_per_s": commits / secs,
-                             "launches_per_batch": launches / iters}
+                nxt = run_steps(e, n_slots, 16 if n_slots == 8 else 2, mode)
+                secs, commits, launches, _ = timed(e, torch, n_slots, n_it, mode, nxt, None)
+                res[mode] = {"ms_per_batch": secs * 1e3 / n_it, "committed_per_s": commits / secs,
+                             "launches_per_batch": launches / n_it}
             res["best_mode"] = min(("plain", "fused", "persistent", "graph"), key=lambda m: res[m]["ms_per_batch"])
-            res["commits"] = commits // iters
+            res["commits"] = commits // n_it
             res["batch_txn"] = b.n_txn
             out[name] = res
         finally:
@@ -623,6 +691,7 @@ def reference_arm(args, w, rank):
         return
     threads = os.cpu_count() or 1
     t_start = time.perf_counter()
+    theta = None
     if w["kind"] == "ycsb":
         import oracle
         from ltpg_gb300 import YcsbGenerator
@@ -663,47 +732,54 @@ def reference_arm(args, w, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": secs * 1e3 / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": w["name"]},
+            "config": bench_config(w, theta),
             "cpu_baseline": {"value": v, "unit": "txn/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": "txn/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t_start}
     if not args.no_reference_gpu:
         try:
-            line["reference_gpu"] = reference_gpu(200)
+            line["reference_gpu"] = reference_gpu(200, args.ref_scale_iters)
         except Exception as exc:  # the CPU arm's line stands on its own
             line["reference_gpu"] = {"unavailable": f"{type(exc).__name__}: {exc}"[:200]}
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
-    ws, rank, local, dist = dist_setup()
-    w = dict(WORKLOADS[args.workload])
-    if args.impl == "reference":
-        reference_arm(args, w, rank)
-        return
-    import __graft_entry__
-    __graft_entry__.build()
-    import torch
-    torch.cuda.set_device(local)
-    peaks, peak_kind = measured_peaks()
+def bench_config(w, theta):
+    """The workload as both arms name it: the same dict in both JSON lines."""
+    cfg = {"workload": w["name"], "batch_txn": w["n_txn"],
+           "l2": "inputs larger than L2 (table, registration slots and batch exceed 129 MB)"}
     if w["kind"] == "ycsb":
-        theta = args.theta if args.theta is not None else w["theta"]
-        res, exact, e2e, batches = ycsb_bench(args, w, theta, dist)
-    else:
-        theta = None
-        res, exact, e2e, batches = tpcc_bench(args, w, dist)
+        cfg["theta"] = theta
+    return cfg
+
+
+def tpcc_registrations_per_txn(batches):
+    """Registration atomics per transaction that the tuned TPC-C execute
+    kernel issues before its slot filter: NewOrder 3 header ops + 2 per order
+    line (stock write, ORDER-LINE insert), Payment 3 (customer read and write,
+    HISTORY insert); reads of WAREHOUSE / DISTRICT / ITEM do not register."""
+    from ltpg_gb300 import abi
+    total, n = 0, 0
+    for b in batches:
+        kind = b.txns["kind_info"] & 0xFF
+        cnt = (b.txns["kind_info"] >> 8) & 0xFF
+        no = kind == abi.TPCC_NEWORDER
+        total += int((3 + 2 * cnt[no].astype(np.int64)).sum()) + 3 * int((kind == abi.TPCC_PAYMENT).sum())
+        n += len(kind)
+    return total / n
+
+
+def workload_record(args, w, theta, dist, res, exact, e2e, batches, peaks, peak_kind):
+    """One workload's figures (after the reductions over ranks): tuned value,
+    plain path, bit-exactness, roofline of the dominant kernel, end to end."""
     tuned, plain = res[args.mode], res["plain"]
     launch = res.get("launch")
     ceilings = res.get("ceilings")
     secs = reduce_max(dist, tuned["secs"])
-    commits = reduce_sum(dist, tuned["commits"])
-    value = commits / secs
+    value = reduce_sum(dist, tuned["commits"]) / secs
     p_secs = reduce_max(dist, plain["secs"])
     p_value = reduce_sum(dist, plain["commits"]) / p_secs
     e2e_value = reduce_sum(dist, e2e["commits"]) / reduce_max(dist, e2e["secs"])
-    if rank != 0:
-        return
     B = w["n_txn"]
     commit_rate = tuned["commits"] / (args.steps * B)
     kt = tuned["kt"]
@@ -743,42 +819,109 @@ def main():
             ("tpcc_checkwb_tuned", cb, cwb_ms)
     achieved = kbytes * B / (kms / 1e3) / 1e9 if kms > 0 else None
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = profile_traffic(args.workload, prof_kernel or kernel)
-    line = {
-        "metric": "committed txns/s", "value": value, "unit": "txn/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": w["name"], "theta": theta, "mode": args.mode, "batch_txn": B,
-                   "l2": "inputs larger than L2 (table, registration slots and batch exceed 129 MB)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+    traffic = profile_traffic(w["key"], prof_kernel or kernel)
+    roof = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_txn": kbytes,
+            "traffic": traffic * B if traffic else None,
+            "traffic_note": "ncu dram bytes per transaction of a 262,144-transaction capture "
+                            "scaled to the batch" if traffic else None,
+            "kernel_ms": kernel_ms,
+            "pattern_ceilings": ceilings,
+            # the dominant kernel against the measured ceiling of its own
+            # access pattern (random 80-byte rows read by 5-lane groups),
+            # where that is the binding pattern
+            "pattern": ({"ceiling": "row_gather_5lane_GBs", "GBs": ceilings["row_gather_5lane_GBs"],
+                         "frac": achieved / ceilings["row_gather_5lane_GBs"]}
+                        if ceilings and achieved and kernel in ("ycsb_read_late", "ycsb_exec_coop") else None)}
+    if w["kind"] == "tpcc" and not w.get("mix") and kernel == "tpcc_exec_tuned" and kms > 0:
+        # the execute kernel is issue- and atomic-bound: its registration
+        # reductions against the measured random red.min rate of this GPU
+        regs = tpcc_registrations_per_txn(batches)
+        rate = regs * B / (kms / 1e3) / 1e9
+        ceil = (ceilings or {}).get("red_min_random_G_per_s")
+        roof["atomics"] = {"registrations_per_txn": regs, "G_per_s": rate, "ceiling": "red_min_random_G_per_s",
+                           "ceiling_G_per_s": ceil, "frac": rate / ceil if ceil else None}
+    return {
+        "value": value, "ms_per_step": secs * 1e3 / args.steps,
         "plain": {"value": p_value, "ms_per_step": p_secs * 1e3 / args.steps,
                   "speedup_tuned_over_plain": value / p_value if p_value else None},
         "bit_exact_tuned_vs_plain": bool(exact),
         "commit_rate": commit_rate,
-        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_txn": kbytes,
-                     "traffic": traffic * B if traffic else None,
-                     "traffic_note": "ncu dram bytes per transaction of a 262,144-transaction capture "
-                                     "scaled to the batch" if traffic else None,
-                     "kernel_ms": kernel_ms,
-                     "pattern_ceilings": ceilings,
-                     # the dominant kernel against the measured ceiling of its
-                     # own access pattern (random 80-byte rows read by 5-lane
-                     # groups), where that is the binding pattern
-                     "pattern": ({"ceiling": "row_gather_5lane_GBs", "GBs": ceilings["row_gather_5lane_GBs"],
-                                  "frac": achieved / ceilings["row_gather_5lane_GBs"]}
-                                 if ceilings and achieved and kernel in ("ycsb_read_late", "ycsb_exec_coop")
-                                 else None)},
+        "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],
                 "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)"},
         "gpu_launches": int(tuned["launches"]),
         "launch": launch,
         "clocks": tuned["clocks"],
+        "modes": res.get("modes"),
     }
-    if res.get("modes"):
-        line["modes"] = res["modes"]
+
+
+def main():
+    args = parse()
+    ws, rank, local, dist = dist_setup()
+    w = dict(WORKLOADS[args.workload], key=args.workload)
+    if args.impl == "reference":
+        reference_arm(args, w, rank)
+        return
+    import __graft_entry__
+    __graft_entry__.build()
+    import torch
+    torch.cuda.set_device(local)
+    peaks, peak_kind = measured_peaks()
+    if w["kind"] == "ycsb":
+        theta = args.theta if args.theta is not None else w["theta"]
+        res, exact, e2e, batches = ycsb_bench(args, w, theta, dist)
+    else:
+        theta = None
+        res, exact, e2e, batches = tpcc_bench(args, w, dist)
+    rec = workload_record(args, w, theta, dist, res, exact, e2e, batches, peaks, peak_kind)
+    # the TPC-C headline workload beside the YCSB one, with the YCSB run's
+    # access-pattern ceilings for its atomic roofline
+    tp = None
+    if w["kind"] == "ycsb" and not args.no_tpcc:
+        wt = dict(WORKLOADS["tpcc"], key="tpcc")
+        r2, ex2, e2e2, b2 = tpcc_bench(args, wt, dist)
+        r2["ceilings"] = res.get("ceilings")
+        tp = workload_record(args, wt, None, dist, r2, ex2, e2e2, b2, peaks, peak_kind)
+        tp["config"] = bench_config(wt, None)
+        if rank == 0 and not args.no_cpu_baseline:
+            v, s_, c = cpu_baseline_tpcc(wt, b2, args.cpu_batches_tpcc)
+            tp["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
+                                  "sample": f"{min(args.cpu_batches_tpcc, len(b2))} whole batches of "
+                                            f"{wt['n_txn']} txn in order, single-threaded oracle replay, {s_:.1f} s"}
+    sweep = None
+    if w["kind"] == "ycsb" and not args.no_sweep:
+        sweep = {}
+        ws_ = dict(w, n_batches=min(w["n_batches"], 8))
+        for th in [0.0, 0.6, 0.8, 0.99]:
+            r, ex, _, _ = ycsb_bench(args, ws_, th, dist, want_extras=False)
+            t_v = reduce_sum(dist, r[args.mode]["commits"]) / reduce_max(dist, r[args.mode]["secs"])
+            p_v = reduce_sum(dist, r["plain"]["commits"]) / reduce_max(dist, r["plain"]["secs"])
+            sweep[str(th)] = {"tuned": t_v, "plain": p_v, "speedup": t_v / p_v if p_v else None,
+                              "bit_exact_tuned_vs_plain": bool(ex), "launch": r.get("launch")}
+    if rank != 0:
+        return
+    B = w["n_txn"]
+    line = {
+        "metric": "committed txns/s", "value": rec["value"], "unit": "txn/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": bench_config(w, theta),
+        "mode": args.mode, "parallelism": "replicas" if ws > 1 else "single GPU",
+        "plain": rec["plain"],
+        "bit_exact_tuned_vs_plain": rec["bit_exact_tuned_vs_plain"],
+        "commit_rate": rec["commit_rate"],
+        "roofline": rec["roofline"],
+        "e2e": rec["e2e"],
+        "gpu_launches": rec["gpu_launches"],
+        "launch": rec["launch"],
+        "clocks": rec["clocks"],
+    }
+    if rec.get("modes"):
+        line["modes"] = rec["modes"]
     if not args.no_cpu_baseline:
         if w["kind"] == "ycsb":
             v, s, c = cpu_baseline_ycsb(w, batches, args.cpu_batches)
@@ -787,21 +930,18 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "txn/s", "cores": 1, "kind": "port",
                                 "sample": f"{min(args.cpu_batches, len(batches))} whole batches of {B} txn in order, "
                                           f"single-threaded oracle replay, {s:.1f} s"}
+    if tp is not None:
+        line["tpcc"] = tp
+    if sweep is not None:
+        line["theta_sweep"] = sweep
     if not args.no_predictor and w["kind"] == "ycsb" and w["n_txn"] >= (1 << 18):
         line["predictor"] = predictor_section(w, batches)
     if not args.no_reference_gpu and args.workload == "ycsb_hc":
-        line["reference_shapes"] = engine_on_ref_shapes(200)
+        line["reference_shapes"] = engine_on_ref_shapes(200, args.ref_scale_iters)
     if not args.no_serving and args.workload == "ycsb_hc":
         line["serving"] = serving_section(args)
     if not args.no_device_gen and args.workload in ("ycsb_hc", "tpcc", "tpcc_mix"):
         line["device_generator"] = device_gen_section(w)
-    if args.sweep and w["kind"] == "ycsb":
-        sweep = {}
-        for th in [0.0, 0.6, 0.8, 0.99]:
-            r, ex, _, _ = ycsb_bench(args, w, th, None, want_extras=False)
-            sweep[str(th)] = {"tuned": r[args.mode]["commits"] / r[args.mode]["secs"],
-                              "plain": r["plain"]["commits"] / r["plain"]["secs"]}
-        line["theta_sweep"] = sweep
     print(json.dumps(line), flush=True)
 
 

@@ -368,7 +368,9 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
  * Launch shape of the tuned kernels of one workload; the autotuner writes it.
  * None of these settings can change a commit decision or the table image.
  * Defaults: 256 threads (TPC-C 128), 1 op per thread, occupancy, 4 ways,
- * filter 1, dedupe 0, late_reads 0.
+ * filter 1, dedupe 0, late_reads 0.  The reference fixes its block sizes at
+ * compile time (TF/Predefine.h:36-46) and sweeps them with scripts; here the
+ * autotuner (ltpg_gb300/tune.py) searches them per workload.
  * late_reads (YCSB, strides <= 32): the execute kernel only registers; the
  * check kernel reads the rows of committed transactions once their commit
  * decision is made, and a third kernel stores the updates.  Commit decisions,
@@ -376,8 +378,9 @@ int ltpg_commit_bitmap_device(ltpg_ctx *ctx, uint32_t slot, const uint32_t **dev
  * an aborted transaction's result is 0 (its reads are void: it runs again in
  * a later batch).  It saves the row reads of aborted transactions. */
 typedef struct {
-    uint32_t block_threads;   /* threads per block, multiple of 32, <= 512 (YCSB;
-                                 the tuned TPC-C kernels use 128)               */
+    uint32_t block_threads;   /* threads per block of the tuned kernels: 128, 256
+                                 or 512 (TPC-C: tiles of 64, 128 or 256
+                                 transactions)                                  */
     uint32_t ops_per_thread;  /* YCSB op words per thread: 1, 2, 4 or 8         */
     uint32_t blocks_per_sm;   /* cap on resident blocks per SM, 0 = occupancy   */
     uint32_t stage_ways;      /* shared-memory staging entries per hot bucket   */
@@ -385,7 +388,9 @@ typedef struct {
     uint32_t dedupe;          /* 1 = one atomic per key per warp (match_any; TPC-C: header ops) */
     uint32_t late_reads;      /* YCSB: rows read after the check (see above):
                                  1 = in the check kernel's tiles, 2 = in a kernel
-                                 of their own */
+                                 of their own, 3 = write-first registration
+                                 (updates register first; a read loads its
+                                 key's slot only when an update writes the key) */
 } ltpg_launch;
 int ltpg_set_launch(ltpg_ctx *ctx, int workload, const ltpg_launch *cfg);
 int ltpg_get_launch(ltpg_ctx *ctx, int workload, ltpg_launch *cfg);
@@ -543,15 +548,6 @@ int ltpg_debug_get_epoch(ltpg_ctx *ctx, uint32_t *epoch);
 int ltpg_debug_noalloc_set_epoch(int device, uint32_t epoch);
 int ltpg_debug_noalloc_get_epoch(int device, uint32_t *epoch);
 int ltpg_debug_barrier(ltpg_ctx *ctx, uint64_t limit_ns, uint32_t skip_block);
-
-/* ---- access-pattern ceilings --------------------------------------------------
- * Runs one access pattern of the engine's kernels alone and reports its rate:
- * kind 0 streaming copy (bytes/s, read + write), 1 random 80-byte row reads by
- * one thread per row (useful bytes/s), 2 the same with five lanes per row,
- * 3 random 16-byte slot loads (loads/s), 4 atomicMin on random slots
- * (atomics/s), 5 atomicMin on one slot (atomics/s).  n_items = rows, loads or
- * atomics per launch (kind 0: 16-byte elements); iters = timed launches. */
-int ltpg_microbench(ltpg_ctx *ctx, int kind, uint64_t n_items, uint32_t iters, double *rate);
 
 /* ---- hashing used by generators and the table image --------------------- */
 uint64_t ltpg_splitmix64(uint64_t x);

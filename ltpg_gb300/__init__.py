@@ -44,6 +44,25 @@ def lib():
     return _lib
 
 
+BENCH_LIB_PATH = os.path.join(HERE, "libltpg_bench.so")
+_bench_lib = None
+
+
+def bench_lib():
+    """The measurement-only library (access-pattern ceilings), built beside libltpg.so."""
+    global _bench_lib
+    if _bench_lib is None:
+        if not os.path.exists(BENCH_LIB_PATH):
+            raise ImportError(f"{BENCH_LIB_PATH} is missing: run `python -m ltpg_gb300.build` first")
+        L = C.CDLL(BENCH_LIB_PATH)
+        for name, (res, args) in abi.BENCH_SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _bench_lib = L
+    return _bench_lib
+
+
 def _p(a):
     return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
 
@@ -234,6 +253,7 @@ class Engine:
         if code != abi.OK:
             raise LtpgError(code, "ltpg_create failed")
         self._h = h
+        self.device = device
         self.n_slots = n_slots
         self.max_txn = max_txn
 
@@ -469,9 +489,13 @@ class Engine:
                   "red_hot": 5, "h2d_kernel": 6, "h2d_copy": 7}
 
     def microbench(self, kind, n_items, iters=5):
-        """Rate of one access pattern alone (see ltpg_microbench in include/ltpg.h)."""
+        """Rate of one access pattern alone on this engine's device and stream
+        (ltpg_microbench in include/ltpg_bench.h, from libltpg_bench.so)."""
         out = C.c_double()
-        self._ck(lib().ltpg_microbench(self._h, self.MICROBENCH[kind], n_items, iters, C.byref(out)))
+        code = bench_lib().ltpg_microbench(self.device, self.stream(), self.MICROBENCH[kind], n_items, iters,
+                                           C.byref(out))
+        if code:
+            raise LtpgError(code, f"microbench {kind} failed")
         return out.value
 
     def set_profiling(self, on=True):

@@ -162,9 +162,14 @@ SIGNATURES = {
     "ltpg_debug_noalloc_set_epoch": (C.c_int, [C.c_int, U32]),
     "ltpg_debug_noalloc_get_epoch": (C.c_int, [C.c_int, C.POINTER(U32)]),
     "ltpg_debug_barrier": (C.c_int, [P, U64, U32]),
-    "ltpg_microbench": (C.c_int, [P, C.c_int, U64, U32, C.POINTER(C.c_double)]),
     "ltpg_splitmix64": (U64, [U64]),
     "ltpg_hash3": (U64, [U64, U64, U64]),
+}
+
+
+# libltpg_bench.so (include/ltpg_bench.h): measurement only
+BENCH_SIGNATURES = {
+    "ltpg_microbench": (C.c_int, [C.c_int, P, C.c_int, U64, U32, C.POINTER(C.c_double)]),
 }
 
 

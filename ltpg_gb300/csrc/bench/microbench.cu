@@ -6,10 +6,14 @@
 // pattern alone over buffers as large as the real ones, so the measured rate
 // is the practical roofline of that pattern (a streaming copy is included as
 // the HBM reference).  Buffers are allocated per call.
+//
+// Measurement only: built into libltpg_bench.so, which bench.py loads; the
+// engine library (libltpg.so) does not contain it.
 #include <cstring>
 #include <vector>
 
-#include "devutil.cuh"
+#include "../../../include/ltpg_bench.h"
+#include "../devutil.cuh"
 
 namespace ltpg {
 
@@ -112,9 +116,13 @@ __global__ void mb_red_hot(RegSlot *slots, uint64_t n_ops) {
 
 using namespace ltpg;
 
-extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t iters, double *rate) {
-    if (!c || !rate || iters == 0 || n_items == 0) return LTPG_ERR_INVALID;
-    if (cudaSetDevice(c->device) != cudaSuccess) return LTPG_ERR_CUDA;
+extern "C" int ltpg_microbench(int device, void *stream_ptr, int kind, uint64_t n_items, uint32_t iters,
+                               double *rate) {
+    if (!rate || iters == 0 || n_items == 0 || kind < 0 || kind > 7) return LTPG_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return LTPG_ERR_CUDA;
+    int sm_count = 0;
+    if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return LTPG_ERR_CUDA;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
     const uint64_t n_rows = 10000000ull, n_slots = 10000000ull;
     void *buf_a = nullptr, *buf_b = nullptr;
     unsigned long long *sink = nullptr;
@@ -132,14 +140,14 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
     cudaError_t e = cudaMalloc(&buf_a, bytes_a);
     if (e == cudaSuccess && bytes_b) e = cudaMalloc(&buf_b, bytes_b);
     if (e == cudaSuccess) e = cudaMalloc(&sink, 8);
-    if (e == cudaSuccess) e = cudaMemsetAsync(buf_a, 0x5A, bytes_a, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(buf_a, 0x5A, bytes_a, stream);
     if (e != cudaSuccess) {
         cudaFree(buf_a);
         cudaFree(buf_b);
         cudaFree(sink);
         return LTPG_ERR_NOMEM;
     }
-    const int grid = c->sm_count * 8, block = 256;
+    const int grid = sm_count * 8, block = 256;
     cudaEvent_t ev0, ev1;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -151,32 +159,32 @@ extern "C" int ltpg_microbench(ltpg_ctx *c, int kind, uint64_t n_items, uint32_t
         const int U = unrolls[ui];
         auto launch = [&]() {
             switch (kind) {
-            case 0: mb_copy<<<grid, block, 0, c->stream>>>((const ulonglong2 *)buf_a, (ulonglong2 *)buf_b, n_items); break;
+            case 0: mb_copy<<<grid, block, 0, stream>>>((const ulonglong2 *)buf_a, (ulonglong2 *)buf_b, n_items); break;
             case 1:
-                if (U == 1) mb_gather_thread<1><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
-                else if (U == 4) mb_gather_thread<4><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
-                else mb_gather_thread<8><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                if (U == 1) mb_gather_thread<1><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                else if (U == 4) mb_gather_thread<4><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                else mb_gather_thread<8><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
                 break;
             case 2:
-                if (U == 1) mb_gather_coop<1><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
-                else if (U == 4) mb_gather_coop<4><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
-                else mb_gather_coop<8><<<grid, block, 0, c->stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                if (U == 1) mb_gather_coop<1><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                else if (U == 4) mb_gather_coop<4><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
+                else mb_gather_coop<8><<<grid, block, 0, stream>>>((const uint64_t *)buf_a, n_rows, n_items, sink);
                 break;
             case 3:
-                if (U == 1) mb_slot_load<1><<<grid, block, 0, c->stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
-                else if (U == 4) mb_slot_load<4><<<grid, block, 0, c->stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
-                else mb_slot_load<8><<<grid, block, 0, c->stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
+                if (U == 1) mb_slot_load<1><<<grid, block, 0, stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
+                else if (U == 4) mb_slot_load<4><<<grid, block, 0, stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
+                else mb_slot_load<8><<<grid, block, 0, stream>>>((const RegSlot *)buf_a, n_slots, n_items, sink);
                 break;
-            case 4: mb_red_random<<<grid, block, 0, c->stream>>>((RegSlot *)buf_a, n_slots, n_items); break;
-            case 6: mb_h2d_kernel<<<grid, block, 0, c->stream>>>((const uint4 *)host, (uint4 *)buf_b, n_items); break;
-            case 7: cudaMemcpyAsync(buf_b, host, n_items * 16, cudaMemcpyHostToDevice, c->stream); break;
-            default: mb_red_hot<<<grid, block, 0, c->stream>>>((RegSlot *)buf_a, n_items); break;
+            case 4: mb_red_random<<<grid, block, 0, stream>>>((RegSlot *)buf_a, n_slots, n_items); break;
+            case 6: mb_h2d_kernel<<<grid, block, 0, stream>>>((const uint4 *)host, (uint4 *)buf_b, n_items); break;
+            case 7: cudaMemcpyAsync(buf_b, host, n_items * 16, cudaMemcpyHostToDevice, stream); break;
+            default: mb_red_hot<<<grid, block, 0, stream>>>((RegSlot *)buf_a, n_items); break;
             }
         };
         launch();  // warm
-        cudaEventRecord(ev0, c->stream);
+        cudaEventRecord(ev0, stream);
         for (uint32_t i = 0; i < iters; ++i) launch();
-        cudaEventRecord(ev1, c->stream);
+        cudaEventRecord(ev1, stream);
         e = cudaEventSynchronize(ev1);
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);

@@ -186,7 +186,7 @@ int ltpg_create(const ltpg_config *cfg, ltpg_ctx **out) {
     }
     c->stream = c->own_stream;
     c->slots.resize(cfg->n_slots);
-    c->launch_c.block = 128;  // the tuned TPC-C kernels' fixed block (64-transaction tiles)
+    c->launch_c.block = 128;  // the tuned TPC-C kernels' default block (64-transaction tiles)
     *out = c;
     return LTPG_OK;
 }
@@ -771,8 +771,8 @@ int ltpg_set_launch(ltpg_ctx *c, int workload, const ltpg_launch *cfg) {
     if (!c || !cfg) return LTPG_ERR_INVALID;
     if (workload != LTPG_WORKLOAD_YCSB && workload != LTPG_WORKLOAD_TPCC)
         return fail(c, LTPG_ERR_INVALID, "unknown workload");
-    if (cfg->block_threads % 32 || cfg->block_threads < 32 || cfg->block_threads > 512)
-        return fail(c, LTPG_ERR_INVALID, "block_threads must be a multiple of 32 in [32, 512]");
+    if (cfg->block_threads != 128 && cfg->block_threads != 256 && cfg->block_threads != 512)
+        return fail(c, LTPG_ERR_INVALID, "block_threads in {128, 256, 512}");
     const uint32_t opt = cfg->ops_per_thread;
     if (opt != 1 && opt != 2 && opt != 4 && opt != 8) return fail(c, LTPG_ERR_INVALID, "ops_per_thread in {1, 2, 4, 8}");
     if (cfg->stage_ways < 1 || cfg->stage_ways > 8) return fail(c, LTPG_ERR_INVALID, "stage_ways in [1, 8]");

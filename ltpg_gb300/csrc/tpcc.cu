@@ -217,10 +217,10 @@ __device__ __forceinline__ bool resolve_by_name(const TpccDev &db, ltpg_tpcc_txn
 }
 
 constexpr uint32_t PT = 64;    // transactions per tile (plain path)
-constexpr uint32_t PTT = 64;   // transactions per tile (tuned path)
 constexpr uint32_t PBS = 256;  // threads per block (plain path)
-constexpr uint32_t TBS = 128;  // threads per block (tuned path): 64-transaction tiles, so a
-                               // tile's barriers hold 4 warps, not 8
+// Tuned path: a block of 2P threads walks tiles of P transactions; P = 64
+// (128-thread blocks, so a tile's barriers hold 4 warps) by default, 128 or
+// 256 by the launch setting block_threads (256 / 512).
 
 template <uint32_t N>
 struct TileHdrN {
@@ -229,7 +229,6 @@ struct TileHdrN {
     uint32_t ok[N];
 };
 using TileHdr = TileHdrN<PT>;
-using TileHdrT = TileHdrN<PTT>;
 
 // Loads a tile and lays out its ops (n_ops_of = ops per transaction).
 template <class H, class F>
@@ -649,14 +648,16 @@ __device__ __forceinline__ void tuned_register(const TpccTunedArgs &a, bool vali
 
 // Order line e of a tile whose line prefix is h.off: owner transaction and
 // the line's index within it.
-__device__ __forceinline__ void tile_line(const TileHdrT &h, uint32_t nt, uint32_t e, uint32_t &i, uint32_t &li) {
+template <class H>
+__device__ __forceinline__ void tile_line(const H &h, uint32_t nt, uint32_t e, uint32_t &i, uint32_t &li) {
     i = tile_owner(h, nt, e);
     li = e - h.off[i];
 }
 
 // Loads a tile, lays out its order lines and returns their number; hk = header
 // lanes per transaction (4 if the tile holds a Delivery, else 3).
-__device__ __forceinline__ uint32_t load_tile_lines(TileHdrT &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
+template <class H>
+__device__ __forceinline__ uint32_t load_tile_lines(H &h, const TpccTunedArgs &a, uint32_t t0, uint32_t nt,
                                                     uint32_t n_lines, uint32_t &hk) {
     const uint32_t total = load_tile(h, a.txns, t0, nt, a.db, n_lines, a.ctl, [&](uint32_t i) {
         return (h.ok[i] && tpcc_kind(h.x[i].kind_info) == LTPG_TPCC_NEWORDER) ? tpcc_ol_cnt(h.x[i].kind_info) : 0u;
@@ -676,7 +677,8 @@ struct TileItem {
     ltpg_tpcc_line ln;
     TpccOp op;
 };
-__device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const TileHdrT &h, uint32_t nt, uint32_t hk,
+template <class H>
+__device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const H &h, uint32_t nt, uint32_t hk,
                                               uint32_t e, uint32_t n_items, uint32_t t0, bool report) {
     TileItem it{0, 0, 0, false, false, false, {0, 0, 0}, {0, 0, 0}};
     if (e >= n_items) return it;
@@ -698,16 +700,17 @@ __device__ __forceinline__ TileItem tile_item(const TpccTunedArgs &a, const Tile
     return it;
 }
 
-__device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT &h, uint64_t tag) {
+template <uint32_t P>
+__device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrN<P> &h, uint64_t tag) {
     const uint32_t n_lines = (uint32_t)a.hdr[0];
-    __shared__ unsigned long long sum[PTT];
-    __shared__ uint32_t wtax[PTT], dtax[PTT], disc[PTT];
-    __shared__ long long res[PTT];
+    __shared__ unsigned long long sum[P];
+    __shared__ uint32_t wtax[P], dtax[P], disc[P];
+    __shared__ long long res[P];
     const bool filt = a.filter != 0u;
-    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
+    const uint32_t n_tiles = (a.B + P - 1) / P;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
-        if (threadIdx.x < PTT) sum[threadIdx.x] = 0ull;
+        const uint32_t t0 = tile * P, nt = min(P, a.B - t0);
+        if (threadIdx.x < P) sum[threadIdx.x] = 0ull;
         uint32_t hk;
         const uint32_t lines_n = load_tile_lines(h, a, t0, nt, n_lines, hk);
         const uint32_t n_items = hk * nt + lines_n;
@@ -756,17 +759,18 @@ __device__ __forceinline__ void tpcc_exec_tiles(const TpccTunedArgs &a, TileHdrT
 }
 
 // hot: 11 W int64 sums in shared memory (W <= HOT_SMEM_MAX_W), or null.
-__device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdrT &h, uint32_t epoch,
+template <uint32_t P>
+__device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileHdrN<P> &h, uint32_t epoch,
                                                    long long *hot) {
     const uint32_t n_lines = (uint32_t)a.hdr[0];
     const uint64_t txn_base = a.hdr[1];
-    __shared__ uint32_t fl[PTT];
+    __shared__ uint32_t fl[P];
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
+    const uint32_t n_tiles = (a.B + P - 1) / P;
     unsigned long long c_com = 0, c_raw = 0, c_war = 0, c_waw = 0;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const uint32_t t0 = tile * PTT, nt = min(PTT, a.B - t0);
-        if (threadIdx.x < PTT) fl[threadIdx.x] = 0u;
+        const uint32_t t0 = tile * P, nt = min(P, a.B - t0);
+        if (threadIdx.x < P) fl[threadIdx.x] = 0u;
         uint32_t hk;
         const uint32_t lines_n = load_tile_lines(h, a, t0, nt, n_lines, hk);
         const uint32_t n_items = hk * nt + lines_n;
@@ -794,7 +798,7 @@ __device__ __forceinline__ void tpcc_checkwb_tiles(const TpccTunedArgs &a, TileH
             if (f) atomicOr(&fl[it.i], f);
         }
         __syncthreads();
-        if (threadIdx.x < PTT) {
+        if (threadIdx.x < P) {
             uint32_t f = threadIdx.x < nt ? fl[threadIdx.x] : 0u;
             const bool com = threadIdx.x < nt && h.ok[threadIdx.x] && commits(f);
             if (com) f |= LTPG_FLAG_COMMIT;
@@ -864,17 +868,19 @@ __device__ __forceinline__ void hot_flush(const TpccDev &db, const long long *ho
     }
 }
 
-__global__ void __launch_bounds__(TBS) tpcc_exec_tuned(TpccTunedArgs a) {
-    __shared__ TileHdrT h;
-    tpcc_exec_tiles(a, h, slot_tag(a.ctl->epoch));
+template <uint32_t P>
+__global__ void __launch_bounds__(2 * P) tpcc_exec_tuned(TpccTunedArgs a) {
+    __shared__ TileHdrN<P> h;
+    tpcc_exec_tiles<P>(a, h, slot_tag(a.ctl->epoch));
 }
 
-__global__ void __launch_bounds__(TBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
-    __shared__ TileHdrT h;
+template <uint32_t P>
+__global__ void __launch_bounds__(2 * P) tpcc_checkwb_tuned(TpccTunedArgs a) {
+    __shared__ TileHdrN<P> h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
     if (hot) hot_init(hot, 11u * a.db.W);
-    tpcc_checkwb_tiles(a, h, a.ctl->epoch, hot);
+    tpcc_checkwb_tiles<P>(a, h, a.ctl->epoch, hot);
     if (hot) hot_flush(a.db, hot);
     finish_batch(a.ctl);
 }
@@ -887,16 +893,53 @@ __global__ void __launch_bounds__(TBS) tpcc_checkwb_tuned(TpccTunedArgs a) {
 // row is written; the second phase's read-modify-writes (C_BALANCE,
 // S_QUANTITY by atomicCAS) touch rows that one committed transaction writes
 // (WAW), whose batch-start value is what they must see.
-__global__ void __launch_bounds__(TBS) tpcc_persistent(TpccTunedArgs a) {
-    __shared__ TileHdrT h;
+template <uint32_t P>
+__global__ void __launch_bounds__(2 * P) tpcc_persistent(TpccTunedArgs a) {
+    __shared__ TileHdrN<P> h;
     extern __shared__ __align__(16) long long hot_dyn[];
     long long *hot = a.db.W <= HOT_SMEM_MAX_W ? hot_dyn : nullptr;
     const uint32_t epoch = a.ctl->epoch;
     if (hot) hot_init(hot, 11u * a.db.W);
-    tpcc_exec_tiles(a, h, slot_tag(epoch));
-    if (grid_barrier(a.ctl)) tpcc_checkwb_tiles(a, h, epoch, hot);
+    tpcc_exec_tiles<P>(a, h, slot_tag(epoch));
+    if (grid_barrier(a.ctl)) tpcc_checkwb_tiles<P>(a, h, epoch, hot);
     if (hot) hot_flush(a.db, hot);
     finish_batch(a.ctl);
+}
+
+template <uint32_t P>
+static cudaError_t tpcc_launch_tuned(ltpg_ctx *c, const TpccTunedArgs &a_in, int mode) {
+    TpccTunedArgs a = a_in;
+    constexpr uint32_t threads = 2 * P;
+    const size_t smem = a.db.W <= HOT_SMEM_MAX_W ? 11u * a.db.W * sizeof(long long) : 0u;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, mode == LTPG_MODE_PERSISTENT ? (const void *)tpcc_persistent<P> : (const void *)tpcc_checkwb_tuned<P>,
+        threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (c->launch_c.blocks_per_sm && (int)c->launch_c.blocks_per_sm < per_sm) per_sm = (int)c->launch_c.blocks_per_sm;
+    const uint32_t n_tiles = (a.B + P - 1) / P;
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm * c->sm_count));
+    if (mode == LTPG_MODE_PERSISTENT) {
+        prof_mark(c, 0);
+        void *args[] = {&a};
+        count_launch(c);
+        e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent<P>, dim3(grid), dim3(threads), args, smem,
+                                        c->stream);
+        if (e != cudaSuccess) return e;
+        for (int m = 1; m < PROF_MARKS; ++m) prof_mark(c, m);
+        return cudaSuccess;
+    }
+    prof_mark(c, 0);
+    count_launch(c);
+    tpcc_exec_tuned<P><<<grid, threads, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 1);
+    count_launch(c);
+    tpcc_checkwb_tuned<P><<<grid, threads, smem, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    for (int m = 2; m < PROF_MARKS; ++m) prof_mark(c, m);
+    return cudaSuccess;
 }
 
 cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
@@ -915,38 +958,14 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.ctl = c->ctl;
     a.filter = c->launch_c.filter;
     a.dedupe = c->launch_c.dedupe;
-    const size_t smem = a.db.W <= HOT_SMEM_MAX_W ? 11u * a.db.W * sizeof(long long) : 0u;
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);
     if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mode == LTPG_MODE_PERSISTENT
-                                                                  ? (const void *)tpcc_persistent
-                                                                  : (const void *)tpcc_checkwb_tuned,
-                                                      TBS, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    if (c->launch_c.blocks_per_sm && (int)c->launch_c.blocks_per_sm < per_sm) per_sm = (int)c->launch_c.blocks_per_sm;
-    const uint32_t n_tiles = (a.B + PTT - 1) / PTT;
-    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(per_sm * c->sm_count));
-    if (mode == LTPG_MODE_PERSISTENT) {
-        prof_mark(c, 0);
-        void *args[] = {&a};
-        count_launch(c);
-        e = cudaLaunchCooperativeKernel((const void *)tpcc_persistent, dim3(grid), dim3(TBS), args, smem, c->stream);
-        if (e != cudaSuccess) return e;
-        for (int m = 1; m < PROF_MARKS; ++m) prof_mark(c, m);
-        return cudaSuccess;
+    // block_threads 128 / 256 / 512: tiles of 64 / 128 / 256 transactions
+    switch (c->launch_c.block) {
+    case 256: return tpcc_launch_tuned<128>(c, a, mode);
+    case 512: return tpcc_launch_tuned<256>(c, a, mode);
+    default: return tpcc_launch_tuned<64>(c, a, mode);
     }
-    prof_mark(c, 0);
-    count_launch(c);
-    tpcc_exec_tuned<<<grid, TBS, 0, c->stream>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_mark(c, 1);
-    count_launch(c);
-    tpcc_checkwb_tuned<<<grid, TBS, smem, c->stream>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    for (int m = 2; m < PROF_MARKS; ++m) prof_mark(c, m);
-    return cudaSuccess;
 }
 
 }  // namespace ltpg

@@ -19,6 +19,7 @@
 //     decision, and a third kernel stores the updates, so that no aborted
 //     transaction's rows are read.
 #include <mutex>
+#include <type_traits>
 #include <unordered_map>
 
 #include "stage.cuh"
@@ -299,7 +300,13 @@ __device__ __forceinline__ void late_read_loop(const YcsbTunedArgs &a) {
     }
 }
 
-__global__ void __launch_bounds__(256) ycsb_read_late(YcsbTunedArgs a) { late_read_loop<false>(a); }
+// The grid-stride kernels below are instantiated per block size (BS = 128,
+// 256, 512: launch setting block_threads), each with launch bounds of its own
+// block: bounds above the block change the compiler's register choice (the
+// read kernel takes 58 registers under 512-thread bounds against 40 under
+// 256, and loses a third of its resident warps).
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_read_late(YcsbTunedArgs a) { late_read_loop<false>(a); }
 
 // ---- write-first registration (late_reads = 3) ---------------------------------
 // The same RAW / WAR / WAW outcome with at most one random slot access per op
@@ -464,11 +471,14 @@ __device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch)
     }
 }
 
-__global__ void __launch_bounds__(256) ycsb_wf_writes(YcsbTunedArgs a) {
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_writes(YcsbTunedArgs a) {
     wf_register_writes<false>(a, slot_tag(a.ctl->epoch));
 }
-__global__ void __launch_bounds__(256) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads<false>(a, a.ctl->epoch); }
-__global__ void __launch_bounds__(256) ycsb_wf_check(YcsbTunedArgs a) { wf_check<false>(a, a.ctl->epoch); }
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads<false>(a, a.ctl->epoch); }
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_check(YcsbTunedArgs a) { wf_check<false>(a, a.ctl->epoch); }
 
 // ---- check + write-back over all tiles assigned to this block ------------------
 // fl: tile flags.  kLate = 0: the third pass stores the committed updates;
@@ -590,8 +600,8 @@ struct OpVec<4> {
     }
 };
 
-template <int OPS, bool kStage, bool kFilter, bool kDedupe>
-__global__ void __launch_bounds__(256) ycsb_exec_fast(YcsbTunedArgs a, uint32_t lpt) {
+template <int OPS, bool kStage, bool kFilter, bool kDedupe, int BS>
+__global__ void __launch_bounds__(BS) ycsb_exec_fast(YcsbTunedArgs a, uint32_t lpt) {
     extern __shared__ __align__(16) char smem[];
     StageEnt *tab = reinterpret_cast<StageEnt *>(smem);
     const uint64_t tag = slot_tag(a.ctl->epoch);
@@ -848,8 +858,8 @@ __device__ __forceinline__ void coop_exec_loop(const YcsbTunedArgs &a, StageEnt 
     }
 }
 
-template <bool kStage, bool kFilter, bool kDedupe, bool kReads>
-__global__ void __launch_bounds__(256) ycsb_exec_coop(YcsbTunedArgs a) {
+template <bool kStage, bool kFilter, bool kDedupe, bool kReads, int BS>
+__global__ void __launch_bounds__(BS) ycsb_exec_coop(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     uint32_t *sbits = reinterpret_cast<uint32_t *>(smem);
     uint32_t *srank = sbits + STAGE_WORDS;
@@ -964,8 +974,8 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     }
 }
 
-template <bool kDecide>
-__global__ void __launch_bounds__(256) ycsb_writeback_late(YcsbTunedArgs a) {
+template <bool kDecide, int BS>
+__global__ void __launch_bounds__(BS) ycsb_writeback_late(YcsbTunedArgs a) {
     writeback_late_loop<kDecide, false>(a);
     finish_batch(a.ctl);
 }
@@ -1041,6 +1051,17 @@ static size_t static_smem(const void *k) {
     return v;
 }
 
+// Calls f with std::integral_constant<int, BS> for the launch's block size
+// (128, 256 or 512; ltpg_set_launch admits no other).
+template <class F>
+static auto with_block(uint32_t block, F f) {
+    switch (block) {
+    case 128: return f(std::integral_constant<int, 128>());
+    case 512: return f(std::integral_constant<int, 512>());
+    default: return f(std::integral_constant<int, 256>());
+    }
+}
+
 // Transactions per tile: as many whole transactions as the block reads with
 // `per_thread` 16-byte vectors per thread, rounded down to a multiple of 32.
 static uint32_t tuned_tile(uint32_t stride, uint32_t threads, uint32_t per_thread) {
@@ -1051,44 +1072,45 @@ static uint32_t tuned_tile(uint32_t stride, uint32_t threads, uint32_t per_threa
 
 // Launches the barrier-free execute kernel when stride / ops-per-thread is a
 // power of two <= 32; returns false (nothing launched) otherwise.
-template <int OPS>
+template <int OPS, int BS>
 static void launch_fast_t(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, uint32_t lpt) {
     const LaunchCfg &L = c->launch_y;
     const size_t smem = stage ? (size_t)a.stage_entries * sizeof(StageEnt) : 0;
     void (*k)(YcsbTunedArgs, uint32_t);
     const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
     switch (sel) {
-    case 0: k = ycsb_exec_fast<OPS, false, false, false>; break;
-    case 1: k = ycsb_exec_fast<OPS, false, false, true>; break;
-    case 2: k = ycsb_exec_fast<OPS, false, true, false>; break;
-    case 3: k = ycsb_exec_fast<OPS, false, true, true>; break;
-    case 4: k = ycsb_exec_fast<OPS, true, false, false>; break;
-    case 5: k = ycsb_exec_fast<OPS, true, false, true>; break;
-    case 6: k = ycsb_exec_fast<OPS, true, true, false>; break;
-    default: k = ycsb_exec_fast<OPS, true, true, true>; break;
+    case 0: k = ycsb_exec_fast<OPS, false, false, false, BS>; break;
+    case 1: k = ycsb_exec_fast<OPS, false, false, true, BS>; break;
+    case 2: k = ycsb_exec_fast<OPS, false, true, false, BS>; break;
+    case 3: k = ycsb_exec_fast<OPS, false, true, true, BS>; break;
+    case 4: k = ycsb_exec_fast<OPS, true, false, false, BS>; break;
+    case 5: k = ycsb_exec_fast<OPS, true, false, true, BS>; break;
+    case 6: k = ycsb_exec_fast<OPS, true, true, false, BS>; break;
+    default: k = ycsb_exec_fast<OPS, true, true, true, BS>; break;
     }
     if (smem + static_smem((const void *)k) > 48 * 1024)
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint32_t threads = BS;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, (int)threads, smem);
     if (per_sm < 1) per_sm = 1;
     if (L.blocks_per_sm && (int)L.blocks_per_sm < per_sm) per_sm = (int)L.blocks_per_sm;
     const uint64_t nv = (uint64_t)a.B * lpt;
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((nv + 255) / 256, (uint64_t)per_sm * c->sm_count);
-    k<<<grid, 256, smem, c->stream>>>(a, lpt);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nv + threads - 1) / threads, (uint64_t)per_sm * c->sm_count);
+    k<<<grid, threads, smem, c->stream>>>(a, lpt);
 }
 
-template <bool kReads>
+template <bool kReads, int BS>
 static void (*coop_kernel(int sel))(YcsbTunedArgs) {
     switch (sel) {
-    case 0: return ycsb_exec_coop<false, false, false, kReads>;
-    case 1: return ycsb_exec_coop<false, false, true, kReads>;
-    case 2: return ycsb_exec_coop<false, true, false, kReads>;
-    case 3: return ycsb_exec_coop<false, true, true, kReads>;
-    case 4: return ycsb_exec_coop<true, false, false, kReads>;
-    case 5: return ycsb_exec_coop<true, false, true, kReads>;
-    case 6: return ycsb_exec_coop<true, true, false, kReads>;
-    default: return ycsb_exec_coop<true, true, true, kReads>;
+    case 0: return ycsb_exec_coop<false, false, false, kReads, BS>;
+    case 1: return ycsb_exec_coop<false, false, true, kReads, BS>;
+    case 2: return ycsb_exec_coop<false, true, false, kReads, BS>;
+    case 3: return ycsb_exec_coop<false, true, true, kReads, BS>;
+    case 4: return ycsb_exec_coop<true, false, false, kReads, BS>;
+    case 5: return ycsb_exec_coop<true, false, true, kReads, BS>;
+    case 6: return ycsb_exec_coop<true, true, false, kReads, BS>;
+    default: return ycsb_exec_coop<true, true, true, kReads, BS>;
     }
 }
 
@@ -1097,56 +1119,68 @@ static void launch_coop(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage, bool re
     const LaunchCfg &L = c->launch_y;
     const size_t smem = stage ? 2 * STAGE_WORDS * sizeof(uint32_t) + (size_t)a.stage_entries * sizeof(StageEnt) : 0;
     const int sel = (stage ? 4 : 0) | (L.filter ? 2 : 0) | (L.dedupe ? 1 : 0);
-    void (*k)(YcsbTunedArgs) = reads ? coop_kernel<true>(sel) : coop_kernel<false>(sel);
+    void (*k)(YcsbTunedArgs) = with_block(L.block, [&](auto bs) {
+        constexpr int BS = decltype(bs)::value;
+        return reads ? coop_kernel<true, BS>(sel) : coop_kernel<false, BS>(sel);
+    });
     if (smem + static_smem((const void *)k) > 48 * 1024)
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint32_t threads = L.block;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, (int)threads, smem);
     if (per_sm < 1) per_sm = 1;
     if (L.blocks_per_sm && (int)L.blocks_per_sm < per_sm) per_sm = (int)L.blocks_per_sm;
     const uint64_t nw = (uint64_t)a.B * a.lpt;
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((nw + 255) / 256, (uint64_t)per_sm * c->sm_count);
-    k<<<grid, 256, smem, c->stream>>>(a);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nw + threads - 1) / threads, (uint64_t)per_sm * c->sm_count);
+    k<<<grid, threads, smem, c->stream>>>(a);
 }
 
-// Grid of a 256-thread grid-stride kernel over `items` lanes: at most the
-// blocks that fit on the GPU at once (blocks_per_sm caps them when set).
+// Grid of a grid-stride kernel of block_threads threads over `items` lanes:
+// at most the blocks that fit on the GPU at once (blocks_per_sm caps them
+// when set).
 static uint32_t stride_grid(ltpg_ctx *c, const void *k, uint64_t items) {
+    const uint32_t threads = c->launch_y.block;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, (int)threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
     if (c->launch_y.blocks_per_sm && (int)c->launch_y.blocks_per_sm < per_sm) per_sm = (int)c->launch_y.blocks_per_sm;
-    const uint64_t g = std::min<uint64_t>((items + 255) / 256, (uint64_t)per_sm * c->sm_count);
+    const uint64_t g = std::min<uint64_t>((items + threads - 1) / threads, (uint64_t)per_sm * c->sm_count);
     return (uint32_t)std::max<uint64_t>(g, 1);
 }
 
 // Write-first registration (late_reads = 3): write registration, read
 // registration + RAW, WAR / WAW, committed reads, commit decision +
 // write-back.  Profiled as [registration (both), check, reads, write-back].
-static cudaError_t launch_write_first(ltpg_ctx *c, const YcsbTunedArgs &a) {
+template <int BS>
+static cudaError_t launch_write_first_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
     const uint64_t lanes = (uint64_t)a.B * a.lpt;
     prof_mark(c, 0);
     count_launch(c, 2);
-    ycsb_wf_writes<<<stride_grid(c, (const void *)ycsb_wf_writes, (uint64_t)a.B * a.stride / 4), 256, 0,
-                     c->stream>>>(a);
-    ycsb_wf_reads<<<stride_grid(c, (const void *)ycsb_wf_reads, (uint64_t)a.B * a.stride / 4), 256, 0,
-                    c->stream>>>(a);
+    ycsb_wf_writes<BS><<<stride_grid(c, (const void *)ycsb_wf_writes<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
+                         c->stream>>>(a);
+    ycsb_wf_reads<BS><<<stride_grid(c, (const void *)ycsb_wf_reads<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
+                        c->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     prof_mark(c, 1);
     count_launch(c, 2);
-    ycsb_wf_check<<<stride_grid(c, (const void *)ycsb_wf_check, (uint64_t)a.B * a.stride / 4), 256, 0,
-                    c->stream>>>(a);
+    ycsb_wf_check<BS><<<stride_grid(c, (const void *)ycsb_wf_check<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
+                        c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 2);
-    ycsb_read_late<<<stride_grid(c, (const void *)ycsb_read_late, lanes), 256, 0, c->stream>>>(a);
+    ycsb_read_late<BS><<<stride_grid(c, (const void *)ycsb_read_late<BS>, lanes), BS, 0, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 3);
     count_launch(c);
-    ycsb_writeback_late<true>
-        <<<stride_grid(c, (const void *)ycsb_writeback_late<true>, a.B), 256, 0, c->stream>>>(a);
+    ycsb_writeback_late<true, BS>
+        <<<stride_grid(c, (const void *)ycsb_writeback_late<true, BS>, a.B), BS, 0, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 4);
     return predictor_after_batch(c);
+}
+
+static cudaError_t launch_write_first(ltpg_ctx *c, const YcsbTunedArgs &a) {
+    return with_block(c->launch_y.block, [&](auto bs) { return launch_write_first_t<decltype(bs)::value>(c, a); });
 }
 
 // Launch shapes of the execute phase, by ops_per_thread: 1 = cooperative row
@@ -1164,9 +1198,12 @@ static bool launch_fast_exec(ltpg_ctx *c, const YcsbTunedArgs &a, bool stage) {
     if (a.stride % ops) return false;
     const uint32_t lpt = a.stride / ops;
     if (lpt == 0 || lpt > 32 || (lpt & (lpt - 1))) return false;
-    if (ops == 1) launch_fast_t<1>(c, a, stage, lpt);
-    else if (ops == 2) launch_fast_t<2>(c, a, stage, lpt);
-    else launch_fast_t<4>(c, a, stage, lpt);
+    with_block(c->launch_y.block, [&](auto bs) {
+        constexpr int BS = decltype(bs)::value;
+        if (ops == 2) launch_fast_t<2, BS>(c, a, stage, lpt);
+        else launch_fast_t<4, BS>(c, a, stage, lpt);
+        return 0;
+    });
     return true;
 }
 
@@ -1264,25 +1301,23 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     prof_mark(c, 2);
     if (late_mode == 2u) {
         count_launch(c);
-        int per_sm_rd = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rd, ycsb_read_late, 256, 0);
-        if (e != cudaSuccess) return e;
-        if (per_sm_rd < 1) per_sm_rd = 1;
-        const uint64_t nw = (uint64_t)a.B * a.lpt;
-        const uint32_t grid_rd = (uint32_t)std::min<uint64_t>((nw + 255) / 256, (uint64_t)per_sm_rd * c->sm_count);
-        ycsb_read_late<<<grid_rd, 256, 0, c->stream>>>(a);
+        with_block(threads, [&](auto bs) {
+            constexpr int BS = decltype(bs)::value;
+            ycsb_read_late<BS><<<stride_grid(c, (const void *)ycsb_read_late<BS>, (uint64_t)a.B * a.lpt), BS, 0,
+                                 c->stream>>>(a);
+            return 0;
+        });
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     prof_mark(c, 3);
     if (late) {  // the write-back waits for every read of the batch
         count_launch(c);
-        int per_sm_wb = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_wb, ycsb_writeback_late<false>, 256, 0);
-        if (e != cudaSuccess) return e;
-        if (per_sm_wb < 1) per_sm_wb = 1;
-        const uint32_t grid_wb = (uint32_t)std::min<uint64_t>(((uint64_t)a.B + 255) / 256,
-                                                              (uint64_t)per_sm_wb * c->sm_count);
-        ycsb_writeback_late<false><<<grid_wb, 256, 0, c->stream>>>(a);
+        with_block(threads, [&](auto bs) {
+            constexpr int BS = decltype(bs)::value;
+            ycsb_writeback_late<false, BS>
+                <<<stride_grid(c, (const void *)ycsb_writeback_late<false, BS>, a.B), BS, 0, c->stream>>>(a);
+            return 0;
+        });
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     prof_mark(c, 4);

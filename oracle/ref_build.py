@@ -8,8 +8,19 @@ from the reference: its sources are compiled where they lie.
   * <prog>.cubin  — the reference program compiled for sm_103a with
                     `nvcc -cubin` (device code only; its host main is ignored).
                     YCSB/1/ycsb.cu and TPCC-allopt-final/tp.cu, as shipped;
-                    tf50: tp.cu with NEWORDER_PERCENT = 50 (compiled from a
-                    temporary copy outside the repository).
+                    and copies with constants of Predefine.h changed (each
+                    compiled from a temporary copy outside the repository,
+                    the way the reference's own sweep scripts rewrite those
+                    lines, TPCC-allopt-final/tpcc_script.py:18-44):
+                      tf50:   NEWORDER_PERCENT = 50 (32,768 NewOrders +
+                              32,768 Payments);
+                      tf_c3:  BATCH_SIZE = 1,048,576, NEWORDER_PERCENT = 50
+                              (the TPC-C headline batch, W = 64);
+                      y1_c2:  BATCH_SIZE = 1,048,576, YCSB_SIZE = 10,000,000,
+                              16 ops of which 15 reads, uniform mode (the
+                              YCSB high-contention scale; uniform mode drops
+                              the shipped build's key-0 bypass, so every key
+                              registers and is checked).
   * <prog>_layout.json — sizes and field offsets of the reference's buffer
                     structs and its launch constants, printed by a small host
                     program of ours that includes the reference's Predefine.h /
@@ -26,7 +37,8 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = "/root/reference/LTPG"
+# root of the reference project (read-only); the recipe builds nothing when absent
+REF = os.path.join(os.environ.get("LTPG_REFERENCE_ROOT", "/root/reference"), "LTPG")
 NVCC = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
 
 PROGRAMS = {
@@ -87,11 +99,22 @@ int main() {
               "_Z12KERNEL_CHECKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX",
               "_Z16KERNEL_WRITEBACKP12NEWORDER_SETP11PAYMENT_SETP14NEWORDER_QUERYP13PAYMENT_QUERYP3LOGP8SNAPSHOTP5INDEX"]),
 }
-# The same program with half its batch NewOrders: the shipped sources copied to
-# a temporary directory outside the repository, NEWORDER_PERCENT (a const in
-# Predefine.h, so not settable by -D) changed from 0 to 50, compiled there.
-PROGRAMS["tf50"] = dict(PROGRAMS["tf"], patch=("Predefine.h", r"NEWORDER_PERCENT\s*=\s*\(unsigned int\)0;",
-                                               "NEWORDER_PERCENT =(unsigned int)50;"))
+# Copies with other constants: the shipped sources copied to a temporary
+# directory outside the repository, lines of Predefine.h (consts, so not
+# settable by -D) changed, compiled there.  Each patch must match once.
+def _const(name, typ, old, new):
+    return ("Predefine.h", rf"{name}\s*=\s*\({typ}\){old};", f"{name} =({typ}){new};")
+
+
+PROGRAMS["tf50"] = dict(PROGRAMS["tf"], patches=[_const("NEWORDER_PERCENT", "unsigned int", 0, 50)])
+PROGRAMS["tf_c3"] = dict(PROGRAMS["tf"], patches=[_const("BATCH_SIZE", "unsigned int", 65536, 1048576),
+                                                  _const("NEWORDER_PERCENT", "unsigned int", 0, 50)])
+PROGRAMS["y1_c2"] = dict(PROGRAMS["y1"], patches=[
+    _const("BATCH_SIZE", "unsigned int", 10000, 1048576),
+    _const("YCSB_SIZE", "unsigned long long", 1000000, 10000000),
+    _const("YCSB_OP_SIZE", "unsigned int", 10, 16),
+    _const("YCSB_READ_SIZE", "unsigned int", 9, 15),
+    _const("DATA_DISTRIBUTION", "unsigned int", "ZIPFIAN", "UNIFORM")])
 LAYOUT_VERSION = 2  # neworder_counters / neworder_fields
 
 
@@ -107,16 +130,16 @@ def build(force=False):
     for name, p in PROGRAMS.items():
         src_dir = os.path.join(REF, p["dir"])
         tmp = None
-        if "patch" in p:
+        if "patches" in p:
             tmp = tempfile.mkdtemp(prefix="ltpg_ref_")
             shutil.copytree(src_dir, os.path.join(tmp, "src"))
             src_dir = os.path.join(tmp, "src")
-            fname, pattern, repl = p["patch"]
-            path = os.path.join(src_dir, fname)
-            text, n = re.subn(pattern, repl, open(path).read())
-            if n != 1:
-                raise RuntimeError(f"{name}: patch of {fname} matched {n} times")
-            open(path, "w").write(text)
+            for fname, pattern, repl in p["patches"]:
+                path = os.path.join(src_dir, fname)
+                text, n = re.subn(pattern, repl, open(path).read())
+                if n != 1:
+                    raise RuntimeError(f"{name}: patch {pattern!r} of {fname} matched {n} times")
+                open(path, "w").write(text)
         try:
             _build_one(name, p, src_dir, force)
         finally:
@@ -128,28 +151,27 @@ def build(force=False):
 def _build_one(name, p, src_dir, force):
     cubin = os.path.join(OUT, f"{name}.cubin")
     layout = os.path.join(OUT, f"{name}_layout.json")
-    if True:
-        if force or not os.path.exists(cubin):
-            subprocess.run([NVCC, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-                            "-w", "-o", cubin, os.path.join(src_dir, p["main"])], check=True, capture_output=True)
-        stale = os.path.exists(layout) and json.load(open(layout)).get("layout_version", 1) < LAYOUT_VERSION
-        if force or stale or not os.path.exists(layout):
-            cpp = os.path.join(OUT, f"{name}_layout.cpp")
-            exe = os.path.join(OUT, f"{name}_layout")
-            with open(cpp, "w") as f:
-                f.write(p["layout"])
-            subprocess.run(["g++", "-std=c++17", "-w", "-I" + src_dir, cpp, "-o", exe], check=True,
-                           capture_output=True)
-            out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
-            data = json.loads(out)
-            data["kernels"] = p["kernels"]
-            data["layout_version"] = LAYOUT_VERSION
-            if "cid_kernel" in p:
-                data["cid_kernel"] = p["cid_kernel"]
-            with open(layout, "w") as f:
-                json.dump(data, f, indent=1)
-            os.remove(exe)
-            os.remove(cpp)
+    if force or not os.path.exists(cubin):
+        subprocess.run([NVCC, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                        "-w", "-o", cubin, os.path.join(src_dir, p["main"])], check=True, capture_output=True)
+    stale = os.path.exists(layout) and json.load(open(layout)).get("layout_version", 1) < LAYOUT_VERSION
+    if force or stale or not os.path.exists(layout):
+        cpp = os.path.join(OUT, f"{name}_layout.cpp")
+        exe = os.path.join(OUT, f"{name}_layout")
+        with open(cpp, "w") as f:
+            f.write(p["layout"])
+        subprocess.run(["g++", "-std=c++17", "-w", "-I" + src_dir, cpp, "-o", exe], check=True,
+                       capture_output=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+        data = json.loads(out)
+        data["kernels"] = p["kernels"]
+        data["layout_version"] = LAYOUT_VERSION
+        if "cid_kernel" in p:
+            data["cid_kernel"] = p["cid_kernel"]
+        with open(layout, "w") as f:
+            json.dump(data, f, indent=1)
+        os.remove(exe)
+        os.remove(cpp)
 
 
 if __name__ == "__main__":

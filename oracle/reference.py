@@ -5,12 +5,15 @@ oracle/ref_build.py (oracle/_ref/) and runs them through ref_harness.cu:
   RefY1  LTPG/YCSB/1 as shipped: 10,000 transactions x (9 reads + 1 write)
          over 1,000,000 records (Y1/Predefine.h:8-12).  Its Zipfian mode routes
          key 0 around registration (Y1/Genericfunction.h:163-187), so batches
-         for it use keys 1 .. N-1.
+         for it use keys 1 .. N-1.  RefY1("y1_c2"): the same sources at the
+         high-contention scale, 1,048,576 transactions x (15 reads + 1 write)
+         over 10,000,000 records, uniform mode (every key registers).
   RefTF  LTPG/TPCC-allopt-final as shipped: 65,536 Payments (NEWORDER_PERCENT
          = 0), 64 warehouses (TF/Predefine.h:8-10), customers by id; and its
          KERNEL_CID by-name lookup (TF/tp.cu:11-23) on its own.  RefTF("tf50"):
          the same sources with NEWORDER_PERCENT = 50 (32,768 NewOrders +
-         32,768 Payments).
+         32,768 Payments); RefTF("tf_c3"): 1,048,576 transactions, half of
+         them NewOrders (524,288 of each kind).
 Both return per-transaction flags rebuilt from the reference's conflict
 counters raw / war / waw (the commit flag from its own rule,
 TF/Execute_payment.h:607, Y1/Execute.h:187).
@@ -116,8 +119,9 @@ def covered_txns(layout, warps_per_group, batch):
 
 
 class RefY1:
-    def __init__(self):
-        self.L = json.load(open(os.path.join(REF, "y1_layout.json")))
+    def __init__(self, prog="y1"):
+        self.prog = prog
+        self.L = json.load(open(os.path.join(REF, f"{prog}_layout.json")))
         self.B = self.L["batch"]
         self.n = self.L["table"]
         self.reads = self.L["reads"]
@@ -147,7 +151,7 @@ class RefY1:
         # per batch the reference refills its registration tables with 0xFF
         # (clear_LOG) and starts from fresh conflict counters and marks
         resets = [(2, 0, lg["ytd"], 0xFF), (0, s["war"], s["size"] - s["war"], 0)]
-        ms = _launch("y1", L, [set_b, query, log, snap, index], [1, 0, 0, 0, 0], resets, iters)
+        ms = _launch(self.prog, L, [set_b, query, log, snap, index], [1, 0, 0, 0, 0], resets, iters)
         sv = set_b.view(np.uint32)
         raw = sv[s["raw"] // 4:s["raw"] // 4 + B]
         war = sv[s["war"] // 4:s["war"] // 4 + B]

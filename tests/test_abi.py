@@ -87,3 +87,15 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(py, "size")] == C.sizeof(cls), py
         for name, _ in cls._fields_:
             assert got[(py, name)] == getattr(cls, name).offset, (py, name)
+
+
+def test_bench_library_exports_its_header(built_lib):
+    """The measurement-only library exports what include/ltpg_bench.h declares,
+    and the engine library does not carry it."""
+    from ltpg_gb300 import build
+    bench = C.CDLL(build.BENCH_LIB)
+    declared = abi.declared_functions(os.path.join(ROOT, "include", "ltpg_bench.h"))
+    assert declared == sorted(abi.BENCH_SIGNATURES)
+    assert all(hasattr(bench, n) for n in declared)
+    engine = C.CDLL(built_lib)
+    assert not any(hasattr(engine, n) for n in declared)

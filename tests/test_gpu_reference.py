@@ -183,3 +183,73 @@ def test_reference_name_lookup_matches(ref, data):
         assert np.array_equal(eng.txn_flags(0, B), o.run(mb)[0])
     finally:
         eng.close()
+
+
+def _ycsb_write_last_batch(keys):
+    """One batch of len(keys) transactions whose last key is an update and the
+    others reads (the reference's fixed shape: reads first, then the write)."""
+    B, k = keys.shape
+    stride = (k + 3) & ~3
+    ops = np.full((B, stride), abi.YCSB_OP_PAD, dtype=np.uint32)
+    ops[:, :k - 1] = keys[:, :k - 1]
+    ops[:, k - 1] = np.uint32(0x80000000) | keys[:, k - 1]
+    return YcsbBatch(ops.ravel(), np.arange(B + 1, dtype=np.uint32), np.arange(B, dtype=np.uint64) + 7, B, k)
+
+
+def test_reference_ycsb_flags_match_at_headline_scale(ref):
+    """YCSB/1 compiled at the high-contention scale (1,048,576 transactions x
+    (15 reads + 1 write), 10,000,000 records, uniform mode so that every key
+    registers): its flags on a theta = 0.99 batch equal the oracle's and the
+    engine's for every transaction."""
+    if not reference.available("y1_c2"):
+        pytest.skip("y1_c2 not built (oracle/ref_build.py where the reference sources are)")
+    r = reference.RefY1("y1_c2")
+    B, n = r.B, r.n
+    assert (B, n, r.reads) == (1 << 20, 10_000_000, 15) and r.covered == B
+    g = YcsbGenerator(21, n, B, 16, 0, 0.99, 8)
+    keys = (g.batch(0).ops.reshape(B, 16) & KEY_MASK).astype(np.uint32)
+    ref_flags, mark = r.run(keys[:, :15], keys[:, 15])
+    b = _ycsb_write_last_batch(keys)
+    want = oracle.YcsbOracle(21, n).run(b, threads=8)[0]
+    assert np.array_equal(ref_flags, want), np.nonzero(ref_flags != want)[0][:10]
+    assert np.array_equal(mark.astype(bool), (want & abi.FLAG_COMMIT) != 0)
+    assert (want & abi.FLAG_RAW).any() and (want & abi.FLAG_WAW).any()
+    eng = Engine(device=0, n_slots=1, max_txn=B, max_ops_per_txn=16)
+    try:
+        eng.load_ycsb(21, n)
+        eng.set_launch("ycsb", late_reads=3)
+        eng.upload(0, b)
+        eng.run_batch(0, "graph")
+        eng.sync()
+        assert np.array_equal(eng.txn_flags(0, B), want)
+    finally:
+        eng.close()
+
+
+def test_reference_neworder_payment_flags_match_at_headline_scale(ref):
+    """TPCC-allopt-final compiled for the TPC-C headline batch (1,048,576
+    transactions, 524,288 NewOrders + 524,288 Payments, W = 64): its flags
+    equal the oracle's and the engine's for every transaction."""
+    if not reference.available("tf_c3"):
+        pytest.skip("tf_c3 not built (oracle/ref_build.py where the reference sources are)")
+    r = reference.RefTF("tf_c3")
+    nc, pc, W = r.L["neworder_cnt"], r.L["payment_cnt"], r.W
+    assert (nc, pc, W) == (1 << 19, 1 << 19, 64) and r.covered >= max(nc, pc)
+    g = TpccGenerator(23, W, 1_100_000, neworder_pct=50)
+    b = _mixed_batch(g, nc, pc)
+    # the first batch's order-line ids stay far from each warehouse's end, so
+    # the reference's unwrapped ORDER-LINE keys (W * 450000 + OL_ID + i) are in range
+    assert b.txns["c"].max() + 15 < 450000
+    ref_flags = r.run(b.txns, b.lines)
+    want = oracle.TpccOracle(23, W).run(b, threads=8)[0]
+    bad = np.nonzero(ref_flags != want)[0]
+    assert len(bad) == 0, (bad[:10], ref_flags[bad[:5]], want[bad[:5]])
+    eng = Engine(device=0, n_slots=1, max_txn=b.n_txn, max_ops_per_txn=16, max_lines=b.n_lines)
+    try:
+        eng.load_tpcc(23, W)
+        eng.upload(0, b)
+        eng.run_batch(0, "graph")
+        eng.sync()
+        assert np.array_equal(eng.txn_flags(0, b.n_txn), want)
+    finally:
+        eng.close()
