@@ -1024,10 +1024,19 @@ def device_gen_section(w, reps=8):
 
 
 def serving_section(args):
-    """Serving loop (configs[4]): Poisson arrivals at 1M / 5M / 20M txn/s, 70 %
-    TPC-C (W = 64) and 30 % YCSB (1M records, 10 ops, 50/50, theta 0.9), batches
-    closing at 262,144 requests or 2 ms, 40 GB device budget; plain vs tuned."""
+    """Serving loop: Poisson arrivals at 1M / 5M / 20M txn/s, 70 % TPC-C
+    (W = 64) and 30 % YCSB (1M records, 10 ops, 50/50, theta 0.9), batches
+    closing at 262,144 requests or 2 ms, 40 GB device budget; plain (three
+    kernels per part) vs tuned (fused kernels with the autotuned launch shapes
+    of the TPC-C W=64 and small-YCSB workloads).  The tuned arm is not run as
+    CUDA graphs: a graph is captured for one batch size, and served batches
+    differ in size."""
     import ltpg_gb300 as L
+    from ltpg_gb300 import tune
+
+    def shape(key):
+        cfg = tune.load_cached(key, args.tune_cache) or {}
+        return {k: v for k, v in cfg.items() if k in dict(L.abi.LaunchC._fields_)}
     tp = dict(seed=SEED, warehouses=64, n_txn=262144)
     yp = dict(seed=SEED + 1, n_records=1_000_000, n_txn=262144, ops_per_txn=10, update_pct=50, theta=0.9)
     c = L.Engine(device=0, n_slots=4, max_txn=262144, max_ops_per_txn=16, max_lines=15 * 262144)
@@ -1038,6 +1047,9 @@ def serving_section(args):
             for mode in ["plain", "fused"]:
                 c.load_tpcc(tp["seed"], tp["warehouses"])
                 y.load_ycsb(yp["seed"], yp["n_records"])
+                if mode == "fused":
+                    c.set_launch("tpcc", **shape("tpcc"))
+                    y.set_launch("ycsb", **shape("ycsb_small|theta=0.6"))
                 st = L.serve(c, y, rate=rate, duration_s=args.serve_seconds, tpcc_params=tp, ycsb_params=yp,
                              deadline_ms=2.0, max_batch=262144, tpcc_pct=70, mode=mode, budget_bytes=40 << 30,
                              slots=4)

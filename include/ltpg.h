@@ -474,8 +474,62 @@ typedef struct {
     double wait_ms, launch_ms, device_ms;
 } ltpg_serve_stats;
 typedef struct ltpg_serve_record ltpg_serve_record;
+/* The request loop over generated pools, driven by ltpg_serve_submit /
+ * ltpg_serve_poll below: each request is submitted at its arrival time. */
 int ltpg_serve_run(ltpg_ctx *tpcc_ctx, ltpg_ctx *ycsb_ctx, const ltpg_serve_cfg *cfg, const ltpg_tpcc_params *tp,
                    const ltpg_ycsb_params *yp, ltpg_serve_stats *out, ltpg_serve_record **record);
+
+/* Serving caller-owned transactions.  Replaces the reference's host loop that
+ * stages each batch through a 2-slot prefetch (TF/Query.h:526-605): requests
+ * join the forming batch as they are submitted (packed into pinned staging at
+ * once); a batch closes at max_batch requests, when its TPC-C order lines
+ * would pass the engine's max_lines, or when its first request has waited
+ * deadline_ms (checked by every submit and poll call); it is handed to the
+ * two engines when a device slot is free (slots in flight are bounded by
+ * `slots`, the engines' slots and budget_bytes), the TPC-C and YCSB parts on
+ * streams of their own, so batches overlap on the device.  TIDs are positions
+ * within a batch's part, in submission order.  A full batch with every slot
+ * in flight makes submit wait for the oldest batch.  One driving thread per
+ * server, as for a context; the server sets the contexts' streams while open.
+ * Request ids count from 0 in submission order; batches complete in order, so
+ * the finished requests are always a prefix of the ids. */
+typedef struct ltpg_server ltpg_server;
+typedef struct {
+    double deadline_ms;     /* batch closing deadline (2.0)                          */
+    uint64_t budget_bytes;  /* registration tables + batch buffers in flight, 0 = none */
+    uint32_t max_batch;     /* batch closing size (<= both engines' max_txn)         */
+    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT                  */
+    uint32_t slots;         /* batches in flight (<= the engines' slots)             */
+    uint32_t ycsb_ops;      /* op words per YCSB transaction of a batch (<= the YCSB
+                               engine's max_ops_per_txn); shorter requests are
+                               padded                                                */
+} ltpg_server_cfg;
+typedef struct {
+    int32_t workload;             /* LTPG_WORKLOAD_TPCC or LTPG_WORKLOAD_YCSB           */
+    uint32_t n;                   /* TPC-C: order lines; YCSB: op words (1..ycsb_ops)  */
+    const ltpg_tpcc_txn *txn;     /* TPC-C: the record (its line_off is ignored)        */
+    const ltpg_tpcc_line *lines;  /* TPC-C: its n order lines                           */
+    const uint32_t *ops;          /* YCSB: its n op words                               */
+    const uint64_t *vals;         /* YCSB: one value per update, in op order            */
+} ltpg_request;
+int ltpg_server_open(ltpg_ctx *tpcc_ctx, ltpg_ctx *ycsb_ctx, const ltpg_server_cfg *cfg, ltpg_server **out);
+/* Admits n requests (copied before return); their ids are *first_id .. + n-1. */
+int ltpg_serve_submit(ltpg_server *s, const ltpg_request *reqs, uint32_t n, uint64_t *first_id);
+/* Results of requests first_id .. first_id + n - 1: *n_done = how many of them,
+ * from first_id on, have finished; their flags (LTPG_FLAG_*) and results are
+ * written to flags[0 .. *n_done - 1] and results[...] (either may be NULL).  A
+ * request's result is kept until a poll returns it, and ids below the lowest one
+ * not yet returned are forgotten (LTPG_ERR_INVALID if asked for again). */
+int ltpg_serve_poll(ltpg_server *s, uint64_t first_id, uint32_t n, uint8_t *flags, int64_t *results,
+                    uint32_t *n_done);
+/* Closes the forming batch now and waits until every batch has finished. */
+int ltpg_serve_flush(ltpg_server *s);
+/* Boundaries of the batches closed so far, in order: the first request id and
+ * the number of requests of batch i (for replaying a batch alone). */
+int ltpg_serve_batch_log(const ltpg_server *s, uint64_t *first_ids, uint32_t *counts, size_t cap, size_t *n_batches);
+/* Flushes, restores the contexts' streams, frees the server; stats (optional)
+ * over its life: latency = submit to results on the host, per committed request. */
+int ltpg_server_close(ltpg_server *s, ltpg_serve_stats *stats);
 /* Record: batches[4 * i .. 4 * i + 3] = TPC-C pool start, count, YCSB pool
  * start, count of batch i (pool index = order of arrival within the type). */
 int ltpg_serve_record_sizes(const ltpg_serve_record *r, uint64_t *n_batches, uint64_t *n_tpcc, uint64_t *n_ycsb);

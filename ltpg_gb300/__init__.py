@@ -524,6 +524,79 @@ class Engine:
         self._ck(lib().ltpg_debug_barrier(self._h, limit_ns, 0xFFFFFFFF if skip_block is None else skip_block))
 
 
+class Server:
+    """Continuous batching of caller-owned transactions over a TPC-C engine and
+    a YCSB engine (ltpg_server_open / ltpg_serve_submit / ltpg_serve_poll in
+    include/ltpg.h).  Requests are ("tpcc", txn_record, lines) or ("ycsb",
+    op_words, update_values); ids count from 0 in submission order."""
+
+    def __init__(self, tpcc_engine, ycsb_engine, max_batch=262144, deadline_ms=2.0, mode="fused", slots=4,
+                 budget_bytes=0, ycsb_ops=16):
+        cfg = abi.ServerCfgC(deadline_ms, budget_bytes, max_batch, MODES[mode] if isinstance(mode, str) else mode,
+                             slots, ycsb_ops)
+        h = C.c_void_p()
+        _check(lib().ltpg_server_open(tpcc_engine._h, ycsb_engine._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._engines = (tpcc_engine, ycsb_engine)
+
+    def submit(self, requests):
+        """Admits the requests; returns the id of the first."""
+        n = len(requests)
+        arr = (abi.RequestC * max(1, n))()
+        keep = []
+        for i, r in enumerate(requests):
+            if r[0] == "tpcc":
+                txn = np.ascontiguousarray(np.asarray(r[1]).reshape(1), dtype=TpccBatch.TXN_DTYPE)
+                lines = np.ascontiguousarray(r[2], dtype=TpccBatch.LINE_DTYPE)
+                keep += [txn, lines]
+                arr[i] = abi.RequestC(abi.WORKLOAD_TPCC, len(lines), txn.ctypes.data,
+                                      lines.ctypes.data if len(lines) else None, None, None)
+            else:
+                ops = np.ascontiguousarray(r[1], dtype=np.uint32)
+                vals = np.ascontiguousarray(r[2], dtype=np.uint64)
+                keep += [ops, vals]
+                arr[i] = abi.RequestC(abi.WORKLOAD_YCSB, len(ops), None, None, ops.ctypes.data,
+                                      vals.ctypes.data if len(vals) else None)
+        first = C.c_uint64()
+        code = lib().ltpg_serve_submit(self._h, arr, n, C.byref(first))
+        if code:
+            raise LtpgError(code, "ltpg_serve_submit failed")
+        return first.value
+
+    def poll(self, first_id, n):
+        """(flags, results) of the finished requests first_id, first_id + 1, ... (at most n)."""
+        flags = np.zeros(n, dtype=np.uint8)
+        res = np.zeros(n, dtype=np.int64)
+        done = C.c_uint32()
+        code = lib().ltpg_serve_poll(self._h, first_id, n, _p(flags), _p(res), C.byref(done))
+        if code:
+            raise LtpgError(code, "ltpg_serve_poll failed")
+        return flags[:done.value], res[:done.value]
+
+    def flush(self):
+        code = lib().ltpg_serve_flush(self._h)
+        if code:
+            raise LtpgError(code, "ltpg_serve_flush failed")
+
+    def batch_log(self):
+        """[(first id, request count)] of the batches closed so far."""
+        n = C.c_size_t()
+        lib().ltpg_serve_batch_log(self._h, None, None, 0, C.byref(n))
+        first = np.zeros(n.value, dtype=np.uint64)
+        cnt = np.zeros(n.value, dtype=np.uint32)
+        lib().ltpg_serve_batch_log(self._h, _p(first), _p(cnt), n.value, C.byref(n))
+        return list(zip(first.tolist(), cnt.tolist()))
+
+    def close(self):
+        """Flushes and frees the server; returns its stats dict."""
+        st = abi.ServeStatsC()
+        code = lib().ltpg_server_close(self._h, C.byref(st))
+        self._h = None
+        if code:
+            raise LtpgError(code, "ltpg_server_close failed")
+        return {k: getattr(st, k) for k, _ in abi.ServeStatsC._fields_}
+
+
 def serve(tpcc_engine, ycsb_engine, rate, duration_s, tpcc_params, ycsb_params, deadline_ms=2.0,
           max_batch=262144, tpcc_pct=70, mode="fused", budget_bytes=40 << 30, slots=4, seed=1, record=False):
     """Runs the continuous-batching request loop (see ltpg_serve_run in include/ltpg.h).

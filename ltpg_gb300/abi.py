@@ -79,6 +79,16 @@ class ServeStatsC(C.Structure):
                 ("wait_ms", C.c_double), ("launch_ms", C.c_double), ("device_ms", C.c_double)]
 
 
+class ServerCfgC(C.Structure):
+    _fields_ = [("deadline_ms", C.c_double), ("budget_bytes", C.c_uint64), ("max_batch", C.c_uint32),
+                ("mode", C.c_uint32), ("slots", C.c_uint32), ("ycsb_ops", C.c_uint32)]
+
+
+class RequestC(C.Structure):
+    _fields_ = [("workload", C.c_int32), ("n", C.c_uint32), ("txn", C.c_void_p), ("lines", C.c_void_p),
+                ("ops", C.c_void_p), ("vals", C.c_void_p)]
+
+
 class StatsC(C.Structure):
     _fields_ = [("n_txn", C.c_uint64), ("commits", C.c_uint64), ("raw", C.c_uint64), ("war", C.c_uint64),
                 ("waw", C.c_uint64), ("staged_ops", C.c_uint64), ("total_ops", C.c_uint64)]
@@ -150,6 +160,12 @@ SIGNATURES = {
     "ltpg_predictor_gradients": (C.c_int, [P, P, P, U32, P]),
     "ltpg_serve_run": (C.c_int, [P, P, C.POINTER(ServeCfgC), C.POINTER(TpccParamsC), C.POINTER(YcsbParamsC),
                                  C.POINTER(ServeStatsC), C.POINTER(P)]),
+    "ltpg_server_open": (C.c_int, [P, P, C.POINTER(ServerCfgC), C.POINTER(P)]),
+    "ltpg_serve_submit": (C.c_int, [P, P, U32, C.POINTER(U64)]),
+    "ltpg_serve_poll": (C.c_int, [P, U64, U32, P, P, C.POINTER(U32)]),
+    "ltpg_serve_flush": (C.c_int, [P]),
+    "ltpg_serve_batch_log": (C.c_int, [P, P, P, SZ, C.POINTER(SZ)]),
+    "ltpg_server_close": (C.c_int, [P, C.POINTER(ServeStatsC)]),
     "ltpg_serve_record_sizes": (C.c_int, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64)]),
     "ltpg_serve_record_get": (C.c_int, [P, P, P, P, P, P]),
     "ltpg_serve_record_free": (C.c_int, [P]),

@@ -1,19 +1,23 @@
-// serve.cpp — continuous-batching request loop over two engines (TPC-C, YCSB).
+// serve.cpp — continuous batching of caller-submitted transactions over two
+// engines (TPC-C, YCSB), and the Poisson request loop built on it.
 //
-// Requests arrive open-loop (Poisson, seeded) as a mix of TPC-C NewOrder /
-// Payment transactions and YCSB transactions, drawn in order from pools made
-// by the deterministic generators.  The loop admits every request whose
-// arrival time has passed into the forming batch, closes the batch when it
-// holds max_batch requests or its first request has waited deadline_ms, and
-// hands the two sub-batches to their engines on their own streams, so TPC-C
-// and YCSB kernels run concurrently and the next batch's host-to-device copy
-// overlaps the current batch's kernels.  A batch can only close when both
-// engines have a free slot; the number of slots in flight is bounded by the
-// device-memory budget (batch buffers + registration tables, the tables kept
-// resident).  A request's latency is the time from its arrival to the moment
-// its batch's commit bitmap is in host memory.  With record = 1, the batch
-// boundaries and every request's flags and result are kept, so a test can
-// replay the batches one by one and compare.
+// A server owns the forming batch and the batches in flight.  Submitted
+// requests are packed at once into the forming batch's pinned host staging
+// (one set of staging buffers per batch in flight, plus the forming one), so
+// closing a batch costs its copies and launches, not its packing.  A batch
+// closes at max_batch requests, when its TPC-C order lines would pass the
+// engine's max_lines, or when its first request has waited deadline_ms; it is
+// handed to the engines when a device slot is free: the TPC-C part on one pair
+// of streams (copy, compute), the YCSB part on another, so the two parts and
+// successive batches overlap on the device.  Each engine runs its batches in
+// order on its compute stream, so batches complete in order and the finished
+// requests are always a prefix of the request ids.  A request's flags and
+// result come back with its batch (pinned device-to-host copies behind the
+// kernels) and are kept until a poll returns them.
+//
+// The reference stages caller batches through a two-slot prefetch on host
+// threads and runs one batch at a time (TF/Query.h:526-605, TF/tp.cu:136-261);
+// here admission, batch closing and overlap are the server's.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,6 +40,9 @@ using Clock = std::chrono::steady_clock;
 struct Pinned {
     void *p = nullptr;
     size_t n = 0;
+    Pinned() = default;
+    Pinned(const Pinned &) = delete;
+    Pinned &operator=(const Pinned &) = delete;
     ~Pinned() { ltpg_host_free(p); }
     bool reserve(size_t bytes) {
         if (bytes <= n) return true;
@@ -44,19 +51,34 @@ struct Pinned {
         n = p ? bytes : 0;
         return p != nullptr;
     }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
 };
 
-struct SlotState {
+// Pinned host staging of one batch; bound to that batch until its uploads
+// (recorded by up_c / up_y on the copy streams) are done.
+struct Staging {
+    Pinned c_txns, c_lines, y_ops, y_voff, y_vals;
+    cudaEvent_t up_c = nullptr, up_y = nullptr;
+    bool pending = false;
+};
+
+// A device slot of both engines with the batch it runs.
+struct DevSlot {
     bool busy = false;
-    cudaEvent_t done_c = nullptr, done_y = nullptr;
-    cudaEvent_t start = nullptr;  // recorded when the batch is handed to the engines
-    double t_close = 0;           // host time the batch closed
-    uint64_t c_start = 0, c_count = 0, y_start = 0, y_count = 0;
-    uint64_t c_packed = 0, y_packed = 0;  // requests of the forming batch already in the staging buffers
-    double arrival_first = 0;
-    Pinned c_txns, c_lines, y_ops, y_voff, y_vals;   // host staging of the batch
-    Pinned c_bits, y_bits, c_flags, y_flags, c_res, y_res;
-    std::vector<ltpg_tpcc_txn> tmp_txn;
+    cudaEvent_t start = nullptr, done_c = nullptr, done_y = nullptr;
+    Pinned c_flags, c_res, y_flags, y_res;  // results, copied back behind the kernels
+    uint64_t first_id = 0;
+    uint32_t n = 0, n_c = 0, n_y = 0;
+    std::vector<uint32_t> map;      // per request: (index in its part << 1) | (1 for YCSB)
+    std::vector<double> t_submit;   // per request, server clock (s)
+};
+
+struct Res {
+    int64_t result;
+    uint8_t flags, done, returned;
 };
 
 double percentile(std::vector<double> &v, double q) {
@@ -64,6 +86,313 @@ double percentile(std::vector<double> &v, double q) {
     size_t k = (size_t)std::min<double>(v.size() - 1, std::floor(q * (v.size() - 1)));
     std::nth_element(v.begin(), v.begin() + k, v.end());
     return v[k];
+}
+
+}  // namespace
+
+struct ltpg_server {
+    ltpg_ctx *tc = nullptr, *yc = nullptr;
+    void *tc_stream0 = nullptr, *yc_stream0 = nullptr;  // the contexts' streams before open
+    double deadline_s = 0.002;
+    uint32_t max_batch = 0, mode = 0, allowed = 0, ky = 0, sy = 0;
+    uint64_t max_lines = 0;
+    cudaStream_t cs_c = nullptr, cp_c = nullptr, cs_y = nullptr, cp_y = nullptr;
+    std::vector<Staging> stage;  // allowed + 1 sets
+    std::vector<DevSlot> dev;    // allowed slots, used in order
+    uint32_t hf = 0;             // staging set of the forming batch
+    uint32_t next_dev = 0, oldest = 0, in_flight = 0;
+    // the forming batch
+    uint64_t form_first = 0;
+    uint32_t form_n = 0, form_c = 0, form_y = 0;
+    uint64_t form_lines = 0, form_vals = 0;
+    double form_t_first = 0;
+    std::vector<uint32_t> form_map;
+    std::vector<double> form_t;
+    // request ids and results
+    uint64_t next_id = 0, base_id = 0;
+    std::deque<Res> res;
+    uint64_t c_total = 0;  // TPC-C requests in the batches closed so far (txn_base of the next)
+    std::vector<uint64_t> log_first;
+    std::vector<uint32_t> log_n, log_c;
+    // statistics
+    Clock::time_point t0;
+    double t_last_done = 0;
+    std::vector<double> lat;
+    uint64_t committed = 0, batches = 0, waited_for_slot = 0;
+    double wait_sum = 0, launch_sum = 0, dev_sum = 0;
+    int error = LTPG_OK;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+void destroy(ltpg_server *s) {
+    for (auto &g : s->stage) {
+        if (g.up_c) cudaEventDestroy(g.up_c);
+        if (g.up_y) cudaEventDestroy(g.up_y);
+    }
+    for (auto &d : s->dev) {
+        if (d.start) cudaEventDestroy(d.start);
+        if (d.done_c) cudaEventDestroy(d.done_c);
+        if (d.done_y) cudaEventDestroy(d.done_y);
+    }
+    for (cudaStream_t st : {s->cs_c, s->cp_c, s->cs_y, s->cp_y})
+        if (st) cudaStreamDestroy(st);
+    delete s;
+}
+
+// Records the first error; later calls return it.
+int fail(ltpg_server *s, int code) {
+    if (s->error == LTPG_OK) s->error = code;
+    return code;
+}
+
+// Finishes the oldest batch in flight (waiting for it when block): its
+// requests' flags, results and latencies.  Returns false if none finished.
+bool complete_oldest(ltpg_server *s, bool block) {
+    if (s->in_flight == 0) return false;
+    DevSlot &d = s->dev[s->oldest];
+    if (block) {
+        if (cudaEventSynchronize(d.done_c) != cudaSuccess || cudaEventSynchronize(d.done_y) != cudaSuccess) {
+            fail(s, LTPG_ERR_CUDA);
+            return false;
+        }
+    } else if (cudaEventQuery(d.done_c) != cudaSuccess || cudaEventQuery(d.done_y) != cudaSuccess) {
+        return false;
+    }
+    const double t_done = s->now();
+    float ms_c = 0.f, ms_y = 0.f;
+    cudaEventElapsedTime(&ms_c, d.start, d.done_c);
+    cudaEventElapsedTime(&ms_y, d.start, d.done_y);
+    s->dev_sum += std::max(ms_c, ms_y) * 1e-3;
+    const uint8_t *cf = d.c_flags.as<uint8_t>(), *yf = d.y_flags.as<uint8_t>();
+    const int64_t *cr = d.c_res.as<int64_t>(), *yr = d.y_res.as<int64_t>();
+    for (uint32_t i = 0; i < d.n; ++i) {
+        const uint32_t m = d.map[i], k = m >> 1;
+        Res &r = s->res[d.first_id + i - s->base_id];
+        r.flags = (m & 1u) ? yf[k] : cf[k];
+        r.result = (m & 1u) ? yr[k] : cr[k];
+        r.done = 1;
+        if (r.flags & LTPG_FLAG_COMMIT) {
+            ++s->committed;
+            s->lat.push_back((t_done - d.t_submit[i]) * 1e3);
+        }
+    }
+    s->t_last_done = t_done;
+    d.busy = false;
+    s->oldest = (s->oldest + 1) % s->allowed;
+    --s->in_flight;
+    return true;
+}
+
+// The staging set of a new forming batch must be free of its last batch's uploads.
+int begin_forming(ltpg_server *s, double t) {
+    Staging &g = s->stage[s->hf];
+    if (g.pending) {
+        if (cudaEventSynchronize(g.up_c) != cudaSuccess || cudaEventSynchronize(g.up_y) != cudaSuccess)
+            return fail(s, LTPG_ERR_CUDA);
+        g.pending = false;
+    }
+    s->form_first = s->next_id;
+    s->form_t_first = t;
+    s->form_n = s->form_c = s->form_y = 0;
+    s->form_lines = s->form_vals = 0;
+    s->form_map.clear();
+    s->form_t.clear();
+    return LTPG_OK;
+}
+
+// Hands the forming batch to the engines.  Without a free device slot it
+// waits for the oldest batch when block, else leaves the batch forming.
+int close_batch(ltpg_server *s, bool block) {
+    if (s->form_n == 0) return LTPG_OK;
+    const double t = s->now();
+    DevSlot &d = s->dev[s->next_dev];
+    if (d.busy) {
+        if (!block) {
+            ++s->waited_for_slot;
+            return LTPG_OK;
+        }
+        ++s->waited_for_slot;
+        while (d.busy)
+            if (!complete_oldest(s, true)) return fail(s, s->error ? s->error : LTPG_ERR_CUDA);
+    }
+    Staging &g = s->stage[s->hf];
+    const uint32_t slot = s->next_dev;
+    cudaEventRecord(d.start, s->cp_c);
+    cudaStreamWaitEvent(s->cp_y, d.start, 0);
+    int r = LTPG_OK;
+    if (s->form_c) {
+        ltpg_tpcc_batch b{s->form_c, (uint32_t)s->form_lines, s->c_total, g.c_txns.as<ltpg_tpcc_txn>(),
+                          g.c_lines.as<ltpg_tpcc_line>()};
+        ltpg_set_stream(s->tc, s->cp_c);
+        if ((r = ltpg_batch_upload_tpcc(s->tc, slot, &b))) return fail(s, r);
+        cudaEventRecord(g.up_c, s->cp_c);
+        cudaStreamWaitEvent(s->cs_c, g.up_c, 0);
+        ltpg_set_stream(s->tc, s->cs_c);
+        if ((r = ltpg_run_batch(s->tc, slot, (int)s->mode))) return fail(s, r);
+        const Slot &es = s->tc->slots[slot];
+        cudaMemcpyAsync(d.c_flags.p, es.flags, s->form_c, cudaMemcpyDeviceToHost, s->cs_c);
+        cudaMemcpyAsync(d.c_res.p, es.results, (size_t)s->form_c * 8, cudaMemcpyDeviceToHost, s->cs_c);
+    } else {
+        cudaEventRecord(g.up_c, s->cp_c);
+        cudaStreamWaitEvent(s->cs_c, d.start, 0);
+    }
+    cudaEventRecord(d.done_c, s->cs_c);
+    if (s->form_y) {
+        g.y_voff.as<uint32_t>()[s->form_y] = (uint32_t)s->form_vals;
+        ltpg_ycsb_batch b{s->form_y, s->ky, s->sy, (uint32_t)s->form_vals, g.y_ops.as<uint32_t>(),
+                          g.y_voff.as<uint32_t>(), g.y_vals.as<uint64_t>()};
+        ltpg_set_stream(s->yc, s->cp_y);
+        if ((r = ltpg_batch_upload_ycsb(s->yc, slot, &b))) return fail(s, r);
+        cudaEventRecord(g.up_y, s->cp_y);
+        cudaStreamWaitEvent(s->cs_y, g.up_y, 0);
+        ltpg_set_stream(s->yc, s->cs_y);
+        if ((r = ltpg_run_batch(s->yc, slot, (int)s->mode))) return fail(s, r);
+        const Slot &es = s->yc->slots[slot];
+        cudaMemcpyAsync(d.y_flags.p, es.flags, s->form_y, cudaMemcpyDeviceToHost, s->cs_y);
+        cudaMemcpyAsync(d.y_res.p, es.results, (size_t)s->form_y * 8, cudaMemcpyDeviceToHost, s->cs_y);
+    } else {
+        cudaEventRecord(g.up_y, s->cp_y);
+        cudaStreamWaitEvent(s->cs_y, d.start, 0);
+    }
+    cudaEventRecord(d.done_y, s->cs_y);
+    if (cudaGetLastError() != cudaSuccess) return fail(s, LTPG_ERR_CUDA);
+    g.pending = true;
+    d.busy = true;
+    d.first_id = s->form_first;
+    d.n = s->form_n;
+    d.n_c = s->form_c;
+    d.n_y = s->form_y;
+    d.map.swap(s->form_map);
+    d.t_submit.swap(s->form_t);
+    for (double ts : d.t_submit) s->wait_sum += t - ts;
+    s->log_first.push_back(s->form_first);
+    s->log_n.push_back(s->form_n);
+    s->log_c.push_back(s->form_c);
+    s->c_total += s->form_c;
+    ++s->batches;
+    ++s->in_flight;
+    s->next_dev = (s->next_dev + 1) % s->allowed;
+    s->hf = (s->hf + 1) % (uint32_t)s->stage.size();
+    s->form_n = 0;
+    s->launch_sum += s->now() - t;
+    return LTPG_OK;
+}
+
+// Finished batches, then the forming batch's deadline.
+int progress(ltpg_server *s) {
+    while (complete_oldest(s, false)) {
+    }
+    if (s->error) return s->error;
+    if (s->form_n && s->now() - s->form_t_first >= s->deadline_s) return close_batch(s, false);
+    return LTPG_OK;
+}
+
+int check_request(const ltpg_server *s, const ltpg_request &q) {
+    if (q.workload == LTPG_WORKLOAD_TPCC) {
+        if (!q.txn || (q.n && !q.lines) || q.n > LTPG_TPCC_MAX_LINES || q.n > s->max_lines) return LTPG_ERR_INVALID;
+        const bool no = tpcc_kind(q.txn->kind_info) == LTPG_TPCC_NEWORDER;
+        if (no ? q.n != tpcc_ol_cnt(q.txn->kind_info) : q.n != 0) return LTPG_ERR_INVALID;
+        return LTPG_OK;
+    }
+    if (q.workload == LTPG_WORKLOAD_YCSB) {
+        if (!q.ops || q.n == 0 || q.n > s->ky) return LTPG_ERR_INVALID;
+        for (uint32_t j = 0; j < q.n; ++j)
+            if (!ycsb_is_pad(q.ops[j]) && ycsb_is_update(q.ops[j]) && !q.vals) return LTPG_ERR_INVALID;
+        return LTPG_OK;
+    }
+    return LTPG_ERR_INVALID;
+}
+
+// Packs one request into the forming batch's staging.
+void pack(ltpg_server *s, const ltpg_request &q, double t) {
+    Staging &g = s->stage[s->hf];
+    if (q.workload == LTPG_WORKLOAD_TPCC) {
+        ltpg_tpcc_txn x = *q.txn;
+        x.line_off = (uint32_t)s->form_lines;
+        g.c_txns.as<ltpg_tpcc_txn>()[s->form_c] = x;
+        if (q.n) memcpy(g.c_lines.as<ltpg_tpcc_line>() + s->form_lines, q.lines, (size_t)q.n * sizeof(ltpg_tpcc_line));
+        s->form_lines += q.n;
+        s->form_map.push_back(s->form_c << 1);
+        ++s->form_c;
+    } else {
+        uint32_t *w = g.y_ops.as<uint32_t>() + (size_t)s->form_y * s->sy;
+        uint64_t *v = g.y_vals.as<uint64_t>() + s->form_vals;
+        g.y_voff.as<uint32_t>()[s->form_y] = (uint32_t)s->form_vals;
+        uint32_t nu = 0;
+        for (uint32_t j = 0; j < s->sy; ++j) {
+            const uint32_t op = j < q.n ? q.ops[j] : LTPG_YCSB_OP_PAD;
+            w[j] = op;
+            if (!ycsb_is_pad(op) && ycsb_is_update(op)) {
+                v[nu] = q.vals[nu];
+                ++nu;
+            }
+        }
+        s->form_vals += nu;
+        s->form_map.push_back((s->form_y << 1) | 1u);
+        ++s->form_y;
+    }
+    s->form_t.push_back(t);
+    ++s->form_n;
+    s->res.push_back(Res{0, 0, 0, 0});
+    ++s->next_id;
+}
+
+// Submission with given submit times (t == nullptr: now).
+int submit(ltpg_server *s, const ltpg_request *reqs, uint32_t n, uint64_t *first_id, const double *t_submit) {
+    if (s->error) return s->error;
+    int r = progress(s);
+    if (r) return r;
+    if (first_id) *first_id = s->next_id;
+    for (uint32_t i = 0; i < n; ++i) {
+        const ltpg_request &q = reqs[i];
+        if ((r = check_request(s, q))) return r;
+        const double t = t_submit ? t_submit[i] : s->now();
+        const bool lines_full =
+            q.workload == LTPG_WORKLOAD_TPCC && s->form_lines + q.n > s->max_lines;
+        if (s->form_n && (s->form_n >= s->max_batch || lines_full))
+            if ((r = close_batch(s, true))) return r;
+        if (s->form_n == 0 && (r = begin_forming(s, t))) return r;
+        pack(s, q, t);
+    }
+    if (s->form_n >= s->max_batch && (r = close_batch(s, true))) return r;
+    return progress(s);
+}
+
+int flush(ltpg_server *s) {
+    if (s->error) return s->error;
+    int r = close_batch(s, true);
+    if (r) return r;
+    while (s->in_flight)
+        if (!complete_oldest(s, true)) return fail(s, s->error ? s->error : LTPG_ERR_CUDA);
+    // device-side errors of the batches (out-of-range keys) are reported here
+    int r1 = ltpg_sync(s->tc), r2 = ltpg_sync(s->yc);
+    if (r1 || r2) return fail(s, r1 ? r1 : r2);
+    return LTPG_OK;
+}
+
+void fill_stats(const ltpg_server *s, ltpg_serve_stats *out) {
+    std::vector<double> lat = s->lat;
+    memset(out, 0, sizeof *out);
+    out->submitted = s->next_id;
+    out->committed = s->committed;
+    out->batches = s->batches;
+    out->slots = s->allowed;
+    out->waited_for_slot = s->waited_for_slot;
+    out->wall_s = s->t_last_done;
+    out->throughput = s->t_last_done > 0 ? s->committed / s->t_last_done : 0;
+    out->mean_batch = s->batches ? (double)s->next_id / s->batches : 0;
+    double sum = 0;
+    for (double v : lat) sum += v;
+    out->mean_ms = lat.empty() ? 0 : sum / lat.size();
+    out->p50_ms = percentile(lat, 0.50);
+    out->p99_ms = percentile(lat, 0.99);
+    out->p999_ms = percentile(lat, 0.999);
+    out->wait_ms = s->next_id ? s->wait_sum * 1e3 / s->next_id : 0;
+    out->launch_ms = s->batches ? s->launch_sum * 1e3 / s->batches : 0;
+    out->device_ms = s->batches ? s->dev_sum * 1e3 / s->batches : 0;
 }
 
 }  // namespace
@@ -76,18 +405,24 @@ struct ltpg_serve_record {
 
 extern "C" {
 
-int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const ltpg_tpcc_params *tp,
-                   const ltpg_ycsb_params *yp, ltpg_serve_stats *out, ltpg_serve_record **record) {
-    if (!tc || !yc || !cfg || !tp || !yp || !out) return LTPG_ERR_INVALID;
-    if (cfg->rate <= 0 || cfg->duration_s <= 0 || cfg->max_batch == 0 || cfg->tpcc_pct > 100)
+int ltpg_server_open(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_server_cfg *cfg, ltpg_server **out) {
+    if (!tc || !yc || !cfg || !out || tc == yc) return LTPG_ERR_INVALID;
+    *out = nullptr;
+    if (cfg->max_batch == 0 || cfg->max_batch > tc->cfg.max_txn || cfg->max_batch > yc->cfg.max_txn)
         return LTPG_ERR_INVALID;
-    if (cfg->max_batch > tc->cfg.max_txn || cfg->max_batch > yc->cfg.max_txn) return LTPG_ERR_INVALID;
+    if (cfg->ycsb_ops == 0 || cfg->ycsb_ops > yc->cfg.max_ops_per_txn || cfg->deadline_ms < 0 ||
+        cfg->mode > LTPG_MODE_GRAPH)
+        return LTPG_ERR_INVALID;
     if (!tc->tpcc.W || !yc->ycsb.rows) return LTPG_ERR_STATE;
-    const uint32_t n_slots = std::min<uint32_t>(cfg->slots ? cfg->slots : 4, std::min<uint32_t>(
-                                                   (uint32_t)tc->slots.size(), (uint32_t)yc->slots.size()));
-    // ---- memory budget: registration tables + n_slots batch slots of each engine
-    const uint64_t per_txn_c = 32 + 8 * LTPG_TPCC_MAX_LINES + 1 + 8 + 1;
-    const uint64_t per_txn_y = 4ull * ((yp->ops_per_txn + 3) & ~3u) + 4 + 8ull * yp->ops_per_txn + 1 + 8 + 1;
+    const uint32_t n_slots = std::min<uint32_t>(cfg->slots ? cfg->slots : 4,
+                                                std::min<uint32_t>((uint32_t)tc->slots.size(),
+                                                                   (uint32_t)yc->slots.size()));
+    const uint32_t ky = cfg->ycsb_ops, sy = ycsb_stride(ky);
+    const uint64_t max_lines = std::min<uint64_t>(tc->cfg.max_lines, (uint64_t)cfg->max_batch * LTPG_TPCC_MAX_LINES);
+    // memory budget: the registration tables stay resident; each batch in
+    // flight holds a slot of each engine
+    const uint64_t per_txn_c = 32 + 8ull * LTPG_TPCC_MAX_LINES + 1 + 8 + 1;
+    const uint64_t per_txn_y = 4ull * sy + 4 + 8ull * ky + 1 + 8 + 1;
     const uint64_t tables = tc->tpcc.n_slots * sizeof(RegSlot) + yc->ycsb.n * sizeof(RegSlot);
     const uint64_t slot_bytes = (uint64_t)cfg->max_batch * (per_txn_c + per_txn_y);
     uint32_t allowed = n_slots;
@@ -96,7 +431,108 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         allowed = (uint32_t)std::min<uint64_t>(n_slots, (cfg->budget_bytes - tables) / std::max<uint64_t>(1, slot_bytes));
         if (allowed == 0) return LTPG_ERR_NOMEM;
     }
-    // ---- request pools and arrival times (before the clock starts)
+    ltpg_server *s = new (std::nothrow) ltpg_server();
+    if (!s) return LTPG_ERR_NOMEM;
+    s->tc = tc;
+    s->yc = yc;
+    s->tc_stream0 = ltpg_get_stream(tc) == tc->own_stream ? nullptr : ltpg_get_stream(tc);
+    s->yc_stream0 = ltpg_get_stream(yc) == yc->own_stream ? nullptr : ltpg_get_stream(yc);
+    s->deadline_s = cfg->deadline_ms * 1e-3;
+    s->max_batch = cfg->max_batch;
+    s->mode = cfg->mode;
+    s->allowed = allowed;
+    s->ky = ky;
+    s->sy = sy;
+    s->max_lines = max_lines;
+    bool ok = cudaSetDevice(tc->device) == cudaSuccess;
+    for (cudaStream_t *st : {&s->cs_c, &s->cp_c})
+        ok = ok && cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaSetDevice(yc->device) == cudaSuccess;
+    for (cudaStream_t *st : {&s->cs_y, &s->cp_y})
+        ok = ok && cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) == cudaSuccess;
+    s->stage = std::vector<Staging>(allowed + 1);
+    s->dev = std::vector<DevSlot>(allowed);
+    const uint64_t m = cfg->max_batch;
+    for (auto &g : s->stage) {
+        ok = ok && g.c_txns.reserve(m * sizeof(ltpg_tpcc_txn)) && g.c_lines.reserve((max_lines + 1) * 8) &&
+             g.y_ops.reserve(m * sy * 4) && g.y_voff.reserve((m + 1) * 4) && g.y_vals.reserve((m * ky + 1) * 8);
+        ok = ok && cudaEventCreateWithFlags(&g.up_c, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&g.up_y, cudaEventDisableTiming) == cudaSuccess;
+    }
+    for (auto &d : s->dev) {
+        ok = ok && d.c_flags.reserve(m) && d.c_res.reserve(m * 8) && d.y_flags.reserve(m) && d.y_res.reserve(m * 8);
+        ok = ok && cudaEventCreate(&d.start) == cudaSuccess && cudaEventCreate(&d.done_c) == cudaSuccess &&
+             cudaEventCreate(&d.done_y) == cudaSuccess;
+    }
+    if (!ok) {
+        destroy(s);
+        return LTPG_ERR_NOMEM;
+    }
+    s->t0 = Clock::now();
+    *out = s;
+    return LTPG_OK;
+}
+
+int ltpg_serve_submit(ltpg_server *s, const ltpg_request *reqs, uint32_t n, uint64_t *first_id) {
+    if (!s || (n && !reqs)) return LTPG_ERR_INVALID;
+    return submit(s, reqs, n, first_id, nullptr);
+}
+
+int ltpg_serve_poll(ltpg_server *s, uint64_t first_id, uint32_t n, uint8_t *flags, int64_t *results,
+                    uint32_t *n_done) {
+    if (!s || !n_done) return LTPG_ERR_INVALID;
+    *n_done = 0;
+    int r = progress(s);
+    if (r) return r;
+    if (first_id < s->base_id) return LTPG_ERR_INVALID;
+    uint32_t k = 0;
+    while (k < n && first_id + k < s->next_id) {
+        Res &q = s->res[first_id + k - s->base_id];
+        if (!q.done) break;
+        if (flags) flags[k] = q.flags;
+        if (results) results[k] = q.result;
+        q.returned = 1;
+        ++k;
+    }
+    *n_done = k;
+    while (!s->res.empty() && s->res.front().returned) {
+        s->res.pop_front();
+        ++s->base_id;
+    }
+    return LTPG_OK;
+}
+
+int ltpg_serve_flush(ltpg_server *s) { return s ? flush(s) : LTPG_ERR_INVALID; }
+
+int ltpg_serve_batch_log(const ltpg_server *s, uint64_t *first_ids, uint32_t *counts, size_t cap, size_t *n_batches) {
+    if (!s || !n_batches) return LTPG_ERR_INVALID;
+    *n_batches = s->log_first.size();
+    const size_t k = std::min(cap, s->log_first.size());
+    if (first_ids) memcpy(first_ids, s->log_first.data(), k * 8);
+    if (counts) memcpy(counts, s->log_n.data(), k * 4);
+    return LTPG_OK;
+}
+
+int ltpg_server_close(ltpg_server *s, ltpg_serve_stats *stats) {
+    if (!s) return LTPG_ERR_INVALID;
+    const int r = flush(s);
+    if (stats) fill_stats(s, stats);
+    ltpg_set_stream(s->tc, s->tc_stream0);
+    ltpg_set_stream(s->yc, s->yc_stream0);
+    cudaStreamSynchronize(s->cs_c);
+    cudaStreamSynchronize(s->cs_y);
+    destroy(s);
+    return r;
+}
+
+// ---- the request loop over generated pools ----------------------------------
+int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const ltpg_tpcc_params *tp,
+                   const ltpg_ycsb_params *yp, ltpg_serve_stats *out, ltpg_serve_record **record) {
+    if (!tc || !yc || !cfg || !tp || !yp || !out) return LTPG_ERR_INVALID;
+    if (cfg->rate <= 0 || cfg->duration_s <= 0 || cfg->max_batch == 0 || cfg->tpcc_pct > 100)
+        return LTPG_ERR_INVALID;
+    if (yp->ops_per_txn == 0 || yp->ops_per_txn > LTPG_YCSB_MAX_OPS) return LTPG_ERR_INVALID;
+    // ---- arrival times and request pools (before the clock starts)
     const uint64_t expected = (uint64_t)(cfg->rate * cfg->duration_s);
     std::mt19937_64 rng(cfg->seed ^ 0x5E57ull);
     std::exponential_distribution<double> gap(cfg->rate);
@@ -119,7 +555,7 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
     // TPC-C pool: consecutive generator batches
     std::vector<ltpg_tpcc_txn> c_pool;
     std::vector<ltpg_tpcc_line> c_lines;
-    std::vector<uint64_t> c_line_off;  // global line offset of each pool transaction
+    std::vector<uint64_t> c_line_off;  // line offset of each pool transaction
     {
         ltpg_tpcc_params p = *tp;
         p.n_txn = std::max<uint32_t>(1, std::min<uint64_t>(p.n_txn, n_c ? n_c : 1));
@@ -142,10 +578,10 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         ltpg_gen_destroy(g);
     }
     // YCSB pool
-    const uint32_t ky = yp->ops_per_txn, sy = (ky + 3) & ~3u;
+    const uint32_t ky = yp->ops_per_txn, sy = ycsb_stride(ky);
     std::vector<uint32_t> y_ops;
     std::vector<uint64_t> y_vals;
-    std::vector<uint64_t> y_voff;  // global value offset of each pool transaction
+    std::vector<uint64_t> y_voff;  // value offset of each pool transaction
     {
         ltpg_ycsb_params p = *yp;
         p.n_txn = std::max<uint32_t>(1, std::min<uint64_t>(p.n_txn, n_y ? n_y : 1));
@@ -166,283 +602,76 @@ int ltpg_serve_run(ltpg_ctx *tc, ltpg_ctx *yc, const ltpg_serve_cfg *cfg, const 
         y_voff.push_back(y_vals.size());
         ltpg_gen_destroy(g);
     }
-    // ---- slots, streams
-    std::vector<SlotState> slots(allowed);
-    cudaStream_t cs_c, cs_y, cp_c, cp_y;
-    cudaSetDevice(tc->device);
-    cudaStreamCreateWithFlags(&cs_c, cudaStreamNonBlocking);
-    cudaStreamCreateWithFlags(&cp_c, cudaStreamNonBlocking);
-    cudaSetDevice(yc->device);
-    cudaStreamCreateWithFlags(&cs_y, cudaStreamNonBlocking);
-    cudaStreamCreateWithFlags(&cp_y, cudaStreamNonBlocking);
-    for (auto &s : slots) {
-        cudaEventCreate(&s.done_c);
-        cudaEventCreate(&s.done_y);
-        cudaEventCreate(&s.start);
-    }
-    // pinned staging for the largest batch, reserved before the clock starts
-    for (auto &s : slots) {
-        const uint64_t m = cfg->max_batch;
-        if (!s.c_txns.reserve(m * sizeof(ltpg_tpcc_txn)) || !s.c_lines.reserve((m * LTPG_TPCC_MAX_LINES + 1) * 8) ||
-            !s.c_bits.reserve((m + 31) / 32 * 4) || !s.c_flags.reserve(m) || !s.c_res.reserve(m * 8) ||
-            !s.y_ops.reserve(m * sy * 4) || !s.y_voff.reserve((m + 1) * 4) || !s.y_vals.reserve((m * ky + 1) * 8) ||
-            !s.y_bits.reserve((m + 31) / 32 * 4) || !s.y_flags.reserve(m) || !s.y_res.reserve(m * 8))
-            return LTPG_ERR_NOMEM;
-    }
-    cudaEvent_t up_c, up_y;
-    cudaEventCreateWithFlags(&up_c, cudaEventDisableTiming);
-    cudaEventCreateWithFlags(&up_y, cudaEventDisableTiming);
-    ltpg_serve_record *rec = nullptr;
-    if (record) {
-        rec = new (std::nothrow) ltpg_serve_record();
-        if (!rec) return LTPG_ERR_NOMEM;
-        rec->c_flags.assign(n_c, 0);
-        rec->y_flags.assign(n_y, 0);
-        rec->c_res.assign(n_c, 0);
-        rec->y_res.assign(n_y, 0);
-    }
-    std::vector<double> lat;  // committed requests' latencies (ms)
-    lat.reserve(N);
-    double wait_sum = 0, pack_sum = 0, dev_sum = 0;  // latency parts (s): close wait per request, per batch
-    std::vector<double> arr_c(n_c), arr_y(n_y);
-    {
-        uint64_t ic = 0, iy = 0;
-        for (uint64_t i = 0; i < N; ++i) (is_tpcc[i] ? arr_c[ic++] : arr_y[iy++]) = arrival[i];
-    }
-    uint64_t next = 0, pos_c = 0, pos_y = 0;  // next arrival; next pool index per type
-    uint64_t form_start = 0;                  // first arrival of the forming batch
-    uint64_t batches = 0, committed = 0, waited_for_slot = 0;
-    double batch_sizes = 0;
-    int rc = LTPG_OK;
-    const int mode = (int)cfg->mode;
-    const double deadline = cfg->deadline_ms * 1e-3;
-    const Clock::time_point t0 = Clock::now();
-    auto now_s = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
-
-    auto complete = [&](SlotState &s, double t_done) {
-        float ms_c = 0.f, ms_y = 0.f;
-        cudaEventElapsedTime(&ms_c, s.start, s.done_c);
-        cudaEventElapsedTime(&ms_y, s.start, s.done_y);
-        dev_sum += std::max(ms_c, ms_y) * 1e-3;
-        (void)t_done;
-        // latency of every committed request of the batch
-        const uint32_t *bc = static_cast<const uint32_t *>(s.c_bits.p);
-        const uint32_t *by = static_cast<const uint32_t *>(s.y_bits.p);
-        for (uint64_t i = 0; i < s.c_count; ++i)
-            if (bc[i >> 5] >> (i & 31) & 1u) {
-                lat.push_back((t_done - arr_c[s.c_start + i]) * 1e3);
-                ++committed;
-            }
-        for (uint64_t i = 0; i < s.y_count; ++i)
-            if (by[i >> 5] >> (i & 31) & 1u) {
-                lat.push_back((t_done - arr_y[s.y_start + i]) * 1e3);
-                ++committed;
-            }
-        if (rec) {
-            memcpy(&rec->c_flags[s.c_start], s.c_flags.p, s.c_count);
-            memcpy(&rec->y_flags[s.y_start], s.y_flags.p, s.y_count);
-            memcpy(&rec->c_res[s.c_start], s.c_res.p, s.c_count * 8);
-            memcpy(&rec->y_res[s.y_start], s.y_res.p, s.y_count * 8);
-        }
-        s.busy = false;
-    };
-
-    // Packs pool requests [c_start + c_packed, c_end) and [y_start + y_packed,
-    // y_end) into the slot's pinned staging: called as requests are admitted,
-    // so a batch is mostly packed when it closes.
-    auto pack_upto = [&](SlotState &s, uint64_t c_end, uint64_t y_end) {
-        const uint64_t c_from = s.c_start + s.c_packed;
-        if (c_end > c_from) {
-            const uint64_t l0 = c_line_off[s.c_start];
-            ltpg_tpcc_txn *tx = static_cast<ltpg_tpcc_txn *>(s.c_txns.p);
-            for (uint64_t i = c_from; i < c_end; ++i) {
-                tx[i - s.c_start] = c_pool[i];
-                tx[i - s.c_start].line_off = (uint32_t)(c_line_off[i] - l0);
-            }
-            memcpy(static_cast<ltpg_tpcc_line *>(s.c_lines.p) + (c_line_off[c_from] - l0), c_lines.data() + c_line_off[c_from],
-                   (c_line_off[c_end] - c_line_off[c_from]) * 8);
-            s.c_packed = c_end - s.c_start;
-        }
-        const uint64_t y_from = s.y_start + s.y_packed;
-        if (y_end > y_from) {
-            const uint64_t v0 = y_voff[s.y_start];
-            memcpy(static_cast<uint32_t *>(s.y_ops.p) + (y_from - s.y_start) * sy, y_ops.data() + y_from * sy,
-                   (y_end - y_from) * sy * 4);
-            uint32_t *vo = static_cast<uint32_t *>(s.y_voff.p);
-            for (uint64_t i = y_from; i < y_end; ++i) vo[i - s.y_start] = (uint32_t)(y_voff[i] - v0);
-            memcpy(static_cast<uint64_t *>(s.y_vals.p) + (y_voff[y_from] - v0), y_vals.data() + y_voff[y_from],
-                   (y_voff[y_end] - y_voff[y_from]) * 8);
-            s.y_packed = y_end - s.y_start;
-        }
-    };
-
-    // Hands a closed, packed batch to the two engines.
-    auto launch = [&](SlotState &s, uint32_t slot_idx) -> int {
-        const uint64_t nc = s.c_count, ny = s.y_count;
-        pack_upto(s, s.c_start + nc, s.y_start + ny);
-        cudaEventRecord(s.start, cp_c);
-        // ---- TPC-C sub-batch
-        if (nc) {
-            const uint64_t l0 = c_line_off[s.c_start], l1 = c_line_off[s.c_start + nc];
-            ltpg_tpcc_batch b{(uint32_t)nc, (uint32_t)(l1 - l0), s.c_start, static_cast<ltpg_tpcc_txn *>(s.c_txns.p),
-                              static_cast<ltpg_tpcc_line *>(s.c_lines.p)};
-            ltpg_set_stream(tc, cp_c);
-            int r = ltpg_batch_upload_tpcc(tc, slot_idx, &b);
-            if (r) return r;
-            cudaEventRecord(up_c, cp_c);
-            cudaStreamWaitEvent(cs_c, up_c, 0);
-            ltpg_set_stream(tc, cs_c);
-            if ((r = ltpg_run_batch(tc, slot_idx, mode))) return r;
-            const uint32_t *dbits;
-            ltpg_commit_bitmap_device(tc, slot_idx, &dbits);
-            cudaMemcpyAsync(s.c_bits.p, dbits, (nc + 31) / 32 * 4, cudaMemcpyDeviceToHost, cs_c);
-            if (rec) {
-                cudaMemcpyAsync(s.c_flags.p, tc->slots[slot_idx].flags, nc, cudaMemcpyDeviceToHost, cs_c);
-                cudaMemcpyAsync(s.c_res.p, tc->slots[slot_idx].results, nc * 8, cudaMemcpyDeviceToHost, cs_c);
-            }
-        }
-        cudaEventRecord(s.done_c, cs_c);
-        // ---- YCSB sub-batch
-        if (ny) {
-            const uint64_t v0 = y_voff[s.y_start], v1 = y_voff[s.y_start + ny];
-            uint32_t *vo = static_cast<uint32_t *>(s.y_voff.p);
-            vo[ny] = (uint32_t)(v1 - v0);
-            ltpg_ycsb_batch b{(uint32_t)ny, ky, sy, (uint32_t)(v1 - v0), static_cast<uint32_t *>(s.y_ops.p), vo,
-                              static_cast<uint64_t *>(s.y_vals.p)};
-            ltpg_set_stream(yc, cp_y);
-            int r = ltpg_batch_upload_ycsb(yc, slot_idx, &b);
-            if (r) return r;
-            cudaEventRecord(up_y, cp_y);
-            cudaStreamWaitEvent(cs_y, up_y, 0);
-            ltpg_set_stream(yc, cs_y);
-            if ((r = ltpg_run_batch(yc, slot_idx, mode))) return r;
-            const uint32_t *dbits;
-            ltpg_commit_bitmap_device(yc, slot_idx, &dbits);
-            cudaMemcpyAsync(s.y_bits.p, dbits, (ny + 31) / 32 * 4, cudaMemcpyDeviceToHost, cs_y);
-            if (rec) {
-                cudaMemcpyAsync(s.y_flags.p, yc->slots[slot_idx].flags, ny, cudaMemcpyDeviceToHost, cs_y);
-                cudaMemcpyAsync(s.y_res.p, yc->slots[slot_idx].results, ny * 8, cudaMemcpyDeviceToHost, cs_y);
-            }
-        }
-        cudaEventRecord(s.done_y, cs_y);
-        s.busy = true;
-        s.c_packed = s.y_packed = 0;
-        if (rec) {
-            rec->batches.push_back(s.c_start);
-            rec->batches.push_back(nc);
-            rec->batches.push_back(s.y_start);
-            rec->batches.push_back(ny);
-        }
-        return LTPG_OK;
-    };
-
-    uint32_t rr = 0;           // next slot in round-robin order (batches complete in order)
-    uint64_t form_c = 0;       // TPC-C requests in the forming batch (the rest are YCSB)
-    bool form_packing = false; // the forming batch is being packed into slots[rr]
-    while (rc == LTPG_OK) {
-        const double t = now_s();
-        // completions
-        for (uint32_t k = 0; k < allowed; ++k) {
-            SlotState &s = slots[(rr + k) % allowed];
-            if (!s.busy) continue;
-            if (cudaEventQuery(s.done_c) == cudaSuccess && cudaEventQuery(s.done_y) == cudaSuccess)
-                complete(s, now_s());
-        }
-        // admission: requests that have arrived join the forming batch
-        uint64_t form_end = next;
-        while (form_end < N && arrival[form_end] <= t && form_end - form_start < cfg->max_batch) {
-            form_c += is_tpcc[form_end];
-            ++form_end;
-        }
-        next = form_end;
-        const uint64_t size = next - form_start;
-        // pack the admitted requests now if the forming batch's slot is free
-        SlotState &fs = slots[rr];
-        if (!fs.busy && size > 0) {
-            if (!form_packing) {
-                fs.c_start = pos_c;
-                fs.y_start = pos_y;
-                fs.c_packed = fs.y_packed = 0;
-                form_packing = true;
-            }
-            pack_upto(fs, pos_c + form_c, pos_y + (size - form_c));
-        }
-        const bool full = size >= cfg->max_batch;
-        const bool due = size > 0 && t - arrival[form_start] >= deadline;
-        const bool drain = next >= N && size > 0;
-        if (full || due || drain) {
-            SlotState &s = slots[rr];
-            if (s.busy) {
-                ++waited_for_slot;  // all slots in flight: the batch keeps forming
+    // ---- the server; each request is submitted at its arrival time
+    ltpg_server_cfg sc{cfg->deadline_ms, cfg->budget_bytes, cfg->max_batch, cfg->mode, cfg->slots, ky};
+    ltpg_server *s = nullptr;
+    int rc = ltpg_server_open(tc, yc, &sc, &s);
+    if (rc) return rc;
+    std::vector<ltpg_request> reqs;
+    reqs.reserve(4096);
+    uint64_t next = 0, pos_c = 0, pos_y = 0;
+    while (rc == LTPG_OK && next < N) {
+        const double t = s->now();
+        reqs.clear();
+        const uint64_t from = next;
+        while (next < N && arrival[next] <= t && reqs.size() < 4096) {
+            ltpg_request q{};
+            if (is_tpcc[next]) {
+                q.workload = LTPG_WORKLOAD_TPCC;
+                q.txn = &c_pool[pos_c];
+                q.lines = c_lines.data() + c_line_off[pos_c];
+                q.n = (uint32_t)(c_line_off[pos_c + 1] - c_line_off[pos_c]);
+                ++pos_c;
             } else {
-                const uint64_t nc = form_c;
-                if (!form_packing) {
-                    s.c_packed = s.y_packed = 0;
-                }
-                s.c_start = pos_c;
-                s.c_count = nc;
-                s.y_start = pos_y;
-                s.y_count = size - nc;
-                s.arrival_first = arrival[form_start];
-                s.t_close = t;
-                for (uint64_t i = form_start; i < next; ++i) wait_sum += t - arrival[i];
-                pos_c += nc;
-                pos_y += size - nc;
-                rc = launch(s, rr);
-                pack_sum += now_s() - t;
-                batches++;
-                batch_sizes += (double)size;
-                form_start = next;
-                form_c = 0;
-                form_packing = false;
-                rr = (rr + 1) % allowed;
+                q.workload = LTPG_WORKLOAD_YCSB;
+                q.ops = y_ops.data() + pos_y * sy;
+                q.vals = y_vals.data() + y_voff[pos_y];
+                q.n = ky;
+                ++pos_y;
+            }
+            reqs.push_back(q);
+            ++next;
+        }
+        rc = reqs.empty() ? progress(s) : submit(s, reqs.data(), (uint32_t)reqs.size(), nullptr, &arrival[from]);
+    }
+    if (rc == LTPG_OK) rc = flush(s);
+    ltpg_serve_record *rec = nullptr;
+    if (rc == LTPG_OK && record) {
+        rec = new (std::nothrow) ltpg_serve_record();
+        if (!rec) rc = LTPG_ERR_NOMEM;
+    }
+    if (rec) {
+        // per request, in submission order: flags and results by type; batch
+        // boundaries as pool ranges per type
+        std::vector<uint8_t> f(N);
+        std::vector<int64_t> r(N);
+        uint32_t got = 0;
+        for (uint64_t i = 0; i < N && rc == LTPG_OK; i += got) {
+            const uint32_t want = (uint32_t)std::min<uint64_t>(N - i, 1u << 20);
+            rc = ltpg_serve_poll(s, i, want, f.data() + i, r.data() + i, &got);
+            if (rc == LTPG_OK && got == 0) rc = LTPG_ERR_STATE;
+        }
+        for (uint64_t i = 0; i < N; ++i) {
+            if (is_tpcc[i]) {
+                rec->c_flags.push_back(f[i]);
+                rec->c_res.push_back(r[i]);
+            } else {
+                rec->y_flags.push_back(f[i]);
+                rec->y_res.push_back(r[i]);
             }
         }
-        if (next >= N && form_start >= N) {
-            bool any = false;
-            for (auto &s : slots) any |= s.busy;
-            if (!any) break;
+        uint64_t cs = 0, ys = 0;
+        for (size_t b = 0; b < s->log_first.size(); ++b) {
+            const uint64_t nc = s->log_c[b], ny = s->log_n[b] - nc;
+            rec->batches.insert(rec->batches.end(), {cs, nc, ys, ny});
+            cs += nc;
+            ys += ny;
         }
     }
-    const double wall = now_s();
-    ltpg_set_stream(tc, nullptr);
-    ltpg_set_stream(yc, nullptr);
-    cudaStreamSynchronize(cs_c);
-    cudaStreamSynchronize(cs_y);
-    for (auto &s : slots) {
-        cudaEventDestroy(s.done_c);
-        cudaEventDestroy(s.done_y);
-        cudaEventDestroy(s.start);
-    }
-    cudaEventDestroy(up_c);
-    cudaEventDestroy(up_y);
-    cudaStreamDestroy(cs_c);
-    cudaStreamDestroy(cp_c);
-    cudaStreamDestroy(cs_y);
-    cudaStreamDestroy(cp_y);
-    if (rc == LTPG_OK) {
-        int r1 = ltpg_sync(tc), r2 = ltpg_sync(yc);
-        rc = r1 ? r1 : r2;
-    }
-    memset(out, 0, sizeof *out);
-    out->submitted = N;
-    out->committed = committed;
-    out->batches = batches;
-    out->slots = allowed;
-    out->waited_for_slot = waited_for_slot;
-    out->wall_s = wall;
-    out->throughput = wall > 0 ? committed / wall : 0;
-    out->mean_batch = batches ? batch_sizes / batches : 0;
-    double sum = 0;
-    for (double v : lat) sum += v;
-    out->mean_ms = lat.empty() ? 0 : sum / lat.size();
-    out->p50_ms = percentile(lat, 0.50);
-    out->p99_ms = percentile(lat, 0.99);
-    out->p999_ms = percentile(lat, 0.999);
-    out->wait_ms = N ? wait_sum * 1e3 / N : 0;
-    out->launch_ms = batches ? pack_sum * 1e3 / batches : 0;
-    out->device_ms = batches ? dev_sum * 1e3 / batches : 0;
-    if (record) *record = rec;
+    const int rc_close = ltpg_server_close(s, out);
+    if (rc == LTPG_OK) rc = rc_close;
+    if (record) *record = rc == LTPG_OK ? rec : nullptr;
+    if (rc != LTPG_OK) delete rec;
     return rc;
 }
 

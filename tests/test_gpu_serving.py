@@ -120,3 +120,101 @@ def test_admission_by_memory_budget():
     finally:
         c.close()
         y.close()
+
+
+def test_caller_requests_same_alone_and_in_the_mix():
+    """Caller-owned requests through ltpg_serve_submit / ltpg_serve_poll: two
+    request sources (a TPC-C client and a YCSB client, interleaved by one
+    driving thread) submit in chunks of varying size with polls in between;
+    results come back by id.  Replaying each logged batch alone, in order, on
+    fresh engines gives every request's flags and result, and the tables."""
+    rng = np.random.default_rng(5)
+    nc, ny = 12000, 15000
+    ctx, clines, coff = _tpcc_pool(nc)
+    yops, yvals, yoff = _ycsb_pool(ny)
+    stride = (YP["ops_per_txn"] + 3) & ~3
+    # the two sources' arrival order, interleaved at random
+    order = np.array([0] * nc + [1] * ny)
+    rng.shuffle(order)
+    reqs, kind_idx = [], []
+    ic = iy = 0
+    for o in order:
+        if o == 0:
+            reqs.append(("tpcc", ctx[ic], clines[coff[ic]:coff[ic + 1]]))
+            kind_idx.append((0, ic))
+            ic += 1
+        else:
+            ops = yops[iy * stride:iy * stride + YP["ops_per_txn"]]
+            reqs.append(("ycsb", ops, yvals[yoff[iy]:yoff[iy + 1]]))
+            kind_idx.append((1, iy))
+            iy += 1
+    c, y = _engines()
+    flags = np.zeros(len(reqs), dtype=np.uint8)
+    results = np.zeros(len(reqs), dtype=np.int64)
+    try:
+        srv = L.Server(c, y, max_batch=3000, deadline_ms=0.3, mode="fused", slots=3, ycsb_ops=YP["ops_per_txn"])
+        pos, got = 0, 0
+        while pos < len(reqs):
+            k = int(rng.integers(1, 700))
+            first = srv.submit(reqs[pos:pos + k])
+            assert first == pos
+            pos += k
+            f, r = srv.poll(got, len(reqs) - got)  # finished requests come back as a prefix of the ids
+            flags[got:got + len(f)] = f
+            results[got:got + len(f)] = r
+            got += len(f)
+        srv.flush()
+        f, r = srv.poll(got, len(reqs) - got)
+        flags[got:got + len(f)] = f
+        results[got:got + len(f)] = r
+        got += len(f)
+        assert got == len(reqs)
+        with pytest.raises(L.LtpgError):  # results already returned are forgotten
+            srv.poll(0, 1)
+        log = srv.batch_log()
+        stats = srv.close()
+        mix_tables = [c.download_table(t) for t in range(abi.TPCC_TABLES)]
+        mix_ycsb = y.download_table(abi.TABLE_YCSB)
+    finally:
+        c.close()
+        y.close()
+    assert sum(n for _, n in log) == len(reqs) and len(log) > 8
+    assert [f for f, _ in log] == list(np.cumsum([0] + [n for _, n in log])[:-1])
+    assert stats["submitted"] == len(reqs) and stats["committed"] == int((flags & abi.FLAG_COMMIT != 0).sum())
+    assert 0 < stats["p50_ms"] <= stats["p99_ms"]
+    c, y = _engines()
+    try:
+        c_base = 0
+        for first, n in log:
+            idx = [kind_idx[i] for i in range(first, first + n)]
+            ci = [j for k, j in idx if k == 0]
+            yi = [j for k, j in idx if k == 1]
+            pos_c = [first + t for t, (k, _) in enumerate(idx) if k == 0]
+            pos_y = [first + t for t, (k, _) in enumerate(idx) if k == 1]
+            if ci:
+                t = ctx[ci].copy()
+                cnt = (coff[np.array(ci) + 1] - coff[ci]).astype(np.int64)
+                t["line_off"] = (np.cumsum(cnt) - cnt).astype(np.uint32)
+                lines = np.concatenate([clines[coff[j]:coff[j + 1]] for j in ci])
+                c.upload(0, TpccBatch(t, lines, txn_base=c_base))
+                c.run_batch(0, "plain")
+                c.sync()
+                assert np.array_equal(c.txn_flags(0, len(ci)), flags[pos_c])
+                assert np.array_equal(c.txn_results(0, len(ci)), results[pos_c])
+                c_base += len(ci)
+            if yi:
+                ops = np.concatenate([yops[j * stride:(j + 1) * stride] for j in yi])
+                nv = np.array([yoff[j + 1] - yoff[j] for j in yi], dtype=np.int64)
+                voff = np.concatenate([[0], np.cumsum(nv)]).astype(np.uint32)
+                vals = np.concatenate([yvals[yoff[j]:yoff[j + 1]] for j in yi] + [np.zeros(0, np.uint64)])
+                y.upload(0, YcsbBatch(ops, voff, vals, len(yi), YP["ops_per_txn"]))
+                y.run_batch(0, "plain")
+                y.sync()
+                assert np.array_equal(y.txn_flags(0, len(yi)), flags[pos_y])
+                assert np.array_equal(y.txn_results(0, len(yi)), results[pos_y])
+        for t in range(abi.TPCC_TABLES):
+            assert np.array_equal(c.download_table(t), mix_tables[t]), t
+        assert np.array_equal(y.download_table(abi.TABLE_YCSB), mix_ycsb)
+    finally:
+        c.close()
+        y.close()
