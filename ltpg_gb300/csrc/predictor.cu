@@ -10,6 +10,9 @@
 //             batch's registration contention");
 //   infer     all 65,536 buckets from batches t-4..t-1;
 //   select    the top-k scores become the staged set (k = staging groups).
+// Six kernels per batch: roll (+ ring advance), training forward, fused
+// backward (+ loss), Adam (+ BF16 copies), inference forward, select (+ step
+// counters).
 // The forward pass runs on the tensor cores (mma.sync m16n8k16, BF16 inputs,
 // FP32 accumulators); backward and Adam are FP32.  The predictor only picks
 // the staged set, which changes speed, never a commit decision.
@@ -35,8 +38,8 @@ struct PredDev {
     uint32_t *ring;                       // P_RING x buckets
     float *scores;                        // buckets
     float *act;                           // training activations: X [S][4], H1 [S][64], H2 [S][64], Y [S], T [S]
-    uint32_t *state;                      // [0] ring position, [1] step, [2] batches seen
-    float *loss;                          // last training loss
+    uint32_t *state;                      // [0] ring position, [1] step, [2] batches seen, [3] blocks done
+    float *loss;                          // [0] last training loss, [1] its running sum over sample tiles
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -202,77 +205,99 @@ __global__ void __launch_bounds__(256) pred_forward(PredDev p, uint32_t n, int m
 // grad layout = packed params.  Loss = mean over samples of (y - t)^2.
 // dz2[s][j] = 2 (y - t) / S * w3[j] * [h2 > 0];  dh1[s][k] = sum_j dz2[s][j] W2[j][k];
 // dz1 = dh1 * [h1 > 0].  The weights used are the BF16 copies the forward used.
-__global__ void pred_backward_rows(PredDev p, uint32_t S, float *__restrict__ dz2, float *__restrict__ dz1) {
+// One kernel: a block walks tiles of PB samples; per tile dz2 and dz1 are made
+// in shared memory, and each thread adds the tile's terms of its parameters
+// (tid, tid + 256, ...) to registers; the block adds its sums to the global
+// gradient once at the end, and its share of the squared error to loss[1].
+constexpr int PB = 16;                                  // samples per tile
+constexpr int P_PER_THREAD = (P_NPARAM + 255) / 256;    // parameters per thread (256 threads)
+
+__global__ void __launch_bounds__(256) pred_backward(PredDev p, uint32_t S) {
     const float *X = p.act, *H1 = X + P_TRAIN * PF, *H2 = H1 + P_TRAIN * PH, *Y = H2 + P_TRAIN * PH, *T = Y + P_TRAIN;
     __shared__ float w2[PH * PH];
+    __shared__ float w3[PH];
+    __shared__ float d2[PB][PH], d1[PB][PH], h1[PB][PH], h2[PB][PH];
+    __shared__ float xs[PB][PF], dys[PB];
+    __shared__ float lsum[8];
     for (int i = threadIdx.x; i < PH * PH; i += blockDim.x) w2[i] = __bfloat162float(p.w2b[i]);
+    for (int i = threadIdx.x; i < PH; i += blockDim.x) w3[i] = p.param[P_W3 + i];
+    float acc[P_PER_THREAD];
+#pragma unroll
+    for (int r = 0; r < P_PER_THREAD; ++r) acc[r] = 0.f;
+    float lacc = 0.f;
+    const uint32_t n_tiles = (S + PB - 1) / PB;
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t s0 = tile * PB;
+        __syncthreads();  // w2 / w3 loaded, or the previous tile consumed
+        if (threadIdx.x < PB) {
+            const uint32_t s = s0 + threadIdx.x;
+            const float e = s < S ? Y[s] - T[s] : 0.f;
+            dys[threadIdx.x] = 2.f * e / (float)S;
+            lacc += e * e;
+            for (int f = 0; f < PF; ++f)  // layer 1 consumed BF16(x)
+                xs[threadIdx.x][f] = s < S ? __bfloat162float(__float2bfloat16_rn(X[s * PF + f])) : 0.f;
+        }
+        for (uint32_t i = threadIdx.x; i < PB * PH; i += blockDim.x) {
+            const uint32_t r = i / PH, j = i % PH, s = s0 + r;
+            h1[r][j] = s < S ? H1[s * PH + j] : 0.f;
+            h2[r][j] = s < S ? H2[s * PH + j] : 0.f;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < PB * PH; i += blockDim.x) {
+            const uint32_t r = i / PH, j = i % PH;
+            d2[r][j] = h2[r][j] > 0.f ? dys[r] * w3[j] : 0.f;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < PB * PH; i += blockDim.x) {
+            const uint32_t r = i / PH, k = i % PH;
+            float a = 0.f;
+#pragma unroll 16
+            for (int j = 0; j < PH; ++j) a += d2[r][j] * w2[j * PH + k];
+            d1[r][k] = h1[r][k] > 0.f ? a : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < P_PER_THREAD; ++q) {
+            const uint32_t i = threadIdx.x + 256u * q;
+            float a = 0.f;
+            if (i < (uint32_t)P_B1) {
+                const uint32_t j = i / PF, f = i % PF;
+                for (int r = 0; r < PB; ++r) a += d1[r][j] * xs[r][f];
+            } else if (i < (uint32_t)P_W2) {
+                for (int r = 0; r < PB; ++r) a += d1[r][i - P_B1];
+            } else if (i < (uint32_t)P_B2) {
+                const uint32_t j = (i - P_W2) / PH, k = (i - P_W2) % PH;
+                for (int r = 0; r < PB; ++r) a += d2[r][j] * h1[r][k];
+            } else if (i < (uint32_t)P_W3) {
+                for (int r = 0; r < PB; ++r) a += d2[r][i - P_B2];
+            } else if (i < (uint32_t)P_B3) {
+                for (int r = 0; r < PB; ++r) a += dys[r] * h2[r][i - P_W3];
+            } else if (i < (uint32_t)P_NPARAM) {
+                for (int r = 0; r < PB; ++r) a += dys[r];
+            }
+            acc[q] += a;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < P_PER_THREAD; ++q) {
+        const uint32_t i = threadIdx.x + 256u * q;
+        if (i < (uint32_t)P_NPARAM && acc[q] != 0.f) atomicAdd(&p.grad[i], acc[q]);
+    }
+    for (int o = 16; o > 0; o >>= 1) lacc += __shfl_xor_sync(FULL, lacc, o);
+    if ((threadIdx.x & 31) == 0) lsum[threadIdx.x >> 5] = lacc;
     __syncthreads();
-    for (uint32_t s = blockIdx.x; s < S; s += gridDim.x) {
-        const float dy = 2.f * (Y[s] - T[s]) / (float)S;
-        __shared__ float d2[PH];
-        for (int j = threadIdx.x; j < PH; j += blockDim.x) {
-            const float v = H2[s * PH + j] > 0.f ? dy * p.param[P_W3 + j] : 0.f;
-            d2[j] = v;
-            dz2[s * PH + j] = v;
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k < PH; k += blockDim.x) {
-            float acc = 0.f;
-            for (int j = 0; j < PH; ++j) acc += d2[j] * w2[j * PH + k];
-            dz1[s * PH + k] = H1[s * PH + k] > 0.f ? acc : 0.f;
-        }
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += lsum[w];
+        atomicAdd(&p.loss[1], t);
     }
 }
 
-// Parameter gradients: sums over samples, one thread per parameter, split over
-// sample chunks (blockIdx.y) and added with atomics.
-__global__ void pred_backward_params(PredDev p, uint32_t S, const float *__restrict__ dz2,
-                                     const float *__restrict__ dz1) {
-    const float *X = p.act, *H1 = X + P_TRAIN * PF, *H2 = H1 + P_TRAIN * PH, *Y = H2 + P_TRAIN * PH, *T = Y + P_TRAIN;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P_NPARAM) return;
-    const uint32_t chunk = (S + gridDim.y - 1) / gridDim.y;
-    const uint32_t s0 = blockIdx.y * chunk, s1 = min(S, s0 + chunk);
-    float acc = 0.f;
-    for (uint32_t s = s0; s < s1; ++s) {
-        float g;
-        if (i < P_B1) {
-            const uint32_t j = i / PF, f = i % PF;  // W1[j][f]: layer 1 consumed BF16(x)
-            g = dz1[s * PH + j] * __bfloat162float(__float2bfloat16_rn(X[s * PF + f]));
-        } else if (i < P_W2) {
-            g = dz1[s * PH + (i - P_B1)];
-        } else if (i < P_B2) {
-            const uint32_t j = (i - P_W2) / PH, k = (i - P_W2) % PH;  // W2[j][k]
-            g = dz2[s * PH + j] * H1[s * PH + k];
-        } else if (i < P_W3) {
-            g = dz2[s * PH + (i - P_B2)];
-        } else if (i < P_B3) {
-            g = 2.f * (Y[s] - T[s]) / (float)S * H2[s * PH + (i - P_W3)];
-        } else {
-            g = 2.f * (Y[s] - T[s]) / (float)S;
-        }
-        acc += g;
-    }
-    atomicAdd(&p.grad[i], acc);
-}
-
-__global__ void pred_loss(PredDev p, uint32_t S) {
-    const float *Y = p.act + P_TRAIN * PF + 2 * P_TRAIN * PH, *T = Y + P_TRAIN;
-    __shared__ float part[256];
-    float acc = 0.f;
-    for (uint32_t s = threadIdx.x; s < S; s += blockDim.x) acc += (Y[s] - T[s]) * (Y[s] - T[s]);
-    part[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *p.loss = part[0] / (float)S;
-}
-
-// Adam (Kingma & Ba, 2015) on the FP32 master parameters, then the BF16 copies.
-__global__ void pred_adam(PredDev p, float lr) {
+// Adam (Kingma & Ba, 2015) on the FP32 master parameters; each updated weight
+// of W1 / W2 is also written to its BF16 copy (the zero padding of W1's K
+// dimension is written once, by pred_cast).  The first thread turns the
+// summed squared error into the step's loss.
+__global__ void pred_adam(PredDev p, float lr, uint32_t S) {
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const uint32_t t = p.state[1] + 1;
     const float c1 = 1.f - powf(b1, (float)t), c2 = 1.f - powf(b2, (float)t);
@@ -282,8 +307,15 @@ __global__ void pred_adam(PredDev p, float lr) {
         const float v = b2 * p.v[i] + (1.f - b2) * g * g;
         p.m[i] = m;
         p.v[i] = v;
-        p.param[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+        const float w = p.param[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+        p.param[i] = w;
         p.grad[i] = 0.f;
+        if (i < (uint32_t)P_B1) p.w1b[(i / PF) * 16 + i % PF] = __float2bfloat16_rn(w);
+        else if (i >= (uint32_t)P_W2 && i < (uint32_t)P_B2) p.w2b[i - P_W2] = __float2bfloat16_rn(w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p.loss[0] = p.loss[1] / (float)S;
+        p.loss[1] = 0.f;
     }
 }
 
@@ -306,67 +338,110 @@ __global__ void pred_step_done(PredDev p, int trained) {
     }
 }
 
-// The batch's counts enter the ring; the counters restart for the next batch.
+// The batch's counts enter the ring and the counters restart for the next
+// batch; the last block to finish advances the ring position.
 __global__ void pred_roll(PredDev p, uint32_t *__restrict__ counts) {
     const uint32_t pos = p.state[0];
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < STAGE_BUCKETS; b += gridDim.x * blockDim.x) {
         p.ring[pos * STAGE_BUCKETS + b] = counts[b];
         counts[b] = 0u;
     }
-}
-__global__ void pred_advance(PredDev p) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) p.state[0] = (p.state[0] + 1) % P_RING;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&p.state[3], 1u) == gridDim.x - 1u) {
+            p.state[3] = 0u;
+            p.state[0] = (pos + 1) % P_RING;
+        }
+    }
 }
 
-// Top-k scores -> staged set, in one block of 1024 threads.  Scores are mapped
-// to order-preserving uint32 keys; two 2048-bin histogram passes find the k-th
-// largest key's top 22 bits; buckets above it are taken, then ties in bucket
-// order until k.
+// Top-k scores -> staged set, in one block of 1024 threads.  Each score becomes
+// a 16-bit order-preserving key (sign, exponent and 7 mantissa bits) kept in
+// shared memory, so the passes below read no global memory: two 256-bin
+// histogram passes find the k-th largest key (one shared atomic per distinct
+// bin of a warp); buckets above it are taken, then ties in bucket order until
+// k.  Thread t owns buckets 64t .. 64t+63 (its bitmap words 2t, 2t+1); their
+// keys are row t of the shared array, rows padded by 4 bytes so that the
+// warp's row walks hit 32 different banks.  Outputs: the bitmap and per-word
+// ranks and the bucket -> group map.  The first thread also ends the
+// predictor step (training step count when `trained`, batches seen).
+constexpr uint32_t SELECT_ROW = 66u;  // 64 keys + 2 of padding
+constexpr uint32_t SELECT_SMEM = STAGE_BUCKETS / 64u * SELECT_ROW * 2u;
+__device__ __forceinline__ uint32_t select_idx(uint32_t b) { return (b >> 6) * SELECT_ROW + (b & 63u); }
+
 __global__ void __launch_bounds__(1024) pred_select(PredDev p, uint32_t k, uint32_t *__restrict__ bits,
-                                                    uint32_t *__restrict__ rank, uint16_t *__restrict__ map) {
-    __shared__ uint32_t hist[2048];
-    __shared__ uint32_t sel_prefix, need_ties;
+                                                    uint32_t *__restrict__ rank, uint16_t *__restrict__ map,
+                                                    int trained) {
+    extern __shared__ __align__(16) uint16_t keys[];  // STAGE_BUCKETS / 64 rows of SELECT_ROW
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t sel_bin, sel_rem;
     __shared__ uint32_t wsum[32];
     const uint32_t tid = threadIdx.x;
-    auto okey = [](float f) {
+    auto okey16 = [](float f) {
         const uint32_t u = __float_as_uint(f);
-        return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        return (uint16_t)(((u & 0x80000000u) ? ~u : (u | 0x80000000u)) >> 16);
     };
-    uint32_t prefix = 0, remaining = k;
-    for (int pass = 0; pass < 2; ++pass) {
-        const int shift = pass == 0 ? 21 : 10;
-        for (uint32_t i = tid; i < 2048; i += blockDim.x) hist[i] = 0;
-        __syncthreads();
-        for (uint32_t b = tid; b < STAGE_BUCKETS; b += blockDim.x) {
-            const uint32_t u = okey(p.scores[b]);
-            if (pass == 0 || (u >> 21) == (prefix >> 21)) atomicAdd(&hist[(u >> shift) & 2047u], 1u);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t acc = 0, bin = 0;
-            for (int i = 2047; i >= 0; --i) {
-                if (acc + hist[i] >= remaining) {
-                    bin = (uint32_t)i;
-                    break;
-                }
-                acc += hist[i];
-            }
-            remaining -= acc;
-            prefix |= bin << shift;
-            sel_prefix = prefix;
-            need_ties = remaining;
-        }
-        __syncthreads();
-        prefix = sel_prefix;
-        remaining = need_ties;
+    // keys of all buckets, loaded 16 bytes a thread, consecutive threads on
+    // consecutive buckets
+    const float4 *src = reinterpret_cast<const float4 *>(p.scores);
+#pragma unroll 4
+    for (uint32_t v = tid; v < STAGE_BUCKETS / 4u; v += blockDim.x) {
+        const float4 f = src[v];
+        uint16_t *k4 = keys + select_idx(4u * v);  // four buckets of one row
+        k4[0] = okey16(f.x);
+        k4[1] = okey16(f.y);
+        k4[2] = okey16(f.z);
+        k4[3] = okey16(f.w);
     }
-    // prefix: top 22 bits of the k-th largest key; `remaining` of the buckets
-    // whose key has that prefix are still needed
-    const uint32_t hi = prefix >> 10;
+    // two passes: the high byte of the k-th largest key, then its low byte
+    uint32_t hi = 0, remaining = k;
+    for (int pass = 0; pass < 2; ++pass) {
+        if (tid < 256) hist[tid] = 0;
+        __syncthreads();
+        for (uint32_t b = tid; b < STAGE_BUCKETS; b += blockDim.x) {  // interleaved
+            const uint32_t u = keys[select_idx(b)];
+            const bool in = pass == 0 || (u >> 8) == hi;
+            const uint32_t bin = !in ? 256u : pass == 0 ? (u >> 8) : (u & 255u);
+            const unsigned peers = __match_any_sync(FULL, bin);
+            if (in && (tid & 31u) == (uint32_t)__ffs(peers) - 1u) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+        }
+        __syncthreads();
+        if (tid < 32) {  // the bin holding the remaining-th largest key: warp-wide suffix sums
+            const uint32_t lo = (31u - tid) * 8u;  // lane 0 holds the highest bins
+            uint32_t c[8], tot = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) tot += (c[i] = hist[lo + i]);
+            uint32_t incl = tot;  // keys in this lane's bins and all higher ones
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                if (tid >= (uint32_t)o) incl += v;
+            }
+            const uint32_t above = incl - tot;  // keys in higher lanes' bins
+            if (above < remaining && incl >= remaining) {
+                uint32_t acc = above, bin = lo;
+                for (int i = 7; i >= 0; --i) {
+                    if (acc + c[i] >= remaining) {
+                        bin = lo + (uint32_t)i;
+                        break;
+                    }
+                    acc += c[i];
+                }
+                sel_bin = bin;
+                sel_rem = remaining - acc;
+            }
+        }
+        __syncthreads();
+        hi = pass == 0 ? sel_bin : (hi << 8) | sel_bin;
+        remaining = sel_rem;
+    }
+    // hi: the k-th largest key; `remaining` of the buckets with that key are
+    // still needed, taken in bucket order (exclusive scan of each thread's
+    // count of such buckets among its 64)
     uint32_t tie_before = 0;
-    {  // ties in bucket order: exclusive scan of tie counts over the 64 buckets each thread owns
+    {
         uint32_t mine = 0;
-        for (uint32_t b = tid * 64; b < tid * 64 + 64; ++b) mine += (okey(p.scores[b]) >> 10) == hi;
+        for (uint32_t i = 0; i < 64; ++i) mine += keys[tid * SELECT_ROW + i] == hi;
         uint32_t incl = mine;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t v = __shfl_up_sync(FULL, incl, o);
@@ -388,8 +463,7 @@ __global__ void __launch_bounds__(1024) pred_select(PredDev p, uint32_t k, uint3
     // bitmap words: thread owns buckets tid*64 .. tid*64+63 = words 2 tid, 2 tid + 1
     uint32_t word[2] = {0u, 0u};
     for (uint32_t i = 0; i < 64; ++i) {
-        const uint32_t b = tid * 64 + i;
-        const uint32_t u = okey(p.scores[b]) >> 10;
+        const uint32_t u = keys[tid * SELECT_ROW + i];
         bool take = u > hi;
         if (u == hi) {
             take = tie_before < remaining;
@@ -421,10 +495,17 @@ __global__ void __launch_bounds__(1024) pred_select(PredDev p, uint32_t k, uint3
     const uint32_t r0 = wsum[tid >> 5] + incl - mine;
     rank[2 * tid] = r0;
     rank[2 * tid + 1] = r0 + c0;
+    // the map, row by row into the keys' place, then out in bucket order
     uint32_t r = r0;
     for (uint32_t i = 0; i < 64; ++i) {
         const bool on = (word[i >> 5] >> (i & 31u)) & 1u;
-        map[tid * 64 + i] = on ? (uint16_t)r++ : (uint16_t)STAGE_NONE;
+        keys[tid * SELECT_ROW + i] = on ? (uint16_t)r++ : (uint16_t)STAGE_NONE;
+    }
+    __syncthreads();
+    for (uint32_t b = tid; b < STAGE_BUCKETS; b += blockDim.x) map[b] = keys[select_idx(b)];
+    if (tid == 0) {
+        if (trained) p.state[1] += 1;
+        p.state[2] += 1;
     }
 }
 
@@ -434,7 +515,7 @@ using namespace ltpg;
 
 struct ltpg_predictor_state {
     PredDev d{};
-    float *dz2 = nullptr, *dz1 = nullptr, *io = nullptr;  // backward scratch, test io buffer
+    float *io = nullptr;  // test io buffer
     float lr = 3e-3f;
     uint32_t train_every = 1;
     uint64_t steps_host = 0;
@@ -500,9 +581,8 @@ int ltpg_predictor_enable(ltpg_ctx *c, const ltpg_predictor_cfg *cfg) {
         PCK(cudaMalloc(&d.scores, STAGE_BUCKETS * 4));
         PCK(cudaMalloc(&d.act, (size_t)P_TRAIN * (PF + 2 * PH + 2) * 4));
         PCK(cudaMalloc(&d.state, 16));
-        PCK(cudaMalloc(&d.loss, 4));
-        PCK(cudaMalloc(&P->dz2, (size_t)P_TRAIN * PH * 4));
-        PCK(cudaMalloc(&P->dz1, (size_t)P_TRAIN * PH * 4));
+        PCK(cudaMalloc(&d.loss, 8));
+        PCK(cudaFuncSetAttribute(pred_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SELECT_SMEM));
         PCK(cudaMalloc(&P->io, (size_t)P_TRAIN * 8 * 4));
     }
     ltpg_predictor_state *P = c->pred;
@@ -515,7 +595,7 @@ int ltpg_predictor_enable(ltpg_ctx *c, const ltpg_predictor_cfg *cfg) {
     PCK(cudaMemset(P->d.ring, 0, (size_t)P_RING * STAGE_BUCKETS * 4));
     PCK(cudaMemset(P->d.scores, 0, STAGE_BUCKETS * 4));
     PCK(cudaMemset(P->d.state, 0, 16));
-    PCK(cudaMemset(P->d.loss, 0, 4));
+    PCK(cudaMemset(P->d.loss, 0, 8));
     pred_cast<<<32, 256, 0, c->stream>>>(P->d);
     PCK(cudaGetLastError());
     P->lr = cfg->lr > 0.f ? cfg->lr : 3e-3f;
@@ -575,11 +655,11 @@ int ltpg_predictor_gradients(ltpg_ctx *c, const float *host_x, const float *host
     float *T = P->d.act + P_TRAIN * PF + 2 * P_TRAIN * PH + P_TRAIN;
     PCK(cudaMemcpyAsync(T, host_t, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
     PCK(cudaMemsetAsync(P->d.grad, 0, P_NPARAM * 4, c->stream));
-    pred_backward_rows<<<256, 64, 0, c->stream>>>(P->d, n, P->dz2, P->dz1);
-    pred_backward_params<<<dim3((P_NPARAM + 255) / 256, 16), 256, 0, c->stream>>>(P->d, n, P->dz2, P->dz1);
+    pred_backward<<<64, 256, 0, c->stream>>>(P->d, n);
     PCK(cudaGetLastError());
     PCK(cudaMemcpyAsync(host_grad, P->d.grad, P_NPARAM * 4, cudaMemcpyDeviceToHost, c->stream));
     PCK(cudaMemsetAsync(P->d.grad, 0, P_NPARAM * 4, c->stream));
+    PCK(cudaMemsetAsync(P->d.loss + 1, 0, 4, c->stream));
     return ltpg_sync(c);
 }
 
@@ -590,31 +670,26 @@ namespace ltpg {
 cudaError_t predictor_after_batch(ltpg_ctx *c) {
     ltpg_predictor_state *P = c->pred;
     if (!P || !c->pred_on) return cudaSuccess;
+    // roll (and advance the ring), train, infer, select (and end the step)
     pred_roll<<<64, 256, 0, c->stream>>>(P->d, c->bucket_counts);
-    count_launch(c);
-    pred_advance<<<1, 32, 0, c->stream>>>(P->d);
     count_launch(c);
     int trained = 0;
     if (c->pred_train) {
         pred_forward<<<64, 256, 0, c->stream>>>(P->d, P_TRAIN, 1, nullptr, nullptr);
-        pred_loss<<<1, 256, 0, c->stream>>>(P->d, P_TRAIN);
-        pred_backward_rows<<<256, 64, 0, c->stream>>>(P->d, P_TRAIN, P->dz2, P->dz1);
-        pred_backward_params<<<dim3((P_NPARAM + 255) / 256, 16), 256, 0, c->stream>>>(P->d, P_TRAIN, P->dz2,
-                                                                                     P->dz1);
-        pred_adam<<<32, 256, 0, c->stream>>>(P->d, P->lr);
-        pred_cast<<<32, 256, 0, c->stream>>>(P->d);
-        count_launch(c, 6);
+        pred_backward<<<64, 256, 0, c->stream>>>(P->d, P_TRAIN);
+        pred_adam<<<18, 256, 0, c->stream>>>(P->d, P->lr, P_TRAIN);
+        count_launch(c, 3);
         trained = 1;
     }
-    pred_forward<<<c->sm_count * 2, 256, 0, c->stream>>>(P->d, STAGE_BUCKETS, 0, nullptr, nullptr);
+    pred_forward<<<c->sm_count, 256, 0, c->stream>>>(P->d, STAGE_BUCKETS, 0, nullptr, nullptr);
     count_launch(c);
     if (c->stage_on) {
         const uint32_t ways = c->launch_y.ways ? c->launch_y.ways : 4u;
-        pred_select<<<1, 1024, 0, c->stream>>>(P->d, STAGE_MAX_ENTRIES / ways, c->stage_bits, c->stage_rank,
-                                               c->stage_map);
-        count_launch(c);
+        pred_select<<<1, 1024, SELECT_SMEM, c->stream>>>(P->d, STAGE_MAX_ENTRIES / ways, c->stage_bits,
+                                                         c->stage_rank, c->stage_map, trained);
+    } else {
+        pred_step_done<<<1, 32, 0, c->stream>>>(P->d, trained);
     }
-    pred_step_done<<<1, 32, 0, c->stream>>>(P->d, trained);
     count_launch(c);
     return cudaGetLastError();
 }
@@ -626,7 +701,7 @@ void predictor_free(ltpg_ctx *c) {
     if (!P) return;
     for (void *ptr : {(void *)P->d.param, (void *)P->d.m, (void *)P->d.v, (void *)P->d.grad, (void *)P->d.w1b,
                       (void *)P->d.w2b, (void *)P->d.ring, (void *)P->d.scores, (void *)P->d.act,
-                      (void *)P->d.state, (void *)P->d.loss, (void *)P->dz2, (void *)P->dz1, (void *)P->io})
+                      (void *)P->d.state, (void *)P->d.loss, (void *)P->io})
         if (ptr) cudaFree(ptr);
     delete P;
     c->pred = nullptr;
