@@ -881,7 +881,7 @@ def main():
     # the TPC-C headline workload beside the YCSB one, with the YCSB run's
     # access-pattern ceilings for its atomic roofline
     tp = None
-    if w["kind"] == "ycsb" and not args.no_tpcc:
+    if args.workload == "ycsb_hc" and not args.no_tpcc:
         wt = dict(WORKLOADS["tpcc"], key="tpcc")
         r2, ex2, e2e2, b2 = tpcc_bench(args, wt, dist)
         r2["ceilings"] = res.get("ceilings")
@@ -893,7 +893,7 @@ def main():
                                   "sample": f"{min(args.cpu_batches_tpcc, len(b2))} whole batches of "
                                             f"{wt['n_txn']} txn in order, single-threaded oracle replay, {s_:.1f} s"}
     sweep = None
-    if w["kind"] == "ycsb" and not args.no_sweep:
+    if args.workload == "ycsb_hc" and not args.no_sweep:
         sweep = {}
         ws_ = dict(w, n_batches=min(w["n_batches"], 8))
         for th in [0.0, 0.6, 0.8, 0.99]:
