@@ -25,3 +25,15 @@ def test_ycsb_byte_model(k, u):
     lo, hi = bench.ycsb_bytes_per_txn(k, u, 0.25, late=3), bench.ycsb_bytes_per_txn(k, u, 0.75, late=3)
     assert lo[0] == hi[0] and lo[1] == hi[1]
     assert hi[2] - lo[2] == pytest.approx(0.5 * (4 * k + 80 * (1 - u) * k))
+
+
+@pytest.mark.parametrize("n_slots,steps,start", [(32, 20, 5), (32, 400, 20), (8, 8, 0), (8, 3, 7), (1, 5, 0)])
+def test_step_chunks_cover_the_steps_in_slot_order(n_slots, steps, start):
+    """The timed region's calls: consecutive slots from `start`, wrapping at
+    n_slots, no call past the last slot.  The graph warm-up runs each distinct
+    call once, so the timed region holds no capture."""
+    chunks = bench.step_chunks(n_slots, steps, start)
+    slots = [s + j for s, c in chunks for j in range(c)]
+    assert slots == [(start + i) % n_slots for i in range(steps)]
+    assert all(s + c <= n_slots and c > 0 for s, c in chunks)
+    assert len(set(chunks)) <= 3
