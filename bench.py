@@ -10,11 +10,14 @@ bitmaps and table images.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload ycsb_hc|ycsb_small|tpcc|...] [--theta T] [--no-sweep] [--no-tpcc]
+                  [--no-small]
 
 The default line also carries the TPC-C W=64 NewOrder+Payment workload (key
 "tpcc": tuned and plain, bit-exactness, end to end, HBM and atomic
-rooflines, CPU baseline) and the YCSB theta sweep 0 / 0.6 / 0.8 / 0.99 (key
-"theta_sweep", tuned against plain).
+rooflines, CPU baseline), the YCSB theta sweep 0 / 0.6 / 0.8 / 0.99 (key
+"theta_sweep", tuned against plain) and the small-batch YCSB workload (key
+"small_batches": 65,536 transactions x 10 ops on 1 M records, tuned against
+plain).
 
 --impl reference times the reference protocol's CPU replay (the oracle port,
 all host threads) on the same workload; the reference has no CPU implementation
@@ -75,6 +78,7 @@ def parse():
     ap.add_argument("--workload", default="ycsb_hc", choices=sorted(WORKLOADS))
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--mode", default="graph", choices=["fused", "graph", "persistent"])
+    ap.add_argument("--no-small", action="store_true", help="skip the small-batch (65,536 txn) record")
     ap.add_argument("--no-sweep", action="store_true", help="skip the theta 0/0.6/0.8/0.99 sweep (YCSB)")
     ap.add_argument("--no-tpcc", action="store_true", help="skip the TPC-C W=64 record of the YCSB line")
     ap.add_argument("--cpu-batches-tpcc", type=int, default=3,
@@ -437,26 +441,25 @@ def ycsb_bench(args, w, theta, dist, want_extras=True):
                 "red_min_random_G_per_s": eng.microbench("red_random", 16_000_000) / 1e9,
                 "red_min_one_slot_G_per_s": eng.microbench("red_hot", 1_000_000) / 1e9,
             }
-        # bit-exactness of the tuned path against the plain path on the first batches
-        exact = True
-        if want_extras:
-            ref = {}
-            for mode in ["plain", args.mode]:
-                eng.load_ycsb(SEED, w["n_records"])
-                outs = []
-                for i in range(4):
-                    eng.upload(0, batches[i])
-                    eng.run_batch(0, mode if mode != "graph" else "graph")
-                    eng.sync()
-                    outs.append(eng.commit_bitmap(0, w["n_txn"]))
-                    # results of the committed transactions (with late reads an
-                    # aborted transaction's result is 0 by definition)
-                    com = (eng.txn_flags(0, w["n_txn"]) & L.FLAG_COMMIT) != 0
-                    outs.append(eng.txn_results(0, w["n_txn"])[com])
-                img = eng.download_table(L.TABLE_YCSB)
-                ref[mode] = (outs, int(np.bitwise_xor.reduce(img)), int(img.sum()))
-            a, b = ref["plain"], ref[args.mode]
-            exact = all(np.array_equal(x, y) for x, y in zip(a[0], b[0])) and a[1:] == b[1:]
+        # bit-exactness of the tuned path against the plain path on the first
+        # batches (four with the extras, two for the sweep and the small batches)
+        ref = {}
+        for mode in ["plain", args.mode]:
+            eng.load_ycsb(SEED, w["n_records"])
+            outs = []
+            for i in range(min(len(batches), 4 if want_extras else 2)):
+                eng.upload(0, batches[i])
+                eng.run_batch(0, mode if mode != "graph" else "graph")
+                eng.sync()
+                outs.append(eng.commit_bitmap(0, w["n_txn"]))
+                # results of the committed transactions (with late reads an
+                # aborted transaction's result is 0 by definition)
+                com = (eng.txn_flags(0, w["n_txn"]) & L.FLAG_COMMIT) != 0
+                outs.append(eng.txn_results(0, w["n_txn"])[com])
+            img = eng.download_table(L.TABLE_YCSB)
+            ref[mode] = (outs, int(np.bitwise_xor.reduce(img)), int(img.sum()))
+        a, b = ref["plain"], ref[args.mode]
+        exact = all(np.array_equal(x, y) for x, y in zip(a[0], b[0])) and a[1:] == b[1:]
         # end to end through the host-buffer C-ABI call (pinned host batch, H2D + run + bitmap D2H)
         e2e = None
         if want_extras:
@@ -923,6 +926,22 @@ def main():
             p_v = reduce_sum(dist, r["plain"]["commits"]) / reduce_max(dist, r["plain"]["secs"])
             sweep[str(th)] = {"tuned": t_v, "plain": p_v, "speedup": t_v / p_v if p_v else None,
                               "bit_exact_tuned_vs_plain": bool(ex), "launch": r.get("launch")}
+    # small batches (65,536 transactions on a 1 M-record table): the
+    # latency-bound shape, more steps so that the timed region is not a few
+    # launches long
+    small = None
+    if args.workload == "ycsb_hc" and not args.no_small:
+        wsm = dict(WORKLOADS["ycsb_small"], key="ycsb_small")
+        a2 = argparse.Namespace(**vars(args))
+        a2.steps, a2.warmup = max(args.steps, 320), max(args.warmup, 32)
+        r, ex, _, _ = ycsb_bench(a2, wsm, wsm["theta"], dist, want_extras=False)
+        t_s, p_s = reduce_max(dist, r[args.mode]["secs"]), reduce_max(dist, r["plain"]["secs"])
+        t_v = reduce_sum(dist, r[args.mode]["commits"]) / t_s
+        p_v = reduce_sum(dist, r["plain"]["commits"]) / p_s
+        small = {"workload": wsm["name"], "tuned": t_v, "plain": p_v, "speedup": t_v / p_v if p_v else None,
+                 "ms_per_batch_tuned": t_s * 1e3 / a2.steps, "ms_per_batch_plain": p_s * 1e3 / a2.steps,
+                 "steps": a2.steps, "warmup": a2.warmup, "bit_exact_tuned_vs_plain": bool(ex),
+                 "launch": r.get("launch")}
     if rank != 0:
         return
     B = w["n_txn"]
@@ -955,6 +974,8 @@ def main():
         line["tpcc"] = tp
     if sweep is not None:
         line["theta_sweep"] = sweep
+    if small is not None:
+        line["small_batches"] = small
     if not args.no_predictor and w["kind"] == "ycsb" and w["n_txn"] >= (1 << 18):
         line["predictor"] = predictor_section(w, batches)
     if not args.no_reference_gpu and args.workload == "ycsb_hc":
