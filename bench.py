@@ -1109,15 +1109,20 @@ def serving_section(args):
 
 
 def predictor_section(w, batches):
-    """Predictor-guided staging on the benchmark stream: staging hit rate and
-    execute-kernel time, trained vs untrained vs no staging, with the slot
-    filter off (the warp-aggregated path the predictor complements) and on."""
+    """Predictor-guided staging on the benchmark stream: staging hit rate,
+    execute-kernel time and whole batches (the predictor's own step included:
+    device time per batch and committed txn/s), trained vs untrained vs no
+    staging, with the slot filter off (the warp-aggregated path the predictor
+    complements) and on.  Every variant's commit bitmaps and final table are
+    compared with the no-staging run of the same filter setting."""
+    import torch
     import ltpg_gb300 as L
     out = {}
     n_slots = 8
     for filt in [0, 1]:
-        for name, kw in [("trained", dict(train=True, stage=True)), ("untrained", dict(train=False, stage=True)),
-                         ("no_staging", None)]:
+        ref = None
+        for name, kw in [("no_staging", None), ("trained", dict(train=True, stage=True)),
+                         ("untrained", dict(train=False, stage=True))]:
             e = L.Engine(device=0, n_slots=n_slots, max_txn=w["n_txn"], max_ops_per_txn=w["ops"])
             try:
                 e.load_ycsb(SEED, w["n_records"])
@@ -1125,18 +1130,35 @@ def predictor_section(w, batches):
                 if kw:
                     e.predictor(enable=True, seed=7, **kw)
                 e.set_profiling(True)
-                hits, ms = [], []
+                stream = torch.cuda.ExternalStream(e.stream())
+                hits, ms, batch_ms, commits, bits = [], [], [], 0, []
                 for i, b in enumerate(batches[:24]):
                     e.upload(i % n_slots, b)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
                     e.run_batch(i % n_slots, "fused")
+                    e1.record(stream)
                     e.sync()
+                    torch.cuda.synchronize()
+                    bits.append(e.commit_bitmap(i % n_slots, b.n_txn))
                     if i >= 8:
-                        hits.append(e.stats(i % n_slots)["staged_ops"] / (b.n_txn * w["ops"]))
+                        st = e.stats(i % n_slots)
+                        hits.append(st["staged_ops"] / (b.n_txn * w["ops"]))
                         ms.append(e.kernel_times(i % n_slots)[0])
-                out[f"filter{filt}_{name}"] = {"staging_hit_rate": float(np.mean(hits)),
-                                               "execute_ms": float(np.mean(ms))}
+                        batch_ms.append(e0.elapsed_time(e1))
+                        commits += int(st["commits"])
+                img = e.download_table(L.TABLE_YCSB)
+                got = (bits, int(np.bitwise_xor.reduce(img)), int(img.sum()))
+                if ref is None:
+                    ref = got
+                rec = {"staging_hit_rate": float(np.mean(hits)), "execute_ms": float(np.mean(ms)),
+                       "batch_ms": float(np.mean(batch_ms)),
+                       "committed_per_s": commits / (float(np.sum(batch_ms)) * 1e-3),
+                       "bit_exact_vs_no_staging": bool(all(np.array_equal(x, y) for x, y in zip(got[0], ref[0]))
+                                                       and got[1:] == ref[1:])}
                 if kw and kw["train"]:
-                    out[f"filter{filt}_{name}"]["loss"] = e.predictor_stats()["loss"]
+                    rec["loss"] = e.predictor_stats()["loss"]
+                out[f"filter{filt}_{name}"] = rec
             finally:
                 e.close()
     return out
