@@ -202,6 +202,7 @@ int ltpg_destroy(ltpg_ctx *c) {
     dev_free(c->ycsb.rows);
     dev_free(c->ycsb.reg);
     dev_free(c->ycsb.wbits);
+    dev_free(c->ycsb.upd);
     for (auto &t : c->tpcc.tab) dev_free(t);
     dev_free(c->tpcc.reg);
     dev_free(c->tpcc.name_idx);
@@ -365,6 +366,12 @@ int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, ui
         CK(dev_alloc(&s->vals, cap_vals), "alloc vals");
         s->cap_ops = cap_ops;
         s->cap_vals = cap_vals;
+        if (c->ycsb.upd_cap < cap_vals) {
+            dev_free(c->ycsb.upd);
+            c->ycsb.upd_cap = 0;
+            CK(dev_alloc(&c->ycsb.upd, cap_vals), "alloc update list");
+            c->ycsb.upd_cap = cap_vals;
+        }
         s->cap_txn_y = c->cfg.max_txn;
     }
     int r = ensure_outputs(c, *s, n_txn);

@@ -59,6 +59,11 @@ struct YcsbDb {
     uint64_t *rows = nullptr;  // n * 10 u64
     RegSlot *reg = nullptr;    // n
     uint32_t *wbits = nullptr; // ceil(n / 32): keys with a writer in the batch (write-first registration)
+    // write-first registration: entry u = {TID, op word} of a batch's u-th
+    // update (u = its value index), so that the check and the write-back walk
+    // the updates alone; as many entries as a slot has values
+    uint2 *upd = nullptr;
+    uint64_t upd_cap = 0;
 };
 
 struct TpccDb {

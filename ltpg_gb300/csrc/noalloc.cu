@@ -29,7 +29,8 @@ __global__ void ycsb_check_plain(const uint32_t *__restrict__ ops, uint32_t B, u
                                  uint8_t *__restrict__ flags, DevCtl *ctl);
 __global__ void ycsb_writeback_plain(const uint8_t *__restrict__ flags, uint32_t B, const uint32_t *__restrict__ ops,
                                      uint32_t k, uint32_t stride, const uint32_t *__restrict__ val_off,
-                                     const uint64_t *__restrict__ vals, uint64_t *__restrict__ rows, uint64_t n,
+                                     const uint64_t *__restrict__ vals, uint64_t vals_cap,
+                                     uint64_t *__restrict__ rows, uint64_t n,
                                      uint32_t *__restrict__ bitmap, DevStats *st, DevCtl *ctl);
 }  // namespace ltpg
 
@@ -120,8 +121,9 @@ extern "C" int ltpg_ycsb_batch_noalloc(int device, uint64_t *rows, uint64_t n_re
     if ((r = reserve_epoch(d, s)) != LTPG_OK) return r;
     ycsb_exec_plain<<<grid, tile * k, 0, s>>>(ops, n_txn, k, stride, tile, rows, n_records, d->reg, results, d->ctl);
     ycsb_check_plain<<<grid, tile * k, 0, s>>>(ops, n_txn, k, stride, tile, d->reg, n_records, flags, d->ctl);
-    ycsb_writeback_plain<<<(n_txn + 255) / 256, 256, 0, s>>>(flags, n_txn, ops, k, stride, val_off, vals, rows,
-                                                             n_records, bitmap, d->stats, d->ctl);
+    // the caller's vals hold val_off[n_txn] values, the bound the kernel reads
+    ycsb_writeback_plain<<<(n_txn + 255) / 256, 256, 0, s>>>(flags, n_txn, ops, k, stride, val_off, vals, ~0ull,
+                                                             rows, n_records, bitmap, d->stats, d->ctl);
     if (cudaGetLastError() != cudaSuccess) return LTPG_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return LTPG_ERR_CUDA;
     uint32_t err = 0;

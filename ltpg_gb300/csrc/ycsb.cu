@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) ycsb_check_plain(const uint32_t *__restri
 __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__restrict__ flags, uint32_t B,
                                                             const uint32_t *__restrict__ ops, uint32_t k,
                                                             uint32_t stride, const uint32_t *__restrict__ val_off,
-                                                            const uint64_t *__restrict__ vals,
+                                                            const uint64_t *__restrict__ vals, uint64_t vals_cap,
                                                             uint64_t *__restrict__ rows, uint64_t n,
                                                             uint32_t *__restrict__ bitmap, DevStats *st,
                                                             DevCtl *ctl) {
@@ -131,12 +131,20 @@ __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__res
         if (bwaw) red_add_u64(&st->waw, __popc(bwaw));
     }
     if (com && val_off[t + 1] != val_off[t]) {
+        // value indices stay below the batch's value count and the buffer's
+        // capacity: offsets that disagree with the op words (a malformed
+        // batch) are reported, not followed out of bounds
+        const uint64_t nv = min((uint64_t)val_off[B], vals_cap);
         uint32_t v = val_off[t];
         const uint32_t *w = ops + (uint64_t)t * stride;
         for (uint32_t j = 0; j < k; ++j) {
             const uint32_t x = w[j];
             if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
             const uint32_t key = ycsb_key(x), f = ycsb_field(x);
+            if (v >= nv) {
+                report_error(ctl, DERR_BOUNDS, t);
+                break;
+            }
             if (key < n && f < LTPG_YCSB_FIELDS) rows[(uint64_t)key * LTPG_YCSB_FIELDS + f] = vals[v];
             ++v;
         }
@@ -161,7 +169,8 @@ cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase) {
                                                              c->ycsb.n, s.flags, c->ctl);
     } else {
         ycsb_writeback_plain<<<(B + 255) / 256, 256, 0, c->stream>>>(s.flags, B, s.ops, s.k, s.stride, s.val_off,
-                                                                     s.vals, c->ycsb.rows, c->ycsb.n, s.bitmap,
+                                                                     s.vals, s.cap_vals, c->ycsb.rows, c->ycsb.n,
+                                                                     s.bitmap,
                                                                      s.stats, c->ctl);
     }
     return cudaGetLastError();

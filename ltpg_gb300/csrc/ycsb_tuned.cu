@@ -49,6 +49,9 @@ struct YcsbTunedArgs {
     uint32_t late; // late reads: 0 off, 1 in the check kernel's tiles, 2 in a kernel of their own,
                    // 3 write-first registration
     uint32_t *wbits;  // write-first: one bit per key, set for keys an update of the batch writes
+    uint2 *upd;        // write-first update list: entry u = {TID, op word} of the u-th update (0 entries: none)
+    uint64_t upd_cap;  // entries of the update list
+    uint64_t vals_cap; // values the slot holds (bound of every value index)
 };
 
 __device__ __forceinline__ uint64_t ld_ca_u64(const unsigned long long *p) {
@@ -166,6 +169,9 @@ __device__ __forceinline__ void exec_tiles(const YcsbTunedArgs &a, unsigned long
 __device__ __forceinline__ void write_txn_updates(const YcsbTunedArgs &a, uint32_t t) {
     uint32_t v = a.val_off[t];
     if (v == a.val_off[t + 1]) return;
+    // value indices stay below the batch's value count and the slot's
+    // capacity: offsets that disagree with the op words are reported
+    const uint64_t nv = min((uint64_t)__ldg(a.val_off + a.B), a.vals_cap);
     const uint4 *tw = reinterpret_cast<const uint4 *>(a.ops + (uint64_t)t * a.stride);
     for (uint32_t q4 = 0; q4 < a.stride / 4u; ++q4) {
         const uint4 w4 = ld_nc_u4(tw + q4);
@@ -175,6 +181,10 @@ __device__ __forceinline__ void write_txn_updates(const YcsbTunedArgs &a, uint32
             const uint32_t x = words[q];
             if (ycsb_is_pad(x) || !ycsb_is_update(x)) continue;
             const uint32_t key = ycsb_key(x), fld = ycsb_field(x);
+            if (v >= nv) {
+                report_error(a.ctl, DERR_BOUNDS, t);
+                return;
+            }
             if (key < a.n && fld < LTPG_YCSB_FIELDS) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = a.vals[v];
             ++v;
         }
@@ -382,11 +392,46 @@ __device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key
     return wmin < t;
 }
 
+// The update list: the batch's u-th update (u = its value index, val_off[t]
+// + its rank among transaction t's updates) is stored as {t, op word}, so that
+// the check and the write-back walk the updates alone instead of every op word.
+// The stride / 4 op vectors of a transaction are consecutive lanes of one warp
+// (stride / 4 a power of two <= 8, aligned in the warp); a segmented scan over
+// them gives each lane the updates of the transaction's earlier vectors.  The
+// transaction's last lane checks its update count against its value range:
+// the list positions are only as good as val_off, so a batch whose offsets
+// disagree with its op words is reported (LTPG_ERR_BOUNDS) and its positions
+// are never used past the list.  Called by whole warps.
+__device__ __forceinline__ void wf_list_updates(const YcsbTunedArgs &a, bool act, uint32_t t, const uint32_t *words) {
+    const uint32_t vpt = a.stride / 4u, seg = (threadIdx.x & 31u) & (vpt - 1u);
+    const uint32_t off = act ? __ldg(a.val_off + t) : 0u;
+    const uint32_t end = act && seg == vpt - 1u ? __ldg(a.val_off + t + 1) : 0u;
+    uint32_t n_upd = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n_upd += (!ycsb_is_pad(words[q]) && ycsb_is_update(words[q])) ? 1u : 0u;
+    uint32_t incl = n_upd;
+    for (uint32_t o = 1; o < vpt; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(FULL, incl, o);
+        if (seg >= o) incl += x;
+    }
+    if (act && seg == vpt - 1u && end - off != incl) report_error(a.ctl, DERR_BOUNDS, t);
+    uint64_t u = (uint64_t)off + (incl - n_upd);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (!act || ycsb_is_pad(words[q]) || !ycsb_is_update(words[q])) continue;
+        if (u < a.upd_cap) a.upd[u] = make_uint2(t, words[q]);
+        else report_error(a.ctl, DERR_BOUNDS, t);
+        ++u;
+    }
+}
+
 // (2) reads: four op words per thread (one 16-byte load); the writer-bitmap
 // words of the thread's reads are loaded together, then the slots of those
 // with a writer; the RAW bit is OR-ed into the transaction's flag byte
 // (zeroed by (1)) with a 32-bit atomic.
-template <bool kCoh>
+// kList: the pass also writes the update list (wf_list_updates); its stores
+// wait behind the slot loads this pass is bound by.
+template <bool kCoh, bool kList = false>
 __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32_t epoch) {
     const uint64_t tag = slot_tag(epoch);
     const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
@@ -401,6 +446,7 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
         const uint32_t t = act ? (uint32_t)(v * 4u / a.stride) : 0xFFFFFFFFu;
         const unsigned long long mine = tag | t;
         const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
+        if (kList) wf_list_updates(a, act, t, words);
         bool rd[4];
         uint32_t bits[4];
 #pragma unroll
@@ -479,6 +525,51 @@ template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads<false>(a, a.ctl->epoch); }
 template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_wf_check(YcsbTunedArgs a) { wf_check<false>(a, a.ctl->epoch); }
+
+// ---- write-first with the update list (stride / 4 a power of two <= 8) --------
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_reads_list(YcsbTunedArgs a) {
+    wf_register_reads<false, true>(a, a.ctl->epoch);
+}
+
+// Entries of the batch's update list: val_off[B], bounded by the list.
+__device__ __forceinline__ uint64_t upd_count(const YcsbTunedArgs &a) {
+    const uint64_t n = __ldg(a.val_off + a.B);
+    return n < a.upd_cap ? n : a.upd_cap;
+}
+
+// (3) over the update list: each update's WAR / WAW, OR-ed into its
+// transaction's flag byte.  Four entries per thread and step, their entry and
+// slot loads issued together.
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_check_list(YcsbTunedArgs a) {
+    const uint32_t epoch = a.ctl->epoch;
+    const uint64_t nu = upd_count(a);
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t u0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u0 < nu; u0 += 4 * step) {
+        uint2 e[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t u = u0 + (uint64_t)q * step;
+            e[q] = u < nu ? __ldg(a.upd + u) : make_uint2(0xFFFFFFFFu, 0u);
+        }
+        bool ok[4];
+        ulonglong2 sl[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            ok[q] = e[q].x < a.B && ycsb_key(e[q].y) < a.n;
+            sl[q] = ok[q] ? ld_slot(a.reg + ycsb_key(e[q].y)) : make_ulonglong2(~0ull, ~0ull);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t f = 0;
+            if (slot_min(sl[q].x, epoch) < e[q].x) f |= LTPG_FLAG_WAR;
+            if (slot_min(sl[q].y, epoch) < e[q].x) f |= LTPG_FLAG_WAW;
+            if (ok[q] && f)
+                atomicOr(reinterpret_cast<unsigned *>(a.flags) + (e[q].x >> 2), f << (8u * (e[q].x & 3u)));
+        }
+    }
+}
 
 // ---- check + write-back over all tiles assigned to this block ------------------
 // fl: tile flags.  kLate = 0: the third pass stores the committed updates;
@@ -934,7 +1025,7 @@ __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
 // conflict bits only, and this pass makes the commit decision and writes the
 // final flags, the bitmap (a warp's ballot over 32 consecutive transactions is
 // one bitmap word) and the counters.
-template <bool kDecide, bool kCoh>
+template <bool kDecide, bool kCoh, bool kStore = true>
 __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     const uint32_t step = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
@@ -961,7 +1052,7 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
         } else {
             com = (f & LTPG_FLAG_COMMIT) != 0u;
         }
-        if (com) write_txn_updates(a, t);
+        if (kStore && com) write_txn_updates(a, t);
     }
     if (kDecide && lane == 0u) {
         if (c_com) {
@@ -977,6 +1068,35 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
 template <bool kDecide, int BS>
 __global__ void __launch_bounds__(BS) ycsb_writeback_late(YcsbTunedArgs a) {
     writeback_late_loop<kDecide, false>(a);
+    finish_batch(a.ctl);
+}
+
+// Write-back over the update list: the decision per transaction (flags,
+// bitmap, counters: writeback_late_loop with no stores), then one update per
+// thread.  An update of a committing transaction stores its value unless a
+// later op of the same transaction writes the same field: op order decides, as
+// in a sequential replay (the transaction's entries are consecutive).  The
+// decision is a function of the conflict bits, which nothing changes here, so
+// an update that reads its transaction's flag byte before or after the first
+// loop adds COMMIT to it decides the same.
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
+    writeback_late_loop<true, false, false>(a);
+    const uint64_t nu = upd_count(a);
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += step) {
+        const uint2 e = __ldg(a.upd + u);
+        const uint32_t key = ycsb_key(e.y), fld = ycsb_field(e.y);
+        if (e.x >= a.B || key >= a.n || fld >= LTPG_YCSB_FIELDS) continue;
+        if (!commits(ld_gpu_u8(a.flags + e.x) & (LTPG_FLAG_RAW | LTPG_FLAG_WAR | LTPG_FLAG_WAW))) continue;
+        bool last = true;
+        for (uint64_t u2 = u + 1; u2 < nu; ++u2) {
+            const uint2 e2 = __ldg(a.upd + u2);
+            if (e2.x != e.x) break;
+            if (ycsb_key(e2.y) == key && ycsb_field(e2.y) == fld) last = false;
+        }
+        if (last && u < a.vals_cap) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = __ldg(a.vals + u);
+    }
     finish_batch(a.ctl);
 }
 
@@ -1151,8 +1271,38 @@ static uint32_t stride_grid(ltpg_ctx *c, const void *k, uint64_t items) {
 // Write-first registration (late_reads = 3): write registration, read
 // registration + RAW, WAR / WAW, committed reads, commit decision +
 // write-back.  Profiled as [registration (both), check, reads, write-back].
+// With the update list (stride / 4 a power of two <= 8): the read
+// registration also lists the updates, and the check and the write-back walk
+// that list.
+template <int BS>
+static cudaError_t launch_write_first_list_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
+    const uint64_t lanes = (uint64_t)a.B * a.lpt, nvec = (uint64_t)a.B * a.stride / 4;
+    prof_mark(c, 0);
+    count_launch(c, 2);
+    ycsb_wf_writes<BS><<<stride_grid(c, (const void *)ycsb_wf_writes<BS>, nvec), BS, 0, c->stream>>>(a);
+    ycsb_wf_reads_list<BS><<<stride_grid(c, (const void *)ycsb_wf_reads_list<BS>, nvec), BS, 0, c->stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    prof_mark(c, 1);
+    count_launch(c, 2);
+    ycsb_wf_check_list<BS><<<stride_grid(c, (const void *)ycsb_wf_check_list<BS>, nvec), BS, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 2);
+    ycsb_read_late<BS><<<stride_grid(c, (const void *)ycsb_read_late<BS>, lanes), BS, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 3);
+    count_launch(c);
+    ycsb_writeback_list<BS><<<stride_grid(c, (const void *)ycsb_writeback_list<BS>, std::max<uint64_t>(a.B, nvec)),
+                              BS, 0, c->stream>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    prof_mark(c, 4);
+    return predictor_after_batch(c);
+}
+
 template <int BS>
 static cudaError_t launch_write_first_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
+    const uint32_t vpt = a.stride / 4u;
+    if (a.upd_cap && (vpt == 1u || vpt == 2u || vpt == 4u || vpt == 8u)) return launch_write_first_list_t<BS>(c, a);
     const uint64_t lanes = (uint64_t)a.B * a.lpt;
     prof_mark(c, 0);
     count_launch(c, 2);
@@ -1250,6 +1400,9 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     a.filter = L.filter;
     a.late = late_mode;
     a.wbits = c->ycsb.wbits;
+    a.upd = c->ycsb.upd;
+    a.upd_cap = c->ycsb.upd_cap;
+    a.vals_cap = s.cap_vals;
     const size_t smem = ycsb_smem_bytes(a.tile, threads, a.stage_entries);
     const size_t smem_cwb = ycsb_smem_bytes(a.tile, threads, 0);  // check + write-back needs no staging table
     cudaError_t e = cudaMemsetAsync(s.stats, 0, sizeof(DevStats), c->stream);

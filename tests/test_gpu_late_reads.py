@@ -193,3 +193,50 @@ def test_late_reads_out_of_range_key_reports_error(eng, late, mode):
         ok = YcsbBatch.from_ops([[(3, True, 2)], [(4, False, 0)]], [[9], []])
         _late_same(eng, o, ok, 0, mode)
     assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+@pytest.mark.parametrize("k", [4, 16])
+def test_late_reads_same_field_twice(eng, late, k):
+    """A transaction that writes one field twice keeps its later value (op
+    order, as a sequential replay), and one that writes two fields of a row
+    keeps both, in every mode.  With write-first registration the updates are
+    stored from the update list, one thread per update: only the last write of
+    a field in its transaction stores."""
+    n = 1000
+    eng.load_ycsb(57, n)
+    o = oracle.YcsbOracle(57, n)
+    pad = [(900 + j, False, 0) for j in range(k)]
+    with _late(eng, late):
+        for bid, mode in enumerate(TUNED):
+            b0 = 20 * bid
+            ops = [[(b0 + 1, True, 2), (b0 + 2, False, 0), (b0 + 1, True, 2)],
+                   [(b0 + 3, True, 1), (b0 + 3, True, 4), (b0 + 5, False, 0)],
+                   [(b0 + 1, False, 0)],
+                   [(b0 + 6, True, 7)] * 4,
+                   # the two writes of a field in different op vectors of the transaction
+                   [(b0 + 8, True, 5)] + pad[:k - 2] + [(b0 + 8, True, 5)]]
+            vals = [[100 + bid, 200 + bid], [300 + bid, 400 + bid], [], [1, 2, 3, 4 + bid], [5, 6 + bid]]
+            _late_same(eng, o, YcsbBatch.from_ops(ops, vals), bid % 2, mode)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+@pytest.mark.parametrize("mode", ["plain"] + TUNED)
+def test_value_offsets_that_disagree_with_the_ops_report_error(eng, late, mode):
+    """val_off says one update where the op words hold two: reported as
+    LTPG_ERR_BOUNDS (no value is read past the batch's values, no fault), and
+    the context stays usable."""
+    from ltpg_gb300 import LtpgError
+    n = 1000
+    eng.load_ycsb(58, n)
+    with _late(eng, late):
+        good = YcsbBatch.from_ops([[(5, True, 1), (6, True, 2), (7, False, 0), (8, False, 0)]], [[41, 42]])
+        bad = YcsbBatch(good.ops, np.array([0, 1], dtype=np.uint32), np.array([41], dtype=np.uint64), 1, 4)
+        eng.upload(0, bad)
+        eng.run_batch(0, mode)
+        with pytest.raises(LtpgError) as ei:
+            eng.sync()
+        assert ei.value.code == abi.ERR_BOUNDS
+        eng.load_ycsb(58, n)
+        o = oracle.YcsbOracle(58, n)
+        _late_same(eng, o, good, 0, mode)
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
