@@ -823,11 +823,12 @@ def workload_record(args, w, theta, dist, res, exact, e2e, batches, peaks, peak_
                                             max(1, w.get("scan_len", 0)), late)
         ek = ycsb_exec_kernel_name(launch, (w["ops"] + 3) & ~3)
         ck = "ycsb_checkwb_tuned"
+        wk = "ycsb_writeback_late"
         if late == 3:  # the registration interval is two kernels; the reads' dominates
-            ek, ck = "ycsb_wf_reads", "ycsb_wf_check"
+            ek, ck, wk = "ycsb_wf_reads_list", "ycsb_wf_check_list", "ycsb_writeback_list"
         cands = [(ek, eb, exec_ms), (ck, cb, cwb_ms)]
         if late:
-            cands += [("ycsb_read_late", rb, read_ms), ("ycsb_writeback_late", wb, wb_ms)]
+            cands += [("ycsb_read_late", rb, read_ms), (wk, wb, wb_ms)]
         kernel, kbytes, kms = max(cands, key=lambda c: c[2])
         # the late-read variants of the execute and check kernels have profile
         # summaries of their own (one execute kernel for both; two check kernels)

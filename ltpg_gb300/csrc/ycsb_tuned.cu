@@ -395,24 +395,41 @@ __device__ __forceinline__ bool wf_read_key(const YcsbTunedArgs &a, uint64_t key
 // The update list: the batch's u-th update (u = its value index, val_off[t]
 // + its rank among transaction t's updates) is stored as {t, op word}, so that
 // the check and the write-back walk the updates alone instead of every op word.
-// The stride / 4 op vectors of a transaction are consecutive lanes of one warp
-// (stride / 4 a power of two <= 8, aligned in the warp); a segmented scan over
-// them gives each lane the updates of the transaction's earlier vectors.  The
-// transaction's last lane checks its update count against its value range:
-// the list positions are only as good as val_off, so a batch whose offsets
-// disagree with its op words is reported (LTPG_ERR_BOUNDS) and its positions
-// are never used past the list.  Called by whole warps.
-__device__ __forceinline__ void wf_list_updates(const YcsbTunedArgs &a, bool act, uint32_t t, const uint32_t *words) {
-    const uint32_t vpt = a.stride / 4u, seg = (threadIdx.x & 31u) & (vpt - 1u);
+// A lane holds op vector seg of its transaction (vpt = stride / 4 vectors, at
+// most 8).  With vpt a power of two the transaction's vectors are consecutive
+// lanes of one warp and a segmented scan gives each lane the updates of the
+// earlier vectors; otherwise the lane counts them in those vectors itself
+// (loads that its neighbours made a moment before).  The transaction's last
+// lane checks its update count against its value range: the list positions are
+// only as good as val_off, so a batch whose offsets disagree with its op words
+// is reported (LTPG_ERR_BOUNDS) and its positions are never used past the
+// list.  Called by whole warps.
+__device__ __forceinline__ uint32_t vec_updates(const uint32_t *w) {
+    uint32_t n = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) n += (!ycsb_is_pad(w[q]) && ycsb_is_update(w[q])) ? 1u : 0u;
+    return n;
+}
+__device__ __forceinline__ void wf_list_updates(const YcsbTunedArgs &a, bool act, uint64_t v, uint32_t t,
+                                                const uint32_t *words) {
+    const uint32_t vpt = a.stride / 4u, seg = (uint32_t)(v % vpt);
+    const bool pow2 = (vpt & (vpt - 1u)) == 0u;
     const uint32_t off = act ? __ldg(a.val_off + t) : 0u;
     const uint32_t end = act && seg == vpt - 1u ? __ldg(a.val_off + t + 1) : 0u;
-    uint32_t n_upd = 0;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) n_upd += (!ycsb_is_pad(words[q]) && ycsb_is_update(words[q])) ? 1u : 0u;
+    const uint32_t n_upd = vec_updates(words);
     uint32_t incl = n_upd;
-    for (uint32_t o = 1; o < vpt; o <<= 1) {
-        const uint32_t x = __shfl_up_sync(FULL, incl, o);
-        if (seg >= o) incl += x;
+    if (pow2) {
+        for (uint32_t o = 1; o < vpt; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(FULL, incl, o);
+            if (seg >= o) incl += x;
+        }
+    } else if (act) {
+        const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops) + (v - seg);
+        for (uint32_t q = 0; q < seg; ++q) {
+            const uint4 w4 = ld_nc_u4(vp + q);
+            const uint32_t w[4] = {w4.x, w4.y, w4.z, w4.w};
+            incl += vec_updates(w);
+        }
     }
     if (act && seg == vpt - 1u && end - off != incl) report_error(a.ctl, DERR_BOUNDS, t);
     uint64_t u = (uint64_t)off + (incl - n_upd);
@@ -446,7 +463,7 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
         const uint32_t t = act ? (uint32_t)(v * 4u / a.stride) : 0xFFFFFFFFu;
         const unsigned long long mine = tag | t;
         const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
-        if (kList) wf_list_updates(a, act, t, words);
+        if (kList) wf_list_updates(a, act, v, t, words);
         bool rd[4];
         uint32_t bits[4];
 #pragma unroll
@@ -521,10 +538,6 @@ template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_wf_writes(YcsbTunedArgs a) {
     wf_register_writes<false>(a, slot_tag(a.ctl->epoch));
 }
-template <int BS>
-__global__ void __launch_bounds__(BS) ycsb_wf_reads(YcsbTunedArgs a) { wf_register_reads<false>(a, a.ctl->epoch); }
-template <int BS>
-__global__ void __launch_bounds__(BS) ycsb_wf_check(YcsbTunedArgs a) { wf_check<false>(a, a.ctl->epoch); }
 
 // ---- write-first with the update list (stride / 4 a power of two <= 8) --------
 template <int BS>
@@ -1271,11 +1284,11 @@ static uint32_t stride_grid(ltpg_ctx *c, const void *k, uint64_t items) {
 // Write-first registration (late_reads = 3): write registration, read
 // registration + RAW, WAR / WAW, committed reads, commit decision +
 // write-back.  Profiled as [registration (both), check, reads, write-back].
-// With the update list (stride / 4 a power of two <= 8): the read
-// registration also lists the updates, and the check and the write-back walk
-// that list.
+// The read registration also lists the updates (the list is allocated with
+// the slots' batch arrays, so it exists for every YCSB batch), and the check
+// and the write-back walk that list.
 template <int BS>
-static cudaError_t launch_write_first_list_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
+static cudaError_t launch_write_first_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
     const uint64_t lanes = (uint64_t)a.B * a.lpt, nvec = (uint64_t)a.B * a.stride / 4;
     prof_mark(c, 0);
     count_launch(c, 2);
@@ -1294,36 +1307,6 @@ static cudaError_t launch_write_first_list_t(ltpg_ctx *c, const YcsbTunedArgs &a
     count_launch(c);
     ycsb_writeback_list<BS><<<stride_grid(c, (const void *)ycsb_writeback_list<BS>, std::max<uint64_t>(a.B, nvec)),
                               BS, 0, c->stream>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_mark(c, 4);
-    return predictor_after_batch(c);
-}
-
-template <int BS>
-static cudaError_t launch_write_first_t(ltpg_ctx *c, const YcsbTunedArgs &a) {
-    const uint32_t vpt = a.stride / 4u;
-    if (a.upd_cap && (vpt == 1u || vpt == 2u || vpt == 4u || vpt == 8u)) return launch_write_first_list_t<BS>(c, a);
-    const uint64_t lanes = (uint64_t)a.B * a.lpt;
-    prof_mark(c, 0);
-    count_launch(c, 2);
-    ycsb_wf_writes<BS><<<stride_grid(c, (const void *)ycsb_wf_writes<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
-                         c->stream>>>(a);
-    ycsb_wf_reads<BS><<<stride_grid(c, (const void *)ycsb_wf_reads<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
-                        c->stream>>>(a);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    prof_mark(c, 1);
-    count_launch(c, 2);
-    ycsb_wf_check<BS><<<stride_grid(c, (const void *)ycsb_wf_check<BS>, (uint64_t)a.B * a.stride / 4), BS, 0,
-                        c->stream>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_mark(c, 2);
-    ycsb_read_late<BS><<<stride_grid(c, (const void *)ycsb_read_late<BS>, lanes), BS, 0, c->stream>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    prof_mark(c, 3);
-    count_launch(c);
-    ycsb_writeback_late<true, BS>
-        <<<stride_grid(c, (const void *)ycsb_writeback_late<true, BS>, a.B), BS, 0, c->stream>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     prof_mark(c, 4);
     return predictor_after_batch(c);
