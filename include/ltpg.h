@@ -76,10 +76,11 @@ extern "C" {
  *   bits 0..26  key
  * Updates carry their new values in vals[], in transaction/op order;
  * val_off[t] is the index of transaction t's first value (val_off[n_txn] =
- * number of updates).  Value offsets that disagree with the op words (a
- * transaction's update count, or an index past val_off[n_txn] or the slot's
- * values) are reported as LTPG_ERR_BOUNDS by the batch's sync; no value is
- * read out of bounds.  A read registers and checks every key it covers.
+ * number of updates).  No value is read out of bounds: a value index past
+ * val_off[n_txn] or past the slot's values is reported as LTPG_ERR_BOUNDS by
+ * the batch's sync, and the write-first path (late_reads = 3) also reports a
+ * transaction whose update count disagrees with its offsets.  A read
+ * registers and checks every key it covers.
  * Per-transaction result: sum over the reads j of (xor of the 10 fields of
  * every row the read covers) * (2j + 1), mod 2^64, read from the batch-start
  * image.
