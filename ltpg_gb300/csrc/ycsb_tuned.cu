@@ -1095,7 +1095,10 @@ __global__ void __launch_bounds__(BS) ycsb_writeback_late(YcsbTunedArgs a) {
 template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
     writeback_late_loop<true, false, false>(a);
-    const uint64_t nu = upd_count(a);
+    // a batch whose registration reported an error (a key past the table, or
+    // offsets that disagree with the op words, which leave list positions
+    // unwritten) stores nothing
+    const uint64_t nu = ld_gpu_u32(&a.ctl->error) ? 0ull : upd_count(a);
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += step) {
         const uint2 e = __ldg(a.upd + u);

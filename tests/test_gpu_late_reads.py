@@ -236,7 +236,11 @@ def test_value_offsets_that_disagree_with_the_ops_report_error(eng, late, mode):
         with pytest.raises(LtpgError) as ei:
             eng.sync()
         assert ei.value.code == abi.ERR_BOUNDS
-        eng.load_ycsb(58, n)
         o = oracle.YcsbOracle(58, n)
+        if late == 3 and mode in ("fused", "graph"):
+            # the update list's write-back stores nothing for a batch whose
+            # registration reported an error
+            assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+        eng.load_ycsb(58, n)
         _late_same(eng, o, good, 0, mode)
     assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
