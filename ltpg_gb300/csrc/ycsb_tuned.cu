@@ -1037,7 +1037,8 @@ __global__ void __launch_bounds__(512) ycsb_checkwb_tuned(YcsbTunedArgs a) {
 // stores its updates.  kDecide (write-first registration): the flags hold the
 // conflict bits only, and this pass makes the commit decision and writes the
 // final flags, the bitmap (a warp's ballot over 32 consecutive transactions is
-// one bitmap word) and the counters.
+// one bitmap word) and the counters.  kStore = false: the decision only (the
+// update-list write-back stores from the list).
 template <bool kDecide, bool kCoh, bool kStore = true>
 __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     const uint32_t step = gridDim.x * blockDim.x;
@@ -1078,9 +1079,10 @@ __device__ __forceinline__ void writeback_late_loop(const YcsbTunedArgs &a) {
     }
 }
 
-template <bool kDecide, int BS>
+// Late reads 2: the check kernel made the decisions; this one stores.
+template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_writeback_late(YcsbTunedArgs a) {
-    writeback_late_loop<kDecide, false>(a);
+    writeback_late_loop<false, false>(a);
     finish_batch(a.ctl);
 }
 
@@ -1453,8 +1455,8 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         count_launch(c);
         with_block(threads, [&](auto bs) {
             constexpr int BS = decltype(bs)::value;
-            ycsb_writeback_late<false, BS>
-                <<<stride_grid(c, (const void *)ycsb_writeback_late<false, BS>, a.B), BS, 0, c->stream>>>(a);
+            ycsb_writeback_late<BS>
+                <<<stride_grid(c, (const void *)ycsb_writeback_late<BS>, a.B), BS, 0, c->stream>>>(a);
             return 0;
         });
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
