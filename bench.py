@@ -365,6 +365,24 @@ def modes_run(eng, torch, n_slots, steps, reload):
     return out
 
 
+def h2d_link_gbs(nbytes, reps=4):
+    """Host-to-device copy rate of this machine (one pinned buffer of the batch's
+    size, one cudaMemcpyAsync, CUDA events): the bound of the end-to-end rate
+    when a batch's copy takes longer than its kernels."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d.copy_(h, non_blocking=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        d.copy_(h, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    return nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
 def e2e_run(eng, pinned, mode, steps, n_slots, n_txn, dist, depth=3):
     """End to end through the pipelined host-buffer calls (ltpg_submit_*_host /
     ltpg_host_wait): every step copies its pinned host batch to the device,
@@ -392,7 +410,7 @@ def e2e_run(eng, pinned, mode, steps, n_slots, n_txn, dist, depth=3):
     go(steps)
     t1 = time.perf_counter()
     c1, _ = eng.counters()
-    return dict(secs=t1 - t0, commits=c1 - c0, steps=steps, depth=depth,
+    return dict(secs=t1 - t0, commits=c1 - c0, steps=steps, depth=depth, link_GBs=h2d_link_gbs(pinned[0].nbytes()),
                 h2d=int(np.mean([p.nbytes() for p in pinned])), d2h=words * 4)
 
 
@@ -876,7 +894,11 @@ def workload_record(args, w, theta, dist, res, exact, e2e, batches, peaks, peak_
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],
-                "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)"},
+                "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)",
+                # the copy of a step's batch at the measured host-to-device rate:
+                # the end-to-end rate cannot pass commits per step / this time
+                "h2d_link_GBs": e2e["link_GBs"],
+                "link_bound_value": (e2e["commits"] / e2e["steps"]) / (e2e["h2d"] / (e2e["link_GBs"] * 1e9))},
         "gpu_launches": int(tuned["launches"]),
         "launch": launch,
         "clocks": tuned["clocks"],
