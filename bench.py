@@ -680,13 +680,21 @@ def engine_on_ref_shapes(iters, scale_iters=10):
     (plain, fused, persistent, graph), the same batch in every slot, CUDA
     events around `iters` batches (at the headline scale: max(8, scale_iters)
     batches, with the tuned launch shape of the high-contention YCSB
-    workload); `best_mode` names the fastest."""
+    workload; the reference's 10,000-transaction YCSB batch with its own
+    tuned shape); `best_mode` names the fastest."""
     import torch
 
     import ltpg_gb300 as L
     from ltpg_gb300 import tune
     _, yb, tb, mb = ref_shape_batches()
-    shapes = [("ycsb_10k_x10", lambda e: e.load_ycsb(SEED, REF_Y1["n_records"]), yb, dict(max_ops_per_txn=10), iters),
+    small = tune.load_cached("ycsb_ref_10k|theta=0.99")
+
+    def load_small(e):
+        e.load_ycsb(SEED, REF_Y1["n_records"])
+        if small:
+            e.set_launch("ycsb", **{k: v for k, v in small.items() if k in dict(L.abi.LaunchC._fields_)})
+
+    shapes = [("ycsb_10k_x10", load_small, yb, dict(max_ops_per_txn=10), iters),
               ("payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), tb,
                dict(max_ops_per_txn=16, max_lines=16), iters),
               ("neworder_payment_65536", lambda e: e.load_tpcc(SEED, REF_TF["warehouses"]), mb,
