@@ -903,6 +903,8 @@ def workload_record(args, w, theta, dist, res, exact, e2e, batches, peaks, peak_
         "e2e": {"value": e2e_value, "unit": "txn/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "steps": e2e["steps"], "in_flight": e2e["depth"],
                 "api": "ltpg_submit_*_host / ltpg_host_wait (pinned host buffers)",
+                "inputs": ("op words, value offsets and values" if w["kind"] == "ycsb"
+                           else "transaction records and order lines"),
                 # the copy of a step's batch at the measured host-to-device rate:
                 # the end-to-end rate cannot pass commits per step / this time
                 "h2d_link_GBs": e2e["link_GBs"],

@@ -96,7 +96,10 @@ typedef struct {
     uint32_t op_stride;
     uint32_t n_updates;
     const uint32_t *ops;     /* n_txn * op_stride */
-    const uint32_t *val_off; /* n_txn + 1         */
+    const uint32_t *val_off; /* n_txn + 1; NULL: made on the device from the op
+                                words, and n_updates must equal the number
+                                of update ops (a mismatch is reported as
+                                LTPG_ERR_BOUNDS)                           */
     const uint64_t *vals;    /* n_updates         */
 } ltpg_ycsb_batch;
 
@@ -311,7 +314,9 @@ int ltpg_batch_info_get(ltpg_ctx *ctx, uint32_t slot, ltpg_batch_info *out);
 int ltpg_batch_download(ltpg_ctx *ctx, uint32_t slot, uint32_t part, void *host, size_t bytes);
 
 /* Replaces: Query::copy_to_device (TF/Query.h:532-605, Y1/Query.h:194-213).
- * Copies a host batch into device slot `slot` on the context stream. */
+ * Copies a host batch into device slot `slot` on the context stream.  A YCSB
+ * batch without val_off has its offsets made on the device behind the copy of
+ * its op words (the bytes on the wire are the op words and values only). */
 int ltpg_batch_upload_ycsb(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b);
 int ltpg_batch_upload_tpcc(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b);
 

@@ -77,21 +77,28 @@ class YcsbBatch:
     """A YCSB batch in the engine's format (see include/ltpg.h)."""
 
     def __init__(self, ops, val_off, vals, n_txn, ops_per_txn):
+        """val_off None: the batch carries no value offsets, the engine makes
+        them on the device from the op words (n_updates = len(vals))."""
         self.ops = np.ascontiguousarray(ops, dtype=np.uint32)
-        self.val_off = np.ascontiguousarray(val_off, dtype=np.uint32)
+        self.val_off = None if val_off is None else np.ascontiguousarray(val_off, dtype=np.uint32)
         self.vals = np.ascontiguousarray(vals, dtype=np.uint64)
         self.n_txn = int(n_txn)
         self.ops_per_txn = int(ops_per_txn)
         self.op_stride = (self.ops_per_txn + 3) & ~3
-        self.n_updates = int(self.val_off[self.n_txn])
+        self.n_updates = len(self.vals) if self.val_off is None else int(self.val_off[self.n_txn])
 
     def as_c(self):
         return abi.YcsbBatchC(self.n_txn, self.ops_per_txn, self.op_stride, self.n_updates,
-                              self.ops.ctypes.data, self.val_off.ctypes.data,
+                              self.ops.ctypes.data, None if self.val_off is None else self.val_off.ctypes.data,
                               self.vals.ctypes.data if len(self.vals) else None)
 
+    def without_offsets(self):
+        """The same batch without its value offsets (the engine makes them)."""
+        return YcsbBatch(self.ops, None, self.vals[:self.n_updates], self.n_txn, self.ops_per_txn)
+
     def nbytes(self):
-        return self.n_txn * self.op_stride * 4 + (self.n_txn + 1) * 4 + self.n_updates * 8
+        offs = 0 if self.val_off is None else (self.n_txn + 1) * 4
+        return self.n_txn * self.op_stride * 4 + offs + self.n_updates * 8
 
     @staticmethod
     def from_ops(op_lists, values):
@@ -150,7 +157,8 @@ def pinned_copy(batch):
         return out
 
     if isinstance(batch, YcsbBatch):
-        return YcsbBatch(pin(batch.ops), pin(batch.val_off), pin(batch.vals), batch.n_txn, batch.ops_per_txn)
+        return YcsbBatch(pin(batch.ops), None if batch.val_off is None else pin(batch.val_off), pin(batch.vals),
+                         batch.n_txn, batch.ops_per_txn)
     return TpccBatch(pin(batch.txns), pin(batch.lines), batch.txn_base)
 
 

@@ -39,6 +39,7 @@ void free_slot(Slot &s) {
     dev_free(s.ops);
     dev_free(s.val_off);
     dev_free(s.vals);
+    dev_free(s.off_blocks);
     dev_free(s.txns);
     dev_free(s.lines);
     dev_free(s.dev_hdr);
@@ -363,6 +364,7 @@ int slot_prepare_ycsb(ltpg_ctx *c, uint32_t slot, uint32_t n_txn, uint32_t k, ui
         const uint64_t cap_vals = (uint64_t)c->cfg.max_txn * c->cfg.max_ops_per_txn;
         CK(dev_alloc(&s->ops, cap_ops), "alloc ops");
         CK(dev_alloc(&s->val_off, (uint64_t)c->cfg.max_txn + 1), "alloc val_off");
+        CK(dev_alloc(&s->off_blocks, ((uint64_t)c->cfg.max_txn + 1023) / 1024 + 1), "alloc offset sums");
         CK(dev_alloc(&s->vals, cap_vals), "alloc vals");
         s->cap_ops = cap_ops;
         s->cap_vals = cap_vals;
@@ -416,18 +418,23 @@ int ctx_cuda_fail(ltpg_ctx *c, cudaError_t e, const char *what) { return cuda_fa
 }  // namespace ltpg
 
 namespace {
-int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream_t st) {
+// derive_st: the stream that makes the value offsets of a batch without them
+// (after the op words' copy on st; null: the offsets are left to the caller).
+int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream_t st, cudaStream_t derive_st) {
     if (!c || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
     if (b->ops_per_txn == 0 || b->op_stride != ycsb_stride(b->ops_per_txn))
         return fail(c, LTPG_ERR_INVALID, "bad ops_per_txn / op_stride");
-    if (!b->ops || !b->val_off || (b->n_updates && !b->vals)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    if (!b->ops || (b->n_updates && !b->vals)) return fail(c, LTPG_ERR_INVALID, "null batch array");
     Slot *s = nullptr;
     int r = slot_prepare_ycsb(c, slot, b->n_txn, b->ops_per_txn, b->n_updates, &s);
     if (r) return r;
     const uint64_t n_ops = (uint64_t)b->n_txn * b->op_stride;
     CK(cudaMemcpyAsync(s->ops, b->ops, n_ops * 4, cudaMemcpyHostToDevice, st), "upload ops");
-    CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, st),
-       "upload val_off");
+    if (b->val_off)
+        CK(cudaMemcpyAsync(s->val_off, b->val_off, ((uint64_t)b->n_txn + 1) * 4, cudaMemcpyHostToDevice, st),
+           "upload val_off");
+    else if (derive_st)  // made on the device from the op words, behind their copy
+        CK(ycsb_derive_offsets(c, *s, derive_st), "value offsets");
     if (b->n_updates)
         CK(cudaMemcpyAsync(s->vals, b->vals, (uint64_t)b->n_updates * 8, cudaMemcpyHostToDevice, st), "upload vals");
     return LTPG_OK;
@@ -458,7 +465,7 @@ int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream
 extern "C" {
 
 int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b) {
-    return c ? upload_ycsb(c, slot, b, c->stream) : LTPG_ERR_INVALID;
+    return c ? upload_ycsb(c, slot, b, c->stream, c->stream) : LTPG_ERR_INVALID;
 }
 int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b) {
     return c ? upload_tpcc(c, slot, b, c->stream) : LTPG_ERR_INVALID;
@@ -618,8 +625,11 @@ int ltpg_run_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int
 // of the next batch overlaps this one's kernels.
 extern "C++" {
 namespace {
+// derive: make the YCSB value offsets on the compute stream once the copy is
+// done (a batch uploaded without them): kernels on the copy stream would wait
+// there for SMs held by the previous batch and hold up the next copy.
 template <class Up>
-int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up upload) {
+int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up upload, bool derive = false) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "create copy stream");
@@ -633,6 +643,7 @@ int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up 
     if (r) return r;
     CK(cudaEventRecord(s->copied, c->copy_stream), "record copy");
     CK(cudaStreamWaitEvent(c->stream, s->copied, 0), "wait for the copy");
+    if (derive) CK(ycsb_derive_offsets(c, *s, c->stream), "value offsets");
     r = ltpg_run_batch(c, slot, mode);
     if (r) return r;
     if (host_bitmap)
@@ -647,7 +658,9 @@ int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up 
 
 int ltpg_submit_ycsb_host(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, int mode, uint32_t *host_bitmap) {
     if (!c) return LTPG_ERR_INVALID;
-    return submit_host(c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_ycsb(c, slot, b, st); });
+    return submit_host(
+        c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_ycsb(c, slot, b, st, nullptr); },
+        b && !b->val_off);
 }
 
 int ltpg_submit_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int mode, uint32_t *host_bitmap) {
@@ -706,7 +719,6 @@ int ltpg_batch_download(ltpg_ctx *c, uint32_t slot, uint32_t part, void *host, s
     int r = ltpg_batch_info_get(c, slot, &bi);
     if (r) return r;
     const uint64_t n = bi.n_txn;
-    if (!host) return fail(c, LTPG_ERR_INVALID, "null buffer");
     Slot *s = get_slot(c, slot);
     const void *src = nullptr;
     size_t need = 0;
@@ -720,6 +732,7 @@ int ltpg_batch_download(ltpg_ctx *c, uint32_t slot, uint32_t part, void *host, s
     }
     if (!src) return fail(c, LTPG_ERR_INVALID, "no such batch part");
     if (bytes != need) return fail(c, LTPG_ERR_INVALID, "buffer size differs from the batch part");
+    if (need && !host) return fail(c, LTPG_ERR_INVALID, "null buffer");  // an empty part needs none
     if (need) CK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, c->stream), "batch download");
     return ltpg_sync(c);
 }

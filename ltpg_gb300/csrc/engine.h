@@ -87,6 +87,7 @@ struct Slot {
     uint32_t *ops = nullptr;
     uint32_t *val_off = nullptr;
     uint64_t *vals = nullptr;
+    uint32_t *off_blocks = nullptr;  // value offsets made on the device: per-1024-transaction sums
     uint64_t cap_ops = 0, cap_vals = 0, cap_txn_y = 0;
     // TPC-C
     uint32_t n_lines = 0;
@@ -201,6 +202,9 @@ void predictor_free(ltpg_ctx *c);
 inline void count_launch(ltpg_ctx *c, uint64_t n = 1) { c->launches += n; }
 cudaError_t ycsb_init_table(ltpg_ctx *c);
 cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase);      // 0 exec, 1 check, 2 write-back
+// Value offsets of the batch in s made on the device from its op words (the
+// upload of a batch without val_off), on stream st.
+cudaError_t ycsb_derive_offsets(ltpg_ctx *c, Slot &s, cudaStream_t st);
 cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode);   // fused / persistent
 cudaError_t tpcc_init_tables(ltpg_ctx *c);
 cudaError_t tpcc_build_name_index(ltpg_ctx *c);

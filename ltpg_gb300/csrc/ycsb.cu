@@ -152,6 +152,93 @@ __global__ void __launch_bounds__(256) ycsb_writeback_plain(const uint8_t *__res
     finish_batch(ctl);
 }
 
+// ---- value offsets made on the device -------------------------------------------
+// A batch uploaded without val_off gets it here: the exclusive prefix over
+// transactions of each one's update count, in three passes (per 1024
+// transactions: counts and a block scan; one block: the scan of the block
+// sums; every transaction: its block's offset).  The total must equal the
+// batch's declared n_updates (the values it carries); a mismatch is reported
+// as a range error.
+__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t *total) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += x;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        uint32_t w = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(FULL, w, o);
+            if (lane >= o) w += x;
+        }
+        if (lane < nw) warp_sums[lane] = w;  // inclusive sums of the warps
+    }
+    __syncthreads();
+    const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+    *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();  // warp_sums is reused by the next call
+    return before + incl - v;
+}
+
+__global__ void __launch_bounds__(1024) ycsb_offsets_local(const uint32_t *__restrict__ ops, uint32_t B,
+                                                           uint32_t stride, uint32_t *__restrict__ val_off,
+                                                           uint32_t *__restrict__ blocks) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = 0;
+    if (t < B) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(ops + (uint64_t)t * stride);
+        for (uint32_t q = 0; q < stride / 4u; ++q) {
+            const uint4 w = __ldg(p + q);
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) n += (!ycsb_is_pad(ws[i]) && ycsb_is_update(ws[i])) ? 1u : 0u;
+        }
+    }
+    uint32_t total;
+    const uint32_t excl = block_excl_scan_1024(n, &total);
+    if (t < B) val_off[t] = excl;
+    if (threadIdx.x == 0) blocks[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) ycsb_offsets_blocks(uint32_t *blocks, uint32_t nb) {
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nb; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nb ? blocks[i] : 0u;
+        uint32_t total;
+        const uint32_t excl = block_excl_scan_1024(v, &total);
+        if (i < nb) blocks[i] = carry + excl;
+        carry += total;
+    }
+    if (threadIdx.x == 0) blocks[nb] = carry;
+}
+
+__global__ void __launch_bounds__(1024) ycsb_offsets_add(uint32_t *__restrict__ val_off, uint32_t B,
+                                                         const uint32_t *__restrict__ blocks, uint32_t nb,
+                                                         uint32_t n_updates, DevCtl *ctl) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < B) val_off[t] += blocks[t / 1024u];
+    if (t == 0) {
+        val_off[B] = blocks[nb];
+        if (blocks[nb] != n_updates) report_error(ctl, DERR_BOUNDS, 0u);
+    }
+}
+
+cudaError_t ycsb_derive_offsets(ltpg_ctx *c, Slot &s, cudaStream_t st) {
+    const uint32_t B = s.n_txn, nb = (B + 1023) / 1024;
+    ycsb_offsets_local<<<nb, 1024, 0, st>>>(s.ops, B, s.stride, s.val_off, s.off_blocks);
+    ycsb_offsets_blocks<<<1, 1024, 0, st>>>(s.off_blocks, nb);
+    ycsb_offsets_add<<<nb, 1024, 0, st>>>(s.val_off, B, s.off_blocks, nb, s.n_updates, c->ctl);
+    return cudaGetLastError();
+}
+
 static inline uint32_t plain_tile(uint32_t k) { return k >= 256 ? 1u : 256u / k; }
 
 cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase) {
