@@ -70,7 +70,8 @@ def test_setting_round_trips(eng, late):
 
 @pytest.mark.parametrize("filt", [0, 1])
 @pytest.mark.parametrize("k,upd,theta", [(1, 50, 0.99), (3, 30, 0.99), (7, 20, 0.9), (10, 50, 0.6), (16, 5, 0.99),
-                                         (20, 10, 0.99), (32, 5, 0.8)])
+                                         (20, 10, 0.99), (32, 5, 0.8), (4, 100, 0.99), (32, 100, 0.9),
+                                         (12, 0, 0.99)])
 def test_late_reads_match_oracle(eng, late, k, upd, theta, filt):
     n = 40000
     eng.load_ycsb(51, n)
