@@ -55,6 +55,11 @@ __device__ __forceinline__ uint32_t ld_gpu_u8(const uint8_t *p) {
     asm volatile("ld.relaxed.gpu.global.u8 %0, [%1];" : "=h"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ uint2 ld_gpu_u2(const uint2 *p) {
+    uint2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ ulonglong2 ld_gpu_slot(const RegSlot *p) {
     ulonglong2 v;
     asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");

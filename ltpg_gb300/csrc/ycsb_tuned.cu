@@ -501,38 +501,6 @@ __device__ __forceinline__ void wf_register_reads(const YcsbTunedArgs &a, uint32
     }
 }
 
-// (3) the updates' WAR / WAW, OR-ed into the transaction's flag byte (32-bit
-// atomics on the padded flag array); four op words per thread, the slot loads
-// of a thread's updates all issued before the first is used.  The commit
-// decision is made where it is needed: by the read kernel and by the
-// write-back, which also writes the final flags, bitmap and counters.
-template <bool kCoh>
-__device__ __forceinline__ void wf_check(const YcsbTunedArgs &a, uint32_t epoch) {
-    const uint64_t nvec = (uint64_t)a.B * a.stride / 4u;
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    const uint4 *vp = reinterpret_cast<const uint4 *>(a.ops);
-    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += step) {
-        const uint4 w4 = ld_nc_u4(vp + v);
-        const uint32_t t = (uint32_t)(v * 4u / a.stride);
-        const uint32_t words[4] = {w4.x, w4.y, w4.z, w4.w};
-        bool upd[4];
-        ulonglong2 s[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t w = words[q];
-            upd[q] = !ycsb_is_pad(w) && ycsb_is_update(w) && ycsb_key(w) < a.n;
-            s[q] = upd[q] ? (kCoh ? ld_gpu_slot(a.reg + ycsb_key(w)) : ld_slot(a.reg + ycsb_key(w)))
-                          : make_ulonglong2(~0ull, ~0ull);
-        }
-        uint32_t f = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (slot_min(s[q].x, epoch) < t) f |= LTPG_FLAG_WAR;
-            if (slot_min(s[q].y, epoch) < t) f |= LTPG_FLAG_WAW;
-        }
-        if (f) atomicOr(reinterpret_cast<unsigned *>(a.flags) + (t >> 2), f << (8u * (t & 3u)));
-    }
-}
 
 template <int BS>
 __global__ void __launch_bounds__(BS) ycsb_wf_writes(YcsbTunedArgs a) {
@@ -554,9 +522,15 @@ __device__ __forceinline__ uint64_t upd_count(const YcsbTunedArgs &a) {
 // (3) over the update list: each update's WAR / WAW, OR-ed into its
 // transaction's flag byte.  Four entries per thread and step, their entry and
 // slot loads issued together.
-template <int BS>
-__global__ void __launch_bounds__(BS) ycsb_wf_check_list(YcsbTunedArgs a) {
-    const uint32_t epoch = a.ctl->epoch;
+// An entry of the update list; kCoh: written earlier in the same launch (the
+// persistent kernel), so loaded coherently at L2.
+template <bool kCoh>
+__device__ __forceinline__ uint2 ld_upd(const uint2 *p) {
+    return kCoh ? ld_gpu_u2(p) : __ldg(p);
+}
+
+template <bool kCoh>
+__device__ __forceinline__ void wf_check_list(const YcsbTunedArgs &a, uint32_t epoch) {
     const uint64_t nu = upd_count(a);
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u0 < nu; u0 += 4 * step) {
@@ -564,14 +538,15 @@ __global__ void __launch_bounds__(BS) ycsb_wf_check_list(YcsbTunedArgs a) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint64_t u = u0 + (uint64_t)q * step;
-            e[q] = u < nu ? __ldg(a.upd + u) : make_uint2(0xFFFFFFFFu, 0u);
+            e[q] = u < nu ? ld_upd<kCoh>(a.upd + u) : make_uint2(0xFFFFFFFFu, 0u);
         }
         bool ok[4];
         ulonglong2 sl[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             ok[q] = e[q].x < a.B && ycsb_key(e[q].y) < a.n;
-            sl[q] = ok[q] ? ld_slot(a.reg + ycsb_key(e[q].y)) : make_ulonglong2(~0ull, ~0ull);
+            sl[q] = ok[q] ? (kCoh ? ld_gpu_slot(a.reg + ycsb_key(e[q].y)) : ld_slot(a.reg + ycsb_key(e[q].y)))
+                          : make_ulonglong2(~0ull, ~0ull);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -583,6 +558,8 @@ __global__ void __launch_bounds__(BS) ycsb_wf_check_list(YcsbTunedArgs a) {
         }
     }
 }
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_wf_check_list(YcsbTunedArgs a) { wf_check_list<false>(a, a.ctl->epoch); }
 
 // ---- check + write-back over all tiles assigned to this block ------------------
 // fl: tile flags.  kLate = 0: the third pass stores the committed updates;
@@ -1094,27 +1071,31 @@ __global__ void __launch_bounds__(BS) ycsb_writeback_late(YcsbTunedArgs a) {
 // decision is a function of the conflict bits, which nothing changes here, so
 // an update that reads its transaction's flag byte before or after the first
 // loop adds COMMIT to it decides the same.
-template <int BS>
-__global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
-    writeback_late_loop<true, false, false>(a);
+template <bool kCoh>
+__device__ __forceinline__ void writeback_list(const YcsbTunedArgs &a) {
+    writeback_late_loop<true, kCoh, false>(a);
     // a batch whose registration reported an error (a key past the table, or
     // offsets that disagree with the op words, which leave list positions
     // unwritten) stores nothing
     const uint64_t nu = ld_gpu_u32(&a.ctl->error) ? 0ull : upd_count(a);
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += step) {
-        const uint2 e = __ldg(a.upd + u);
+        const uint2 e = ld_upd<kCoh>(a.upd + u);
         const uint32_t key = ycsb_key(e.y), fld = ycsb_field(e.y);
         if (e.x >= a.B || key >= a.n || fld >= LTPG_YCSB_FIELDS) continue;
         if (!commits(ld_gpu_u8(a.flags + e.x) & (LTPG_FLAG_RAW | LTPG_FLAG_WAR | LTPG_FLAG_WAW))) continue;
         bool last = true;
         for (uint64_t u2 = u + 1; u2 < nu; ++u2) {
-            const uint2 e2 = __ldg(a.upd + u2);
+            const uint2 e2 = ld_upd<kCoh>(a.upd + u2);
             if (e2.x != e.x) break;
             if (ycsb_key(e2.y) == key && ycsb_field(e2.y) == fld) last = false;
         }
         if (last && u < a.vals_cap) a.rows[(uint64_t)key * LTPG_YCSB_FIELDS + fld] = __ldg(a.vals + u);
     }
+}
+template <int BS>
+__global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
+    writeback_list<false>(a);
     finish_batch(a.ctl);
 }
 
@@ -1134,13 +1115,13 @@ __global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
     if (kLate && !kStage && a.late == 3u) {  // write-first: five phases, four grid barriers
         wf_register_writes<true>(a, tag);
         bool ok = grid_barrier(a.ctl);
-        if (ok) wf_register_reads<true>(a, epoch);
+        if (ok) wf_register_reads<true, true>(a, epoch);
         ok = ok && grid_barrier(a.ctl);
-        if (ok) wf_check<true>(a, epoch);
+        if (ok) wf_check_list<true>(a, epoch);
         ok = ok && grid_barrier(a.ctl);
         if (ok) late_read_loop<true>(a);
         ok = ok && grid_barrier(a.ctl);
-        if (ok) writeback_late_loop<true, true>(a);
+        if (ok) writeback_list<true>(a);
         finish_batch(a.ctl);
         return;
     }
