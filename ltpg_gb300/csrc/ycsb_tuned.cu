@@ -1106,8 +1106,12 @@ __global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
 // then check + reads, a second grid barrier, and the write-back.  Phases
 // after the first load what earlier phases wrote with coherent loads
 // (kCoh = true above; checkwb_tiles reads slots with ld.global.cg, at L2).
-template <bool kStage, bool kLate>
-__global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) {
+// kMinB > 1: blocks of at most 256 threads, kMinB of them resident per SM
+// (the register budget that sets, 40 for 6, with a few spills): the row
+// gathers of the late-read phase want the warps more than the other phases
+// want the registers.
+template <bool kStage, bool kLate, int kMinB = 1>
+__global__ void __launch_bounds__(kMinB > 1 ? 256 : 512, kMinB) ycsb_persistent(YcsbTunedArgs a) {
     extern __shared__ __align__(16) char smem[];
     const SmemPtrs p = carve(smem, a.tile);
     const uint32_t epoch = a.ctl->epoch;
@@ -1382,7 +1386,8 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         return e;
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
     auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
-                        : (late ? ycsb_persistent<false, true> : ycsb_persistent<false, false>);
+                        : (late ? (threads <= 256 ? ycsb_persistent<false, true, 6> : ycsb_persistent<false, true>)
+                                : ycsb_persistent<false, false>);
     auto cwb_k = !late ? ycsb_checkwb_tuned<0> : late_mode == 1u ? ycsb_checkwb_tuned<1> : ycsb_checkwb_tuned<2>;
     // above 48 KB of static + dynamic shared memory a kernel must opt in
     for (const void *k : {(const void *)exec_k, (const void *)cwb_k, (const void *)pers_k})
