@@ -1106,12 +1106,8 @@ __global__ void __launch_bounds__(BS) ycsb_writeback_list(YcsbTunedArgs a) {
 // then check + reads, a second grid barrier, and the write-back.  Phases
 // after the first load what earlier phases wrote with coherent loads
 // (kCoh = true above; checkwb_tiles reads slots with ld.global.cg, at L2).
-// kMinB > 1: blocks of at most 256 threads, kMinB of them resident per SM
-// (the register budget that sets, 40 for 6, with a few spills): the row
-// gathers of the late-read phase want the warps more than the other phases
-// want the registers.
-template <bool kStage, bool kLate, int kMinB = 1>
-__global__ void __launch_bounds__(kMinB > 1 ? 256 : 512, kMinB) ycsb_persistent(YcsbTunedArgs a) {
+template <bool kStage, bool kLate>
+__device__ __forceinline__ void ycsb_persistent_body(const YcsbTunedArgs &a) {
     extern __shared__ __align__(16) char smem[];
     const SmemPtrs p = carve(smem, a.tile);
     const uint32_t epoch = a.ctl->epoch;
@@ -1159,6 +1155,15 @@ __global__ void __launch_bounds__(kMinB > 1 ? 256 : 512, kMinB) ycsb_persistent(
         if (ok) writeback_late_loop<false, true>(a);
     }
     finish_batch(a.ctl);
+}
+template <bool kStage, bool kLate>
+__global__ void __launch_bounds__(512) ycsb_persistent(YcsbTunedArgs a) { ycsb_persistent_body<kStage, kLate>(a); }
+// Late reads on blocks of at most 256 threads with registers budgeted for six
+// resident blocks per SM (40, with a few spills, against 59 and four): the row
+// gathers of the late-read phase want the warps more than the other phases
+// want the registers.
+__global__ void __launch_bounds__(256, 6) ycsb_persistent_late_x6(YcsbTunedArgs a) {
+    ycsb_persistent_body<false, true>(a);
 }
 
 // Static shared memory of a kernel, queried once per kernel.
@@ -1386,7 +1391,7 @@ cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
         return e;
     auto exec_k = stage ? ycsb_exec_tuned<true> : ycsb_exec_tuned<false>;
     auto pers_k = stage ? (late ? ycsb_persistent<true, true> : ycsb_persistent<true, false>)
-                        : (late ? (threads <= 256 ? ycsb_persistent<false, true, 6> : ycsb_persistent<false, true>)
+                        : (late ? (threads <= 256 ? ycsb_persistent_late_x6 : ycsb_persistent<false, true>)
                                 : ycsb_persistent<false, false>);
     auto cwb_k = !late ? ycsb_checkwb_tuned<0> : late_mode == 1u ? ycsb_checkwb_tuned<1> : ycsb_checkwb_tuned<2>;
     // above 48 KB of static + dynamic shared memory a kernel must opt in
