@@ -17,7 +17,11 @@
 //   * late reads (a launch setting): execute only registers, the check kernel
 //     reads the rows of the committed transactions after the tile's commit
 //     decision, and a third kernel stores the updates, so that no aborted
-//     transaction's rows are read.
+//     transaction's rows are read;
+//   * write-first registration (late reads 3): the updates register first,
+//     then each read touches its key's slot only when an update writes the
+//     key; the read registration also lists the updates by value index, and
+//     the check and the write-back walk that list instead of the op words.
 #include <mutex>
 #include <type_traits>
 #include <unordered_map>
