@@ -355,6 +355,18 @@ int ltpg_submit_ycsb_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_ycsb_batch *b
 int ltpg_submit_tpcc_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, int mode,
                           uint32_t *host_bitmap);
 int ltpg_host_wait(ltpg_ctx *ctx, uint32_t slot);
+/* TPC-C order lines packed in 4 bytes for the host link: i_id in bits 0..16,
+ * supply_w in bits 17..27, qty in bits 28..31 (so i_id < 2^17, supply_w <
+ * 2^11 and qty < 16, which TPC-C's 100,000 items, up to 2,047 warehouses and
+ * quantities 1..10 meet).  ltpg_tpcc_pack_lines packs n lines (host only; a
+ * line out of those ranges is LTPG_ERR_INVALID).  The packed upload and
+ * submit calls take the batch's records from b (b->lines is not read) and its
+ * lines from `packed`, and unpack them on the device on the context stream
+ * before the batch's kernels: half the lines' bytes on the link. */
+int ltpg_tpcc_pack_lines(const ltpg_tpcc_line *lines, uint64_t n, uint32_t *packed);
+int ltpg_batch_upload_tpcc_packed(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, const uint32_t *packed);
+int ltpg_submit_tpcc_packed_host(ltpg_ctx *ctx, uint32_t slot, const ltpg_tpcc_batch *b, const uint32_t *packed,
+                                 int mode, uint32_t *host_bitmap);
 /* The same pipeline with the batch made on the GPU: generator g's batch
  * batch_id (in order for TPC-C) is generated into `slot` on the copy stream,
  * so it overlaps the kernels of the batches before it, then run and its

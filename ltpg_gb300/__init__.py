@@ -126,19 +126,31 @@ class TpccBatch:
                           ("b", "<u4"), ("c", "<u4"), ("line_off", "<u4")])
     LINE_DTYPE = np.dtype([("i_id", "<u4"), ("supply_w", "<u2"), ("qty", "<u2")])
 
-    def __init__(self, txns, lines, txn_base=0):
+    def __init__(self, txns, lines, txn_base=0, packed=None):
+        """packed (with lines None): the order lines in the 4-byte form of
+        ltpg_tpcc_pack_lines, unpacked on the device by the packed calls."""
         self.txns = np.ascontiguousarray(txns, dtype=self.TXN_DTYPE)
-        self.lines = np.ascontiguousarray(lines, dtype=self.LINE_DTYPE)
+        self.packed = None if packed is None else np.ascontiguousarray(packed, dtype=np.uint32)
+        self.lines = np.ascontiguousarray(np.empty(0, dtype=self.LINE_DTYPE) if lines is None else lines,
+                                          dtype=self.LINE_DTYPE)
         self.n_txn = len(self.txns)
-        self.n_lines = len(self.lines)
+        self.n_lines = len(self.packed) if lines is None and self.packed is not None else len(self.lines)
         self.txn_base = int(txn_base)
 
     def as_c(self):
         return abi.TpccBatchC(self.n_txn, self.n_lines, self.txn_base, self.txns.ctypes.data,
-                              self.lines.ctypes.data if self.n_lines else None)
+                              self.lines.ctypes.data if len(self.lines) else None)
+
+    def with_packed_lines(self):
+        """The same batch with its order lines packed in 4 bytes (ltpg_tpcc_pack_lines)."""
+        p = np.empty(max(self.n_lines, 1), dtype=np.uint32)
+        r = lib().ltpg_tpcc_pack_lines(self.lines.ctypes.data if self.n_lines else None, self.n_lines, _p(p))
+        if r:
+            raise LtpgError(r, "an order line does not fit the packed form")
+        return TpccBatch(self.txns, None, self.txn_base, packed=p[:self.n_lines])
 
     def nbytes(self):
-        return self.n_txn * 32 + self.n_lines * 8
+        return self.n_txn * 32 + self.n_lines * (4 if self.packed is not None else 8)
 
 
 def pinned_copy(batch):
@@ -159,6 +171,8 @@ def pinned_copy(batch):
     if isinstance(batch, YcsbBatch):
         return YcsbBatch(pin(batch.ops), None if batch.val_off is None else pin(batch.val_off), pin(batch.vals),
                          batch.n_txn, batch.ops_per_txn)
+    if batch.packed is not None:
+        return TpccBatch(pin(batch.txns), None, batch.txn_base, packed=pin(batch.packed))
     return TpccBatch(pin(batch.txns), pin(batch.lines), batch.txn_base)
 
 
@@ -316,6 +330,8 @@ class Engine:
         cb = batch.as_c()
         if isinstance(batch, YcsbBatch):
             self._ck(lib().ltpg_batch_upload_ycsb(self._h, slot, C.byref(cb)))
+        elif batch.packed is not None:
+            self._ck(lib().ltpg_batch_upload_tpcc_packed(self._h, slot, C.byref(cb), _p(batch.packed)))
         else:
             self._ck(lib().ltpg_batch_upload_tpcc(self._h, slot, C.byref(cb)))
 
@@ -401,6 +417,8 @@ class Engine:
         m = MODES[mode] if isinstance(mode, str) else mode
         if isinstance(batch, YcsbBatch):
             self._ck(lib().ltpg_submit_ycsb_host(self._h, slot, C.byref(cb), m, _p(bitmap)))
+        elif batch.packed is not None:
+            self._ck(lib().ltpg_submit_tpcc_packed_host(self._h, slot, C.byref(cb), _p(batch.packed), m, _p(bitmap)))
         else:
             self._ck(lib().ltpg_submit_tpcc_host(self._h, slot, C.byref(cb), m, _p(bitmap)))
 

@@ -141,6 +141,9 @@ SIGNATURES = {
     "ltpg_run_tpcc_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), C.c_int, P]),
     "ltpg_submit_ycsb_host": (C.c_int, [P, U32, C.POINTER(YcsbBatchC), C.c_int, P]),
     "ltpg_submit_tpcc_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), C.c_int, P]),
+    "ltpg_tpcc_pack_lines": (C.c_int, [P, U64, P]),
+    "ltpg_batch_upload_tpcc_packed": (C.c_int, [P, U32, C.POINTER(TpccBatchC), P]),
+    "ltpg_submit_tpcc_packed_host": (C.c_int, [P, U32, C.POINTER(TpccBatchC), P, C.c_int, P]),
     "ltpg_host_wait": (C.c_int, [P, U32]),
     "ltpg_commit_bitmap": (C.c_int, [P, U32, P, SZ]),
     "ltpg_txn_flags": (C.c_int, [P, U32, P, SZ]),

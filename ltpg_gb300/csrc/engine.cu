@@ -42,6 +42,7 @@ void free_slot(Slot &s) {
     dev_free(s.off_blocks);
     dev_free(s.txns);
     dev_free(s.lines);
+    dev_free(s.packed_lines);
     dev_free(s.dev_hdr);
     dev_free(s.flags);
     dev_free(s.bitmap);
@@ -440,18 +441,28 @@ int upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, cudaStream
     return LTPG_OK;
 }
 
-int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream_t st) {
+// packed: the order lines in the 4-byte form (b->lines unused), copied to the
+// slot's packed buffer; unpack_st: the stream that unpacks them (null: left to
+// the caller).
+int upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, cudaStream_t st,
+                const uint32_t *packed = nullptr, cudaStream_t unpack_st = nullptr) {
     if (!c || !b) return c ? fail(c, LTPG_ERR_INVALID, "bad slot or batch") : LTPG_ERR_INVALID;
-    if (!b->txns || (b->n_lines && !b->lines)) return fail(c, LTPG_ERR_INVALID, "null batch array");
+    if (!b->txns || (b->n_lines && !b->lines && !packed)) return fail(c, LTPG_ERR_INVALID, "null batch array");
     Slot *s = nullptr;
     int r = slot_prepare_tpcc(c, slot, b->n_txn, b->n_lines, b->txn_base, &s);
     if (r) return r;
     CK(cudaMemcpyAsync(s->txns, b->txns, (uint64_t)b->n_txn * sizeof(ltpg_tpcc_txn), cudaMemcpyHostToDevice, st),
        "upload txns");
-    if (b->n_lines)
+    if (b->n_lines && packed) {
+        if (!s->packed_lines) CK(dev_alloc(&s->packed_lines, s->cap_lines + 1), "alloc packed lines");
+        CK(cudaMemcpyAsync(s->packed_lines, packed, (uint64_t)b->n_lines * 4, cudaMemcpyHostToDevice, st),
+           "upload packed lines");
+        if (unpack_st) CK(tpcc_unpack_lines(*s, unpack_st), "unpack lines");
+    } else if (b->n_lines) {
         CK(cudaMemcpyAsync(s->lines, b->lines, (uint64_t)b->n_lines * sizeof(ltpg_tpcc_line),
                            cudaMemcpyHostToDevice, st),
            "upload lines");
+    }
     s->host_hdr[0] = b->n_lines;
     s->host_hdr[1] = b->txn_base;
     // pageable source: the runtime stages it before returning, so the next
@@ -469,6 +480,20 @@ int ltpg_batch_upload_ycsb(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b)
 }
 int ltpg_batch_upload_tpcc(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b) {
     return c ? upload_tpcc(c, slot, b, c->stream) : LTPG_ERR_INVALID;
+}
+int ltpg_batch_upload_tpcc_packed(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, const uint32_t *packed) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (b && b->n_lines && !packed) return fail(c, LTPG_ERR_INVALID, "null packed lines");
+    return upload_tpcc(c, slot, b, c->stream, packed, c->stream);
+}
+int ltpg_tpcc_pack_lines(const ltpg_tpcc_line *lines, uint64_t n, uint32_t *packed) {
+    if (n && (!lines || !packed)) return LTPG_ERR_INVALID;
+    for (uint64_t i = 0; i < n; ++i) {
+        const ltpg_tpcc_line &l = lines[i];
+        if (l.i_id >= (1u << 17) || l.supply_w >= (1u << 11) || l.qty >= 16u) return LTPG_ERR_INVALID;
+        packed[i] = l.i_id | ((uint32_t)l.supply_w << 17) | ((uint32_t)l.qty << 28);
+    }
+    return LTPG_OK;
 }
 
 }  // extern "C"
@@ -629,7 +654,8 @@ namespace {
 // done (a batch uploaded without them): kernels on the copy stream would wait
 // there for SMs held by the previous batch and hold up the next copy.
 template <class Up>
-int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up upload, bool derive = false) {
+int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up upload, bool derive = false,
+                bool unpack = false) {
     Slot *s = get_slot(c, slot);
     if (!s) return c ? fail(c, LTPG_ERR_INVALID, "bad slot") : LTPG_ERR_INVALID;
     if (!c->copy_stream) CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "create copy stream");
@@ -644,6 +670,7 @@ int submit_host(ltpg_ctx *c, uint32_t slot, int mode, uint32_t *host_bitmap, Up 
     CK(cudaEventRecord(s->copied, c->copy_stream), "record copy");
     CK(cudaStreamWaitEvent(c->stream, s->copied, 0), "wait for the copy");
     if (derive) CK(ycsb_derive_offsets(c, *s, c->stream), "value offsets");
+    if (unpack) CK(tpcc_unpack_lines(*s, c->stream), "unpack lines");
     r = ltpg_run_batch(c, slot, mode);
     if (r) return r;
     if (host_bitmap)
@@ -666,6 +693,15 @@ int ltpg_submit_ycsb_host(ltpg_ctx *c, uint32_t slot, const ltpg_ycsb_batch *b, 
 int ltpg_submit_tpcc_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, int mode, uint32_t *host_bitmap) {
     if (!c) return LTPG_ERR_INVALID;
     return submit_host(c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_tpcc(c, slot, b, st); });
+}
+
+int ltpg_submit_tpcc_packed_host(ltpg_ctx *c, uint32_t slot, const ltpg_tpcc_batch *b, const uint32_t *packed,
+                                 int mode, uint32_t *host_bitmap) {
+    if (!c) return LTPG_ERR_INVALID;
+    if (b && b->n_lines && !packed) return fail(c, LTPG_ERR_INVALID, "null packed lines");
+    return submit_host(
+        c, slot, mode, host_bitmap, [&](cudaStream_t st) { return upload_tpcc(c, slot, b, st, packed, nullptr); },
+        false, b && b->n_lines != 0);
 }
 
 int ltpg_submit_generated(ltpg_ctx *c, ltpg_gen *g, uint64_t batch_id, uint32_t slot, int mode,

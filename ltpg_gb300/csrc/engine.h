@@ -94,6 +94,7 @@ struct Slot {
     uint64_t txn_base = 0;
     ltpg_tpcc_txn *txns = nullptr;
     ltpg_tpcc_line *lines = nullptr;
+    uint32_t *packed_lines = nullptr;  // packed uploads land here before their unpacking
     // {n_lines, txn_base} of the batch in the slot, read by the kernels from
     // device memory so a captured graph stays valid when a new batch is
     // uploaded into the slot.
@@ -205,6 +206,8 @@ cudaError_t ycsb_phase(ltpg_ctx *c, Slot &s, int phase);      // 0 exec, 1 check
 // Value offsets of the batch in s made on the device from its op words (the
 // upload of a batch without val_off), on stream st.
 cudaError_t ycsb_derive_offsets(ltpg_ctx *c, Slot &s, cudaStream_t st);
+// Unpacks the slot's packed order lines into its lines, on stream st.
+cudaError_t tpcc_unpack_lines(Slot &s, cudaStream_t st);
 cudaError_t ycsb_run_tuned(ltpg_ctx *c, Slot &s, int mode);   // fused / persistent
 cudaError_t tpcc_init_tables(ltpg_ctx *c);
 cudaError_t tpcc_build_name_index(ltpg_ctx *c);

@@ -968,4 +968,23 @@ cudaError_t tpcc_run_tuned(ltpg_ctx *c, Slot &s, int mode) {
     }
 }
 
+// Packed order lines (ltpg_tpcc_pack_lines) back to ltpg_tpcc_line: one
+// 4-byte load and one 8-byte store per line.
+__global__ void __launch_bounds__(256) tpcc_unpack_lines_kernel(const uint32_t *__restrict__ packed, uint64_t n,
+                                                                 ltpg_tpcc_line *__restrict__ lines) {
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+        const uint32_t p = __ldg(packed + i);
+        reinterpret_cast<uint2 *>(lines)[i] = make_uint2(p & 0x1FFFFu, ((p >> 17) & 0x7FFu) | ((p >> 28) << 16));
+    }
+}
+
+cudaError_t tpcc_unpack_lines(Slot &s, cudaStream_t st) {
+    const uint64_t n = s.n_lines;
+    if (!n) return cudaSuccess;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((n + 255) / 256, 4096);
+    tpcc_unpack_lines_kernel<<<grid, 256, 0, st>>>(s.packed_lines, n, s.lines);
+    return cudaGetLastError();
+}
+
 }  // namespace ltpg
