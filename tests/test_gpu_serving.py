@@ -122,12 +122,16 @@ def test_admission_by_memory_budget():
         y.close()
 
 
-def test_caller_requests_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("ycsb_late,mode", [(0, "fused"), (3, "graph")])
+def test_caller_requests_same_alone_and_in_the_mix(ycsb_late, mode):
     """Caller-owned requests through ltpg_serve_submit / ltpg_serve_poll: two
     request sources (a TPC-C client and a YCSB client, interleaved by one
     driving thread) submit in chunks of varying size with polls in between;
     results come back by id.  Replaying each logged batch alone, in order, on
-    fresh engines gives every request's flags and result, and the tables."""
+    fresh engines gives every request's flags and result, and the tables.
+    Also with the YCSB engine on write-first registration (late_reads 3, the
+    update list) in graph mode, where every batch size is a new graph; there
+    an aborted YCSB request's result is 0."""
     rng = np.random.default_rng(5)
     nc, ny = 12000, 15000
     ctx, clines, coff = _tpcc_pool(nc)
@@ -149,10 +153,11 @@ def test_caller_requests_same_alone_and_in_the_mix():
             kind_idx.append((1, iy))
             iy += 1
     c, y = _engines()
+    y.set_launch("ycsb", late_reads=ycsb_late)
     flags = np.zeros(len(reqs), dtype=np.uint8)
     results = np.zeros(len(reqs), dtype=np.int64)
     try:
-        srv = L.Server(c, y, max_batch=3000, deadline_ms=0.3, mode="fused", slots=3, ycsb_ops=YP["ops_per_txn"])
+        srv = L.Server(c, y, max_batch=3000, deadline_ms=0.3, mode=mode, slots=3, ycsb_ops=YP["ops_per_txn"])
         pos, got = 0, 0
         while pos < len(reqs):
             k = int(rng.integers(1, 700))
@@ -211,7 +216,10 @@ def test_caller_requests_same_alone_and_in_the_mix():
                 y.run_batch(0, "plain")
                 y.sync()
                 assert np.array_equal(y.txn_flags(0, len(yi)), flags[pos_y])
-                assert np.array_equal(y.txn_results(0, len(yi)), results[pos_y])
+                want = y.txn_results(0, len(yi))
+                if ycsb_late:
+                    want = np.where((flags[pos_y] & abi.FLAG_COMMIT) != 0, want, 0)
+                assert np.array_equal(want, results[pos_y])
         for t in range(abi.TPCC_TABLES):
             assert np.array_equal(c.download_table(t), mix_tables[t]), t
         assert np.array_equal(y.download_table(abi.TABLE_YCSB), mix_ycsb)
