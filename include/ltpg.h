@@ -483,7 +483,8 @@ typedef struct {
     uint64_t seed;
     uint32_t max_batch;     /* batch closing size (262,144)              */
     uint32_t tpcc_pct;      /* share of TPC-C requests (70)              */
-    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT      */
+    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT (GRAPH
+                               captures a graph per batch size)          */
     uint32_t slots;         /* batches in flight (<= engine slots)       */
 } ltpg_serve_cfg;
 typedef struct {
@@ -519,7 +520,9 @@ typedef struct {
     double deadline_ms;     /* batch closing deadline (2.0)                          */
     uint64_t budget_bytes;  /* registration tables + batch buffers in flight, 0 = none */
     uint32_t max_batch;     /* batch closing size (<= both engines' max_txn)         */
-    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT                  */
+    uint32_t mode;          /* LTPG_MODE_PLAIN / FUSED / PERSISTENT; GRAPH is
+                               accepted but captures a graph per batch size, and
+                               served batches vary in size                       */
     uint32_t slots;         /* batches in flight (<= the engines' slots)             */
     uint32_t ycsb_ops;      /* op words per YCSB transaction of a batch (<= the YCSB
                                engine's max_ops_per_txn); shorter requests are
