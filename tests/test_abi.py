@@ -58,6 +58,12 @@ def test_invalid_arguments_rejected(built_lib):
     assert L.ltpg_gen_create_ycsb(C.byref(p), C.byref(h)) == abi.ERR_INVALID
     q = abi.TpccParamsC(1, 0, 10, 50, 1, 15)  # no warehouses
     assert L.ltpg_gen_create_tpcc(C.byref(q), C.byref(h)) == abi.ERR_INVALID
+    # packed order lines: host packing needs its arrays unless there is nothing to pack
+    assert L.ltpg_tpcc_pack_lines(None, 5, None) == abi.ERR_INVALID
+    assert L.ltpg_tpcc_pack_lines(None, 0, None) == 0
+    b = abi.TpccBatchC(1, 0, 0, None, None)
+    assert L.ltpg_batch_upload_tpcc_packed(None, 0, C.byref(b), None) == abi.ERR_INVALID
+    assert L.ltpg_submit_tpcc_packed_host(None, 0, C.byref(b), None, 0, None) == abi.ERR_INVALID
 
 
 STRUCTS = {"YcsbBatchC": "ltpg_ycsb_batch", "YcsbParamsC": "ltpg_ycsb_params", "TpccBatchC": "ltpg_tpcc_batch",
