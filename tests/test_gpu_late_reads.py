@@ -247,3 +247,18 @@ def test_value_offsets_that_disagree_with_the_ops_report_error(eng, late, mode):
         eng.load_ycsb(58, n)
         _late_same(eng, o, good, 0, mode)
     assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
+
+
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_write_first_persistent_every_block_size(eng, block):
+    """The persistent write-first kernel: blocks of up to 256 threads run the
+    form budgeted for six resident blocks per SM, 512-thread blocks the
+    general one; both bit-exact against the oracle across batches."""
+    n = 30000
+    eng.load_ycsb(59, n)
+    o = oracle.YcsbOracle(59, n)
+    g = YcsbGenerator(59, n, 9000, 16, 10, 0.99)
+    with _late(eng, 3, block_threads=block):
+        for bid in range(3):
+            _late_same(eng, o, g.batch(bid), bid % 2, "persistent")
+    assert np.array_equal(eng.download_table(abi.TABLE_YCSB), o.rows)
