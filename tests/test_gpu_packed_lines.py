@@ -72,3 +72,20 @@ def test_pipelined_packed_host_calls(eng):
         assert np.array_equal(bits[i % 3], o.run(batches[i])[1])
     for t in range(abi.TPCC_TABLES):
         assert np.array_equal(eng.download_table(t), o.tables[t])
+
+
+def test_packed_upload_five_kind_mix(eng):
+    """The five-transaction mix (customers by last name too) with packed lines,
+    fused and graph, against the oracle."""
+    eng.load_tpcc(24, 4)
+    o = oracle.TpccOracle(24, 4)
+    g = TpccGenerator(24, 4, 6000, neworder_pct=45, orderstatus_pct=4, delivery_pct=4, stocklevel_pct=4,
+                      by_name_pct=60)
+    for bid, mode in enumerate(["fused", "graph", "persistent"]):
+        b = g.next()
+        eng.upload(bid % 2, b.with_packed_lines())
+        eng.run_batch(bid % 2, mode)
+        eng.sync()
+        _same(eng, o, b, bid % 2)
+    for t in range(abi.TPCC_TABLES):
+        assert np.array_equal(eng.download_table(t), o.tables[t])
